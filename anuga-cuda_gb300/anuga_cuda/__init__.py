@@ -1,0 +1,20 @@
+"""anuga_cuda -- ANUGA's explicit shallow-water evolve step on one GB300.
+
+Drop-in for the reference's ``anuga_cuda.GPU_domain`` path: a domain object
+with ANUGA's method names whose per-step work runs as hand-written sm_103a
+CUDA kernels in libswgpu.so (C ABI in include/swgpu.h), called through
+ctypes.  There is no CPU implementation in this package.
+"""
+from ._build import build, library_path
+from .boundaries import Dirichlet_boundary, Reflective_boundary, Time_stage_sine_boundary
+from .config import DEFAULT, Parameters
+from .gpu_domain import GPU_domain, Quantity
+from .mesh import Mesh, morton_order, rectangular_cross
+
+CUDA_advanced_domain = GPU_domain
+
+__all__ = [
+    "GPU_domain", "CUDA_advanced_domain", "Quantity", "Mesh", "rectangular_cross",
+    "morton_order", "Parameters", "DEFAULT", "Reflective_boundary", "Dirichlet_boundary",
+    "Time_stage_sine_boundary", "build", "library_path",
+]

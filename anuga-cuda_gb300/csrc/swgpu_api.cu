@@ -1,0 +1,1035 @@
+// swgpu_api.cu -- the C ABI of libswgpu.so (declared in include/swgpu.h):
+// device allocation and upload of a mesh, quantity transfer, the
+// per-method entry points that mirror the reference's Domain overrides,
+// and the device-resident evolve loop (CUDA graphs of several Euler steps,
+// host synchronisation only between graphs).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "swgpu_handle.cuh"
+
+namespace swgpu {
+
+static thread_local std::string g_create_error;
+
+static int fail(Handle *h, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h)
+        h->err = buf;
+    else
+        g_create_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? SWGPU_ENOMEM : SWGPU_ECUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__,       \
+                        __LINE__);                                                       \
+    } while (0)
+
+template <typename T>
+static int dalloc(Handle *h, T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc((void **)p, count * sizeof(T)));
+    h->allocs.push_back((void *)*p);
+    CK(cudaMemsetAsync(*p, 0, count * sizeof(T), h->stream));
+    return SWGPU_OK;
+}
+
+template <typename T>
+static int upload(Handle *h, T *dst, const T *src, size_t count) {
+    if (count == 0) return SWGPU_OK;
+    CK(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+template <typename T>
+static int download(Handle *h, T *dst, const T *src, size_t count) {
+    if (count == 0) return SWGPU_OK;
+    CK(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+// AoS [3k+i] (or [6k+j]) host array -> planes [i*N+k]
+template <typename T, typename U>
+static std::vector<T> to_planes(const U *src, int64_t N, int width) {
+    std::vector<T> out((size_t)N * width);
+    for (int64_t k = 0; k < N; k++)
+        for (int j = 0; j < width; j++) out[(size_t)j * N + k] = (T)src[k * width + j];
+    return out;
+}
+
+static int check_launch(Handle *h, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return fail(h, SWGPU_ECUDA, "%s launch: %s", what, cudaGetErrorString(e));
+    return SWGPU_OK;
+}
+
+static int sync_ctrl(Handle *h) {
+    CK(cudaMemcpyAsync(h->h_ctrl, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+static int push_ctrl(Handle *h) {
+    CK(cudaMemcpyAsync(h->d_ctrl, h->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+static const char *status_text(int s) {
+    switch (s) {
+        case SWGPU_OK: return "ok";
+        case SWGPU_EINVAL: return "invalid argument";
+        case SWGPU_ECUDA: return "CUDA error";
+        case SWGPU_ENOMEM: return "out of device memory";
+        case SWGPU_EDENOMINATOR: return "semi-implicit update denominator <= 0";
+        case SWGPU_ESMALLSTEP: return "timestep below evolve_min_timestep even at first order";
+        case SWGPU_ENONFINITE: return "non-finite value reached the flux timestep";
+        case SWGPU_EBED: return "discontinuous elevation across an edge";
+        case SWGPU_EBOUNDARY: return "unknown boundary type";
+        case SWGPU_EOVERSHOOT: return "model time overshot finaltime";
+        case SWGPU_EMESH: return "inconsistent mesh";
+        default: return "unknown status";
+    }
+}
+
+// Device-side failures recorded in Ctrl.status become the call's status.
+static int device_status(Handle *h) {
+    if (h->h_ctrl->status != 0) {
+        const int s = h->h_ctrl->status;
+        return fail(h, s, "device reported: %s", status_text(s));
+    }
+    return SWGPU_OK;
+}
+
+static void fill_state(const Ctrl *c, swgpu_state *s) {
+    s->time = c->time;
+    s->yieldtime = c->yieldtime;
+    s->finaltime = c->finaltime;
+    s->timestep = c->timestep;
+    s->flux_timestep = c->flux_timestep;
+    s->recorded_max_timestep = c->rec_max;
+    s->recorded_min_timestep = c->rec_min;
+    s->order = c->order;
+    s->smallsteps = c->smallsteps;
+    s->number_of_steps = c->steps_since_yield;
+    s->total_steps = c->total_steps;
+    s->stop_reason = c->stop_reason;
+    s->status = c->status;
+}
+
+static void reset_ftmin(Ctrl *c, const DevParams &P) {
+    double m = P.evolve_max_timestep;
+    std::memcpy(&c->ftmin_bits, &m, sizeof m);
+}
+
+// ----------------------------------------------------------- step issue
+
+static int issue_fused_step(Handle *h) {
+    const int fused_flux = kFused;
+    const int fused_update = kFused | kFrictionInline;
+    const int fused_dist = kFused | kWriteBoundary;
+    if (h->precision == SWGPU_FP64) {
+        launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, fused_flux, h->stream);
+        launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, fused_update, h->stream);
+        launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl, fused_dist, h->stream);
+    } else {
+        launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, fused_flux, h->stream);
+        launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, fused_update, h->stream);
+        launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl, fused_dist,
+                                h->stream);
+    }
+    return check_launch(h, "evolve step");
+}
+
+static int build_graph(Handle *h) {
+    if (h->graph) return SWGPU_OK;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < kStepsPerGraph; s++) {
+        if (h->precision == SWGPU_FP64) {
+            launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, kFused, h->stream);
+            launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, kFused | kFrictionInline,
+                               h->stream);
+            launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,
+                                   kFused | kWriteBoundary, h->stream);
+        } else {
+            launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused, h->stream);
+            launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused | kFrictionInline,
+                                h->stream);
+            launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl,
+                                    kFused | kWriteBoundary, h->stream);
+        }
+    }
+    CK(cudaStreamEndCapture(h->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        h->graph = nullptr;
+        return fail(h, SWGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    return SWGPU_OK;
+}
+
+// distribute as the stand-alone method: protect + velocities, then the
+// extrapolation/balance pass with edge values materialised.
+static int issue_distribute(Handle *h, bool with_boundary) {
+    if (h->precision == SWGPU_FP64) {
+        launch_prepare_fp64(h->M, h->S, h->P, h->d_ctrl, h->stream);
+        launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,
+                               kWriteEdges | (with_boundary ? kWriteBoundary : 0), h->stream);
+    } else {
+        launch_prepare_mixed(h->M, h->S, h->X, h->P, h->mixed_from_stage ? 1 : 0, h->stream);
+        h->mixed_from_stage = false;
+        launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl,
+                                with_boundary ? kWriteBoundary : 0, h->stream);
+    }
+    h->vertices_stale = false;
+    return check_launch(h, "distribute");
+}
+
+}  // namespace swgpu
+
+using namespace swgpu;
+
+// ================================================================ C ABI ==
+
+extern "C" {
+
+const char *swgpu_last_error(void *handle) {
+    if (!handle) return g_create_error.c_str();
+    return static_cast<Handle *>(handle)->err.c_str();
+}
+
+int swgpu_device_info(char *buf, int buflen) {
+    Handle *h = nullptr;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    CK(cudaGetDeviceProperties(&p, dev));
+    if (buf && buflen > 0)
+        snprintf(buf, buflen, "%s sm_%d%d, %d SMs, %.1f GB (libswgpu %d)", p.name, p.major,
+                 p.minor, p.multiProcessorCount, p.totalGlobalMem / 1e9, SWGPU_ABI_VERSION);
+    return SWGPU_OK;
+}
+
+int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precision,
+                 void **handle_out) {
+    Handle *h = nullptr;
+    if (!mesh || !params || !handle_out) return fail(nullptr, SWGPU_EINVAL, "null argument");
+    *handle_out = nullptr;
+    if (precision != SWGPU_FP64 && precision != SWGPU_MIXED)
+        return fail(nullptr, SWGPU_EINVAL, "precision must be SWGPU_FP64 or SWGPU_MIXED");
+    const int64_t N = mesh->number_of_elements, Nb = mesh->number_of_boundary_elements;
+    if (N <= 0 || N >= (int64_t(1) << 29) || Nb < 0 || Nb > 3 * N)
+        return fail(nullptr, SWGPU_EINVAL, "bad sizes N=%lld Nb=%lld", (long long)N,
+                    (long long)Nb);
+    if (!mesh->neighbours || !mesh->neighbour_edges || !mesh->surrogate_neighbours ||
+        !mesh->number_of_boundaries || !mesh->normals || !mesh->edgelengths || !mesh->radii ||
+        !mesh->areas || !mesh->vertex_coordinates || !mesh->centroid_coordinates ||
+        (Nb > 0 && (!mesh->boundary_cells || !mesh->boundary_edges || !mesh->boundary_tag)))
+        return fail(nullptr, SWGPU_EINVAL, "null mesh array");
+
+    // ---- validate and pack the topology on the host
+    std::vector<int> nbr((size_t)3 * N), surr((size_t)3 * N);
+    std::vector<uint8_t> nb((size_t)N), order((size_t)N), full((size_t)N);
+    int64_t maxtag = -1;
+    for (int64_t m = 0; m < Nb; m++) {
+        const int64_t c = mesh->boundary_cells[m], e = mesh->boundary_edges[m],
+                      t = mesh->boundary_tag[m];
+        if (c < 0 || c >= N || e < 0 || e > 2 || t < 0 || t > 1000000)
+            return fail(nullptr, SWGPU_EMESH, "boundary slot %lld out of range", (long long)m);
+        if (mesh->neighbours[3 * c + e] != -m - 1)
+            return fail(nullptr, SWGPU_EMESH,
+                        "boundary slot %lld: neighbours[%lld,%lld] is not -%lld-1", (long long)m,
+                        (long long)c, (long long)e, (long long)m);
+        maxtag = std::max(maxtag, t);
+    }
+    for (int64_t k = 0; k < N; k++) {
+        int nbc = 0;
+        for (int i = 0; i < 3; i++) {
+            const int64_t n = mesh->neighbours[3 * k + i];
+            const int64_t s = mesh->surrogate_neighbours[3 * k + i];
+            if (s < 0 || s >= N)
+                return fail(nullptr, SWGPU_EMESH, "surrogate neighbour of %lld out of range",
+                            (long long)k);
+            surr[(size_t)i * N + k] = (int)s;
+            if (n >= 0) {
+                const int64_t m = mesh->neighbour_edges[3 * k + i];
+                if (n >= N || m < 0 || m > 2 || mesh->neighbours[3 * n + m] != k)
+                    return fail(nullptr, SWGPU_EMESH,
+                                "neighbour %lld of triangle %lld edge %d is inconsistent",
+                                (long long)n, (long long)k, i);
+                nbr[(size_t)i * N + k] = pack_neighbour((int)n, (int)m);
+            } else {
+                if (-n - 1 >= Nb)
+                    return fail(nullptr, SWGPU_EMESH, "boundary index of %lld out of range",
+                                (long long)k);
+                nbr[(size_t)i * N + k] = (int)n;
+                nbc++;
+            }
+        }
+        if (mesh->number_of_boundaries[k] != nbc)
+            return fail(nullptr, SWGPU_EMESH, "number_of_boundaries[%lld] != %d", (long long)k,
+                        nbc);
+        nb[k] = (uint8_t)nbc;
+        full[k] = mesh->tri_full_flag ? (mesh->tri_full_flag[k] == 1) : 1;
+        // ANUGA's summation order for triangle k: edges to lower-index
+        // neighbours by neighbour index, then the other edges by index
+        int idx[3] = {0, 1, 2}, cnt = 0, perm[3];
+        for (int i = 0; i < 3; i++) {
+            const int64_t n = mesh->neighbours[3 * k + i];
+            if (n >= 0 && n < k) perm[cnt++] = i;
+        }
+        std::sort(perm, perm + cnt, [&](int a, int b) {
+            return mesh->neighbours[3 * k + a] < mesh->neighbours[3 * k + b];
+        });
+        for (int i = 0; i < 3; i++) {
+            const int64_t n = mesh->neighbours[3 * k + i];
+            if (!(n >= 0 && n < k)) perm[cnt++] = idx[i];
+        }
+        order[k] = (uint8_t)(perm[0] | (perm[1] << 2) | (perm[2] << 4));
+    }
+
+    h = new Handle();
+    h->precision = precision;
+    int rc;
+    {
+        cudaError_t e = cudaGetDevice(&h->device);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            fail(nullptr, SWGPU_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
+            delete h;
+            return SWGPU_ECUDA;
+        }
+    }
+#define TRY(x)                                      \
+    do {                                            \
+        rc = (x);                                   \
+        if (rc) {                                   \
+            g_create_error = h->err;                \
+            swgpu_destroy(h);                       \
+            return rc;                              \
+        }                                           \
+    } while (0)
+
+    const size_t n1 = N, n3 = 3 * N, n6 = 6 * N, nb1 = Nb;
+    DevMesh &M = h->M;
+    M.N = (int)N;
+    M.Nb = (int)Nb;
+    int *d_nbr, *d_surr, *d_bcell, *d_bedge, *d_btag;
+    uint8_t *d_nb, *d_order, *d_full;
+    double *d_normals, *d_len, *d_radii, *d_areas, *d_vxy, *d_cxy;
+    TRY(dalloc(h, &d_nbr, n3));
+    TRY(dalloc(h, &d_surr, n3));
+    TRY(dalloc(h, &d_nb, n1));
+    TRY(dalloc(h, &d_order, n1));
+    TRY(dalloc(h, &d_full, n1));
+    TRY(dalloc(h, &d_normals, n6));
+    TRY(dalloc(h, &d_len, n3));
+    TRY(dalloc(h, &d_radii, n1));
+    TRY(dalloc(h, &d_areas, n1));
+    TRY(dalloc(h, &d_vxy, n6));
+    TRY(dalloc(h, &d_cxy, 2 * n1));
+    TRY(dalloc(h, &d_bcell, nb1));
+    TRY(dalloc(h, &d_bedge, nb1));
+    TRY(dalloc(h, &d_btag, nb1));
+    TRY(upload(h, d_nbr, nbr.data(), n3));
+    TRY(upload(h, d_surr, surr.data(), n3));
+    TRY(upload(h, d_nb, nb.data(), n1));
+    TRY(upload(h, d_order, order.data(), n1));
+    TRY(upload(h, d_full, full.data(), n1));
+    h->h_normals = to_planes<double>(mesh->normals, N, 6);
+    h->h_len = to_planes<double>(mesh->edgelengths, N, 3);
+    h->h_vxy = to_planes<double>(mesh->vertex_coordinates, N, 6);
+    h->h_cxy = to_planes<double>(mesh->centroid_coordinates, N, 2);
+    h->h_areas.assign(mesh->areas, mesh->areas + N);
+    h->h_radii.assign(mesh->radii, mesh->radii + N);
+    h->h_nbr = nbr;
+    h->h_surr = surr;
+    h->h_nb = nb;
+    TRY(upload(h, d_normals, h->h_normals.data(), n6));
+    TRY(upload(h, d_len, h->h_len.data(), n3));
+    TRY(upload(h, d_radii, mesh->radii, n1));
+    TRY(upload(h, d_areas, mesh->areas, n1));
+    TRY(upload(h, d_vxy, h->h_vxy.data(), n6));
+    TRY(upload(h, d_cxy, h->h_cxy.data(), 2 * n1));
+    if (Nb > 0) {
+        std::vector<int> bc(Nb), be(Nb), bt(Nb);
+        for (int64_t m = 0; m < Nb; m++) {
+            bc[m] = (int)mesh->boundary_cells[m];
+            be[m] = (int)mesh->boundary_edges[m];
+            bt[m] = (int)mesh->boundary_tag[m];
+        }
+        TRY(upload(h, d_bcell, bc.data(), nb1));
+        TRY(upload(h, d_bedge, be.data(), nb1));
+        TRY(upload(h, d_btag, bt.data(), nb1));
+    }
+    M.nbr = d_nbr;
+    M.surr = d_surr;
+    M.nb = d_nb;
+    M.order = d_order;
+    M.full = d_full;
+    M.normals = d_normals;
+    M.len = d_len;
+    M.radii = d_radii;
+    M.areas = d_areas;
+    M.vxy = d_vxy;
+    M.cxy = d_cxy;
+    M.bcell = d_bcell;
+    M.bedge = d_bedge;
+    M.btag = d_btag;
+
+    // ---- quantities
+    DevState &S = h->S;
+    TRY(dalloc(h, &S.w, n1));
+    TRY(dalloc(h, &S.uh, n1));
+    TRY(dalloc(h, &S.vh, n1));
+    TRY(dalloc(h, &S.zc, n1));
+    TRY(dalloc(h, &S.fric, n1));
+    TRY(dalloc(h, &S.uvel, n1));
+    TRY(dalloc(h, &S.vvel, n1));
+    TRY(dalloc(h, &S.zv, n3));
+    TRY(dalloc(h, &S.ze, n3));
+    TRY(dalloc(h, &S.wb, nb1));
+    TRY(dalloc(h, &S.uhb, nb1));
+    TRY(dalloc(h, &S.vhb, nb1));
+    TRY(dalloc(h, &S.zb, nb1));
+    TRY(dalloc(h, &S.hc, n1));
+    TRY(dalloc(h, &S.uc, n1));
+    TRY(dalloc(h, &S.vc, n1));
+    TRY(dalloc(h, &S.hb, nb1));
+    TRY(dalloc(h, &S.ub, nb1));
+    TRY(dalloc(h, &S.vb, nb1));
+    TRY(dalloc(h, &S.partials, (size_t)grid_for((int)N) + 1));
+    TRY(dalloc(h, &S.we, n3));
+    TRY(dalloc(h, &S.uhe, n3));
+    TRY(dalloc(h, &S.vhe, n3));
+    if (precision == SWGPU_FP64) {
+        TRY(dalloc(h, &S.wv, n3));
+        TRY(dalloc(h, &S.uhv, n3));
+        TRY(dalloc(h, &S.vhv, n3));
+        TRY(dalloc(h, &S.ew, n1));
+        TRY(dalloc(h, &S.euh, n1));
+        TRY(dalloc(h, &S.evh, n1));
+        TRY(dalloc(h, &S.suh, n1));
+        TRY(dalloc(h, &S.svh, n1));
+        TRY(dalloc(h, &S.max_speed, n1));
+    } else {
+        DevMixed &X = h->X;
+        TRY(dalloc(h, &X.hd, n1));
+        TRY(dalloc(h, &X.hf, n1));
+        TRY(dalloc(h, &X.uvel, n1));
+        TRY(dalloc(h, &X.vvel, n1));
+        TRY(dalloc(h, &X.hv, n3));
+        TRY(dalloc(h, &X.uhv, n3));
+        TRY(dalloc(h, &X.vhv, n3));
+        TRY(dalloc(h, &X.hbf, nb1));
+        TRY(dalloc(h, &X.uhbf, nb1));
+        TRY(dalloc(h, &X.vhbf, nb1));
+        TRY(dalloc(h, &X.ew, n1));
+        TRY(dalloc(h, &X.euh, n1));
+        TRY(dalloc(h, &X.evh, n1));
+        TRY(dalloc(h, &X.nx, n3));
+        TRY(dalloc(h, &X.ny, n3));
+        TRY(dalloc(h, &X.len, n3));
+        TRY(dalloc(h, &X.inv_area, n1));
+        TRY(dalloc(h, &X.radius, n1));
+        TRY(dalloc(h, &X.gc, n6));
+        TRY(dalloc(h, &X.dzn, n3));
+        TRY(dalloc(h, &X.dzv, n3));
+        TRY(dalloc(h, &X.zgrad, 2 * n1));
+        TRY(dalloc(h, &X.fric, n1));
+        TRY(dalloc(h, &X.zmoff, n1));
+        TRY(dalloc(h, &X.kind, n1));
+        // FP64 vertex planes are kept for downloads (stage = depth + bed)
+        TRY(dalloc(h, &S.wv, n3));
+        TRY(dalloc(h, &S.uhv, n3));
+        TRY(dalloc(h, &S.vhv, n3));
+    }
+
+    // ---- parameters, boundary tags, control block
+    DevParams &P = h->P;
+    P.g = params->g;
+    P.epsilon = params->epsilon;
+    P.H0 = params->H0;
+    P.minimum_allowed_height = params->minimum_allowed_height;
+    P.maximum_allowed_speed = params->maximum_allowed_speed;
+    P.beta_w = params->beta_w;
+    P.beta_w_dry = params->beta_w_dry;
+    P.beta_uh = params->beta_uh;
+    P.beta_uh_dry = params->beta_uh_dry;
+    P.beta_vh = params->beta_vh;
+    P.beta_vh_dry = params->beta_vh_dry;
+    P.alpha_balance = params->alpha_balance;
+    P.CFL = params->CFL;
+    P.evolve_max_timestep = params->evolve_max_timestep;
+    P.evolve_min_timestep = params->evolve_min_timestep;
+    P.tight_slope_limiters = (int)params->tight_slope_limiters;
+    P.use_centroid_velocities = (int)params->use_centroid_velocities;
+    P.optimise_dry_cells = (int)params->optimise_dry_cells;
+    P.extrapolate_velocity_second_order = (int)params->extrapolate_velocity_second_order;
+    P.use_sloped_mannings = (int)params->use_sloped_mannings;
+    P.max_smallsteps = (int)params->max_smallsteps;
+    P.default_order = (int)params->default_order;
+    if (!(P.evolve_max_timestep > 0) || (P.default_order != 1 && P.default_order != 2)) {
+        fail(h, SWGPU_EINVAL, "evolve_max_timestep must be > 0 and default_order 1 or 2");
+        g_create_error = h->err;
+        swgpu_destroy(h);
+        return SWGPU_EINVAL;
+    }
+
+    h->ntags = (int)(maxtag + 1);
+    TRY(dalloc(h, &h->d_tags, (size_t)std::max(h->ntags, 1)));  // zero = reflective
+    TRY(dalloc(h, &h->d_ctrl, 1));
+    TRY(dalloc(h, &h->d_scalar, 4));
+    {
+        cudaError_t e = cudaMallocHost((void **)&h->h_ctrl, sizeof(Ctrl));
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_scalar, 4 * sizeof(double));
+        if (e != cudaSuccess) {
+            fail(h, SWGPU_ENOMEM, "pinned host allocation: %s", cudaGetErrorString(e));
+            g_create_error = h->err;
+            swgpu_destroy(h);
+            return SWGPU_ENOMEM;
+        }
+    }
+    std::memset(h->h_ctrl, 0, sizeof(Ctrl));
+    Ctrl *c = h->h_ctrl;
+    c->order = P.default_order;
+    c->finaltime = -1.0;
+    c->yieldtime = 1.0e300;
+    c->yieldstep = 1.0e300;
+    c->time_epsilon = params->epsilon;
+    c->rec_max = P.evolve_min_timestep;
+    c->rec_min = P.evolve_max_timestep;
+    c->budget = -1;
+    reset_ftmin(c, P);
+    TRY(push_ctrl(h));
+    if (precision == SWGPU_MIXED) TRY(build_mixed_geometry(h) ? fail(h, SWGPU_ECUDA, "mixed geometry upload") : SWGPU_OK);
+    *handle_out = h;
+#undef TRY
+    return SWGPU_OK;
+}
+
+int swgpu_destroy(void *handle) {
+    if (!handle) return SWGPU_OK;
+    Handle *h = static_cast<Handle *>(handle);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
+    if (h->h_scalar) cudaFreeHost(h->h_scalar);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SWGPU_OK;
+}
+
+int swgpu_set_boundary_tags(void *handle, const swgpu_boundary_tag *tags, int ntags) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || (!tags && ntags > 0)) return fail(h, SWGPU_EINVAL, "null argument");
+    if (ntags < h->ntags)
+        return fail(h, SWGPU_EINVAL, "mesh uses %d boundary tags, %d given", h->ntags, ntags);
+    std::vector<BcTag> t((size_t)ntags);
+    for (int i = 0; i < ntags; i++) {
+        if (tags[i].type < SWGPU_BC_REFLECTIVE || tags[i].type > SWGPU_BC_TIME_STAGE_SINE)
+            return fail(h, SWGPU_EBOUNDARY, "tag %d: unknown boundary type %lld", i,
+                        (long long)tags[i].type);
+        if (tags[i].type == SWGPU_BC_TIME_STAGE_SINE && !(tags[i].p[2] != 0.0))
+            return fail(h, SWGPU_EINVAL, "tag %d: sine boundary needs a nonzero period", i);
+        t[i].type = (int)tags[i].type;
+        for (int j = 0; j < 4; j++) t[i].p[j] = tags[i].p[j];
+    }
+    const int n = std::max(h->ntags, 1);
+    return upload(h, h->d_tags, t.data(), (size_t)std::min(ntags, n));
+}
+
+int swgpu_set_quantity(void *handle, int q, const double *centroid, const double *vertex,
+                       const double *edge) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !centroid) return fail(h, SWGPU_EINVAL, "null argument");
+    const int64_t N = h->M.N;
+    DevState &S = h->S;
+    double *c = nullptr, *v = nullptr, *e = nullptr;
+    switch (q) {
+        case SWGPU_STAGE: c = S.w; v = S.wv; e = S.we; break;
+        case SWGPU_XMOMENTUM: c = S.uh; v = S.uhv; e = S.uhe; break;
+        case SWGPU_YMOMENTUM: c = S.vh; v = S.vhv; e = S.vhe; break;
+        case SWGPU_ELEVATION: c = S.zc; v = S.zv; e = S.ze; break;
+        case SWGPU_FRICTION: c = S.fric; break;
+        default: return fail(h, SWGPU_EINVAL, "quantity %d cannot be set", q);
+    }
+    int rc = upload(h, c, centroid, (size_t)N);
+    if (rc) return rc;
+    if (v && vertex) {
+        auto pv = to_planes<double>(vertex, N, 3);
+        if ((rc = upload(h, v, pv.data(), (size_t)3 * N))) return rc;
+    }
+    if (e && edge) {
+        auto pe = to_planes<double>(edge, N, 3);
+        if ((rc = upload(h, e, pe.data(), (size_t)3 * N))) return rc;
+    } else if (q == SWGPU_ELEVATION && vertex) {
+        // quantity.c:687-706: bed edge values from the bed vertex values
+        std::vector<double> pe((size_t)3 * N);
+        for (int64_t k = 0; k < N; k++) {
+            const double q0 = vertex[3 * k], q1 = vertex[3 * k + 1], q2 = vertex[3 * k + 2];
+            pe[k] = 0.5 * (q1 + q2);
+            pe[N + k] = 0.5 * (q0 + q2);
+            pe[2 * N + k] = 0.5 * (q0 + q1);
+        }
+        if ((rc = upload(h, e, pe.data(), (size_t)3 * N))) return rc;
+    }
+    if (q == SWGPU_ELEVATION) h->elevation_set = true;
+    if (h->precision == SWGPU_MIXED && (q == SWGPU_ELEVATION || q == SWGPU_FRICTION)) {
+        if (build_mixed_geometry(h)) return fail(h, SWGPU_ECUDA, "mixed geometry upload");
+    }
+    if (q == SWGPU_STAGE || q == SWGPU_ELEVATION) h->mixed_from_stage = true;
+    if (q <= SWGPU_YMOMENTUM) h->vertices_stale = true;
+    return SWGPU_OK;
+}
+
+int swgpu_get_quantity(void *handle, int q, double *centroid, double *vertex, double *edge) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    const int64_t N = h->M.N;
+    DevState &S = h->S;
+    int rc;
+    if (h->precision == SWGPU_MIXED && !h->mixed_from_stage && q <= SWGPU_YMOMENTUM) {
+        launch_vertices_from_mixed(h->M, h->S, h->X, h->stream);
+        if ((rc = check_launch(h, "mixed vertex values"))) return rc;
+    }
+    if ((vertex || edge) && q <= SWGPU_YMOMENTUM) {
+        launch_interpolate_fp64(h->M, h->S, h->stream);
+        if ((rc = check_launch(h, "interpolate"))) return rc;
+    }
+    const double *c = nullptr, *v = nullptr, *e = nullptr;
+    switch (q) {
+        case SWGPU_STAGE: c = S.w; v = S.wv; e = S.we; break;
+        case SWGPU_XMOMENTUM: c = S.uh; v = S.uhv; e = S.uhe; break;
+        case SWGPU_YMOMENTUM: c = S.vh; v = S.vhv; e = S.vhe; break;
+        case SWGPU_ELEVATION: c = S.zc; v = S.zv; e = S.ze; break;
+        case SWGPU_FRICTION: c = S.fric; break;
+        case SWGPU_HEIGHT: c = S.hc; break;
+        case SWGPU_XVELOCITY: c = S.uc; break;
+        case SWGPU_YVELOCITY: c = S.vc; break;
+        default: return fail(h, SWGPU_EINVAL, "unknown quantity %d", q);
+    }
+    if (q >= SWGPU_HEIGHT) {
+        launch_other_quantities(h->M, h->S, h->stream);
+        if ((rc = check_launch(h, "other quantities"))) return rc;
+    }
+    if (centroid && (rc = download(h, centroid, c, (size_t)N))) return rc;
+    std::vector<double> tmp;
+    auto planes_out = [&](double *dst, const double *src) -> int {
+        tmp.resize((size_t)3 * N);
+        int r = download(h, tmp.data(), src, (size_t)3 * N);
+        if (r) return r;
+        for (int64_t k = 0; k < N; k++)
+            for (int i = 0; i < 3; i++) dst[3 * k + i] = tmp[(size_t)i * N + k];
+        return SWGPU_OK;
+    };
+    if (vertex) {
+        if (v) {
+            if ((rc = planes_out(vertex, v))) return rc;
+        } else if (centroid) {
+            for (int64_t k = 0; k < N; k++)
+                vertex[3 * k] = vertex[3 * k + 1] = vertex[3 * k + 2] = centroid[k];
+        }
+    }
+    if (edge) {
+        if (e) {
+            if ((rc = planes_out(edge, e))) return rc;
+        } else if (centroid) {
+            for (int64_t k = 0; k < N; k++)
+                edge[3 * k] = edge[3 * k + 1] = edge[3 * k + 2] = centroid[k];
+        }
+    }
+    return SWGPU_OK;
+}
+
+int swgpu_get_boundary_values(void *handle, int q, double *out) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !out) return fail(h, SWGPU_EINVAL, "null argument");
+    const double *src = nullptr;
+    switch (q) {
+        case SWGPU_STAGE: src = h->S.wb; break;
+        case SWGPU_XMOMENTUM: src = h->S.uhb; break;
+        case SWGPU_YMOMENTUM: src = h->S.vhb; break;
+        case SWGPU_ELEVATION: src = h->S.zb; break;
+        default: return fail(h, SWGPU_EINVAL, "no boundary values for quantity %d", q);
+    }
+    return download(h, out, src, (size_t)h->M.Nb);
+}
+
+static int require_fp64(Handle *h, const char *what) {
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (h->precision != SWGPU_FP64)
+        return fail(h, SWGPU_EINVAL,
+                    "%s is a per-method entry point of the FP64 path; mixed-precision "
+                    "handles run whole steps only",
+                    what);
+    return SWGPU_OK;
+}
+
+int swgpu_get_explicit_update(void *handle, int q, double *out) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "explicit_update");
+    if (rc) return rc;
+    const double *src = q == SWGPU_STAGE ? h->S.ew : q == SWGPU_XMOMENTUM ? h->S.euh
+                                                 : q == SWGPU_YMOMENTUM ? h->S.evh : nullptr;
+    if (!src || !out) return fail(h, SWGPU_EINVAL, "bad quantity or null output");
+    return download(h, out, src, (size_t)h->M.N);
+}
+
+int swgpu_get_semi_implicit_update(void *handle, int q, double *out) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "semi_implicit_update");
+    if (rc) return rc;
+    if (!out) return fail(h, SWGPU_EINVAL, "null output");
+    if (q == SWGPU_STAGE) {
+        std::fill(out, out + h->M.N, 0.0);
+        return SWGPU_OK;
+    }
+    const double *src = q == SWGPU_XMOMENTUM ? h->S.suh : q == SWGPU_YMOMENTUM ? h->S.svh : nullptr;
+    if (!src) return fail(h, SWGPU_EINVAL, "bad quantity");
+    return download(h, out, src, (size_t)h->M.N);
+}
+
+int swgpu_protect(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "protect");
+    if (rc) return rc;
+    launch_prepare_fp64(h->M, h->S, h->P, h->d_ctrl, h->stream);
+    if ((rc = check_launch(h, "protect"))) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+int swgpu_distribute_to_vertices_and_edges(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    int rc = sync_ctrl(h);  // current _order_ lives in the control block
+    if (rc) return rc;
+    if ((rc = issue_distribute(h, false))) return rc;
+    if ((rc = sync_ctrl(h))) return rc;
+    return device_status(h);
+}
+
+int swgpu_update_boundary(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (h->precision == SWGPU_MIXED && !h->mixed_from_stage) {
+        launch_vertices_from_mixed(h->M, h->S, h->X, h->stream);
+    }
+    launch_boundary_fp64(h->M, h->S, h->d_tags, h->d_ctrl, h->stream);
+    int rc = check_launch(h, "update_boundary");
+    if (rc) return rc;
+    if ((rc = sync_ctrl(h))) return rc;
+    return device_status(h);
+}
+
+int swgpu_compute_fluxes(void *handle, double *flux_timestep) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "compute_fluxes");
+    if (rc) return rc;
+    if ((rc = sync_ctrl(h))) return rc;
+    reset_ftmin(h->h_ctrl, h->P);
+    if ((rc = push_ctrl(h))) return rc;
+    launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, kWriteMaxSpeed, h->stream);
+    if ((rc = check_launch(h, "compute_fluxes"))) return rc;
+    if ((rc = sync_ctrl(h))) return rc;
+    double ft;
+    std::memcpy(&ft, &h->h_ctrl->ftmin_bits, sizeof ft);
+    h->h_ctrl->flux_timestep = ft;
+    if ((rc = push_ctrl(h))) return rc;
+    if (flux_timestep) *flux_timestep = ft;
+    return device_status(h);
+}
+
+int swgpu_compute_forcing_terms(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "compute_forcing_terms");
+    if (rc) return rc;
+    launch_forcing_fp64(h->M, h->S, h->P, h->stream);
+    if ((rc = check_launch(h, "compute_forcing_terms"))) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+int swgpu_update_conserved_quantities(void *handle, double timestep) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "update_conserved_quantities");
+    if (rc) return rc;
+    launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, timestep, 0, h->stream);
+    if ((rc = check_launch(h, "update_conserved_quantities"))) return rc;
+    if ((rc = sync_ctrl(h))) return rc;
+    return device_status(h);
+}
+
+int swgpu_update_other_quantities(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    launch_other_quantities(h->M, h->S, h->stream);
+    int rc = check_launch(h, "update_other_quantities");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+int swgpu_mass(void *handle, double *mass) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !mass) return fail(h, SWGPU_EINVAL, "null argument");
+    if (h->precision == SWGPU_MIXED && !h->mixed_from_stage)
+        launch_mass_mixed(h->M, h->S, h->X, h->d_scalar, h->stream);
+    else
+        launch_mass(h->M, h->S, h->d_scalar, h->stream);
+    int rc = check_launch(h, "mass");
+    if (rc) return rc;
+    return download(h, mass, h->d_scalar, 1);
+}
+
+int swgpu_get_state(void *handle, swgpu_state *state) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !state) return fail(h, SWGPU_EINVAL, "null argument");
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    fill_state(h->h_ctrl, state);
+    return SWGPU_OK;
+}
+
+int swgpu_set_state(void *handle, const swgpu_state *s) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !s) return fail(h, SWGPU_EINVAL, "null argument");
+    if (s->order != 1 && s->order != 2) return fail(h, SWGPU_EINVAL, "order must be 1 or 2");
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    Ctrl *c = h->h_ctrl;
+    c->time = s->time;
+    c->yieldtime = s->yieldtime;
+    c->finaltime = s->finaltime;
+    c->timestep = s->timestep;
+    c->flux_timestep = s->flux_timestep;
+    c->rec_max = s->recorded_max_timestep;
+    c->rec_min = s->recorded_min_timestep;
+    c->order = s->order;
+    c->smallsteps = s->smallsteps;
+    c->steps_since_yield = s->number_of_steps;
+    c->total_steps = s->total_steps;
+    c->stop_reason = (int)s->stop_reason;
+    c->status = (int)s->status;
+    return push_ctrl(h);
+}
+
+int swgpu_evolve_start(void *handle, double starttime, double yieldstep, double finaltime) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (!(yieldstep > 0)) return fail(h, SWGPU_EINVAL, "yieldstep must be > 0");
+    if (finaltime > 0 && finaltime < starttime)
+        return fail(h, SWGPU_EINVAL, "finaltime before starttime");
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    // first distribute with the current order (gpu_domain_advanced.py:2476)
+    if ((rc = issue_distribute(h, false))) return rc;
+    if ((rc = sync_ctrl(h))) return rc;
+    Ctrl *c = h->h_ctrl;
+    c->time = starttime;
+    c->order = h->P.default_order;
+    c->finaltime = finaltime > 0 ? finaltime : -1.0;
+    c->yieldstep = yieldstep;
+    c->yieldtime = starttime + yieldstep;
+    c->rec_min = h->P.evolve_max_timestep;
+    c->rec_max = h->P.evolve_min_timestep;
+    c->steps_since_yield = 0;
+    c->total_steps = 0;
+    c->halt = 0;
+    c->halt_pending = 0;
+    c->stop_reason = kStopNone;
+    c->status = 0;
+    c->budget = -1;
+    c->done_update = c->done_distribute = 0;
+    reset_ftmin(c, h->P);
+    if ((rc = push_ctrl(h))) return rc;
+    // update_ghosts (no-op), distribute, update_boundary (:2540-2543)
+    if ((rc = issue_distribute(h, true))) return rc;
+    h->resume_after_yield = false;
+    if ((rc = sync_ctrl(h))) return rc;
+    return device_status(h);
+}
+
+static int prepare_run(Handle *h, int64_t max_steps) {
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    Ctrl *c = h->h_ctrl;
+    if (c->status) return device_status(h);
+    if (c->stop_reason == kStopFinal)
+        return fail(h, SWGPU_EINVAL, "evolve already reached finaltime");
+    if (h->resume_after_yield) {
+        // the generator resumed after a yield (gpu_domain_advanced.py:2649-2654)
+        c->yieldtime += c->yieldstep;
+        c->rec_min = h->P.evolve_max_timestep;
+        c->rec_max = h->P.evolve_min_timestep;
+        c->steps_since_yield = 0;
+        h->resume_after_yield = false;
+    }
+    c->halt = 0;
+    c->halt_pending = 0;
+    c->stop_reason = kStopNone;
+    c->budget = max_steps > 0 ? max_steps : -1;
+    return push_ctrl(h);
+}
+
+static int finish_run(Handle *h, swgpu_state *state) {
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    if (h->h_ctrl->stop_reason == kStopYield) h->resume_after_yield = true;
+    if (state) fill_state(h->h_ctrl, state);
+    return device_status(h);
+}
+
+static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *elapsed_ms);
+
+int swgpu_evolve_run(void *handle, int64_t max_steps, swgpu_state *state) {
+    return run_graphs(static_cast<Handle *>(handle), max_steps, state, nullptr);
+}
+
+int swgpu_evolve_run_timed(void *handle, int64_t max_steps, swgpu_state *state,
+                           double *elapsed_ms) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!elapsed_ms) return fail(h, SWGPU_EINVAL, "null elapsed_ms");
+    return run_graphs(h, max_steps, state, elapsed_ms);
+}
+
+int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !ms || nsteps <= 0) return fail(h, SWGPU_EINVAL, "bad argument");
+    int rc = prepare_run(h, nsteps);
+    if (rc) return rc;
+    cudaEvent_t ev[4];
+    for (int i = 0; i < 4; i++) CK(cudaEventCreate(&ev[i]));
+    double acc[3] = {0, 0, 0};
+    for (int64_t s = 0; s < nsteps; s++) {
+        CK(cudaEventRecord(ev[0], h->stream));
+        if (h->precision == SWGPU_FP64)
+            launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, kFused, h->stream);
+        else
+            launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused, h->stream);
+        CK(cudaEventRecord(ev[1], h->stream));
+        if (h->precision == SWGPU_FP64)
+            launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, kFused | kFrictionInline,
+                               h->stream);
+        else
+            launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused | kFrictionInline,
+                                h->stream);
+        CK(cudaEventRecord(ev[2], h->stream));
+        if (h->precision == SWGPU_FP64)
+            launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,
+                                   kFused | kWriteBoundary, h->stream);
+        else
+            launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl,
+                                    kFused | kWriteBoundary, h->stream);
+        CK(cudaEventRecord(ev[3], h->stream));
+        if ((rc = check_launch(h, "profile step"))) return rc;
+        CK(cudaEventSynchronize(ev[3]));
+        float t;
+        for (int i = 0; i < 3; i++) {
+            CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+            acc[i] += t;
+        }
+    }
+    for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
+    for (int i = 0; i < 3; i++) ms[i] = acc[i];
+    return finish_run(h, nullptr);
+}
+
+static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *elapsed_ms) {
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    int rc = prepare_run(h, max_steps);
+    if (rc) return rc;
+    if ((rc = build_graph(h))) return rc;
+    // keep two graphs in flight: while graph i runs, the host waits on the
+    // control-block copy that follows graph i-1
+    cudaEvent_t ev[2], t0, t1;
+    CK(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+    CK(cudaEventCreate(&t0));
+    CK(cudaEventCreate(&t1));
+    CK(cudaEventRecord(t0, h->stream));
+    int64_t launched = 0;
+    // with a step budget the device stops itself after max_steps steps, so
+    // exactly ceil(max_steps / steps-per-graph) graphs are launched
+    const int64_t max_graphs =
+        max_steps > 0 ? (max_steps + kStepsPerGraph - 1) / kStepsPerGraph : INT64_MAX;
+    cudaError_t e = cudaSuccess;
+    int inflight = 0, slot = 0;
+    bool halted = false;
+    while (!halted && launched < max_graphs) {
+        e = cudaGraphLaunch(h->graph, h->stream);
+        if (e != cudaSuccess) break;
+        e = cudaMemcpyAsync(&h->h_ctrl->halt, &h->d_ctrl->halt, sizeof(int) * 4,
+                            cudaMemcpyDeviceToHost, h->stream);
+        if (e != cudaSuccess) break;
+        e = cudaEventRecord(ev[slot], h->stream);
+        if (e != cudaSuccess) break;
+        launched++;
+        inflight++;
+        slot ^= 1;
+        if (inflight == 2) {
+            e = cudaEventSynchronize(ev[slot]);  // the older of the two
+            if (e != cudaSuccess) break;
+            inflight--;
+            if (h->h_ctrl->halt || h->h_ctrl->status) halted = true;
+        }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(t1, h->stream);
+    cudaError_t e2 = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess && elapsed_ms) {
+        float ms = 0.f;
+        e = cudaEventElapsedTime(&ms, t0, t1);
+        *elapsed_ms = ms;
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (e != cudaSuccess) return fail(h, SWGPU_ECUDA, "evolve_run: %s", cudaGetErrorString(e));
+    return finish_run(h, state);
+}
+
+int swgpu_evolve_one_step(void *handle, swgpu_state *state) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    int rc = prepare_run(h, 1);
+    if (rc) return rc;
+    if ((rc = issue_fused_step(h))) return rc;
+    return finish_run(h, state);
+}
+
+int swgpu_synchronize(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+}  // extern "C"
+
+namespace swgpu {
+Handle *handle_cast(void *p) { return static_cast<Handle *>(p); }
+}  // namespace swgpu

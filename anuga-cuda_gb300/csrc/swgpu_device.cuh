@@ -1,0 +1,175 @@
+// swgpu_device.cuh -- device helpers shared by the FP64 and mixed kernels:
+// comparisons with the reference's min/max semantics, the boundary
+// condition formulas, the device-side update_timestep, last-block-done
+// bookkeeping and the block minimum of the flux timestep.
+#pragma once
+
+#include "swgpu_internal.cuh"
+
+namespace swgpu {
+
+// src/anuga_HMPP/util_ext.h:45-59: plain comparisons, second argument on
+// ties (so the sign of a zero result follows the reference, unlike fmax).
+__device__ __forceinline__ double omax(double x, double y) { return x > y ? x : y; }
+__device__ __forceinline__ double omin(double x, double y) { return x < y ? x : y; }
+__device__ __forceinline__ float omaxf(float x, float y) { return x > y ? x : y; }
+__device__ __forceinline__ float ominf(float x, float y) { return x < y ? x : y; }
+
+__device__ __forceinline__ void set_status(Ctrl *ctrl, int code) {
+    atomicCAS(&ctrl->status, 0, code);
+}
+
+// Boundary value of one boundary edge from the owning triangle's edge
+// values (reflective: src/anuga_cuda/evaluate_segment/evaluate_segment.cu:3-76;
+// Dirichlet: :80-115; the time-dependent stage has no reference GPU
+// counterpart).  Returns false for an unknown type.
+__device__ __forceinline__ bool eval_boundary(const BcTag &T, double time, double we,
+                                              double uhe, double vhe, double n1,
+                                              double n2, double &wb, double &uhb,
+                                              double &vhb) {
+    if (T.type == SWGPU_BC_REFLECTIVE) {
+        const double r1 = -uhe * n1 - vhe * n2;
+        const double r2 = -uhe * n2 + vhe * n1;
+        wb = we;
+        uhb = n1 * r1 - n2 * r2;
+        vhb = n2 * r1 + n1 * r2;
+        return true;
+    }
+    if (T.type == SWGPU_BC_DIRICHLET) {
+        wb = T.p[0];
+        uhb = T.p[1];
+        vhb = T.p[2];
+        return true;
+    }
+    if (T.type == SWGPU_BC_TIME_STAGE_SINE) {
+        const double two_pi = 6.283185307179586;
+        wb = T.p[0] + T.p[1] * sin(two_pi * time / T.p[2] + T.p[3]);
+        uhb = 0.0;
+        vhb = 0.0;
+        return true;
+    }
+    return false;
+}
+
+// Snapshot of the time bookkeeping taken at kernel entry.
+struct StepClock {
+    double dt;          // timestep of this step
+    double ftmin;       // flux timestep (minimum over edges)
+    long long order;    // _order_ after this step's update_timestep
+    long long smallsteps;
+    int small_error;    // ran below the minimum step at order 1
+};
+
+// ANUGA Generic_Domain.update_timestep as restated in
+// src/anuga_HMPP/evolve.c:115-160 (finaltime clamp as finaltime - time).
+// Every thread evaluates it on the same snapshot and gets the same dt.
+__device__ __forceinline__ StepClock device_update_timestep(const Ctrl *c, const DevParams &P) {
+    StepClock s;
+    s.ftmin = __longlong_as_double((long long)c->ftmin_bits);
+    double dt = omin(P.CFL * s.ftmin, P.evolve_max_timestep);
+    s.order = c->order;
+    s.smallsteps = c->smallsteps;
+    s.small_error = 0;
+    if (dt < P.evolve_min_timestep) {
+        s.smallsteps += 1;
+        if (s.smallsteps > P.max_smallsteps) {
+            s.smallsteps = 0;
+            if (s.order == 1) {
+                dt = P.evolve_min_timestep;
+                s.small_error = 1;
+            } else {
+                s.order = 1;
+            }
+        }
+    } else {
+        s.smallsteps = 0;
+        if (s.order == 1 && P.default_order == 2) s.order = 2;
+    }
+    if (c->finaltime > 0 && c->time + dt > c->finaltime) dt = c->finaltime - c->time;
+    if (c->time + dt > c->yieldtime) dt = c->yieldtime - c->time;
+    s.dt = dt;
+    return s;
+}
+
+// Called by thread 0 of each block after the block's work; returns true in
+// exactly one block, the last to finish (all other blocks' writes are then
+// visible).  The counter is reset for the next launch.
+__device__ __forceinline__ bool last_block_done(unsigned int *counter) {
+    __threadfence();
+    const unsigned int prev = atomicAdd(counter, 1u);
+    if (prev == gridDim.x - 1) {
+        __threadfence();
+        *counter = 0;
+        return true;
+    }
+    return false;
+}
+
+// Block-wide minimum of a positive double, then one atomicMin on its bit
+// pattern (positive IEEE doubles order like their bits) only when it lowers
+// the running minimum.
+__device__ __forceinline__ void block_min_timestep(double t, Ctrl *ctrl) {
+    __shared__ double wmin[kBlock / 32];
+    for (int o = 16; o > 0; o >>= 1) t = omin(t, __shfl_xor_sync(0xffffffffu, t, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wmin[warp] = t;
+    __syncthreads();
+    if (warp == 0) {
+        t = lane < (int)(blockDim.x >> 5) ? wmin[lane] : pos_inf();
+        for (int o = 16; o > 0; o >>= 1) t = omin(t, __shfl_xor_sync(0xffffffffu, t, o));
+        if (lane == 0) {
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(t);
+            if (!(t >= 0.0)) {
+                set_status(ctrl, SWGPU_ENONFINITE);  // NaN reached the timestep
+            } else if (bits < *(volatile unsigned long long *)&ctrl->ftmin_bits) {
+                atomicMin(&ctrl->ftmin_bits, bits);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ int ctrl_halted(const Ctrl *c) {
+    return *(volatile const int *)&c->halt;
+}
+
+// Last block of the update kernel: commit the new time and counters and
+// decide whether the loop stops after this step's distribute.
+__device__ __forceinline__ void commit_step(Ctrl *c, const StepClock &s, const DevParams &P) {
+    c->rec_max = omax(s.dt, c->rec_max);
+    c->rec_min = omin(s.dt, c->rec_min);
+    c->order = s.order;
+    c->smallsteps = s.smallsteps;
+    c->flux_timestep = s.ftmin;
+    c->timestep = s.dt;
+    c->time = c->time + s.dt;
+    c->steps_since_yield += 1;
+    c->total_steps += 1;
+    c->ftmin_bits = (unsigned long long)__double_as_longlong(P.evolve_max_timestep);
+    int reason = kStopNone;
+    if (s.small_error) set_status(c, SWGPU_ESMALLSTEP);
+    if (c->status != 0) {
+        reason = kStopError;
+    } else if (c->finaltime > 0 && c->time >= c->finaltime - c->time_epsilon) {
+        if (c->time > c->finaltime) set_status(c, SWGPU_EOVERSHOOT);
+        c->time = c->finaltime;
+        reason = c->status ? kStopError : kStopFinal;
+    } else if (c->time >= c->yieldtime) {
+        reason = kStopYield;
+    }
+    if (reason == kStopNone && c->budget > 0) {
+        c->budget -= 1;
+        if (c->budget == 0) reason = kStopBudget;
+    }
+    if (reason != kStopNone) c->halt_pending = reason;
+}
+
+// Last block of the distribute kernel: a pending stop takes effect.
+__device__ __forceinline__ void apply_pending_halt(Ctrl *c) {
+    if (c->halt_pending) {
+        c->stop_reason = c->halt_pending;
+        c->halt = 1;
+        c->halt_pending = 0;
+    }
+}
+
+}  // namespace swgpu

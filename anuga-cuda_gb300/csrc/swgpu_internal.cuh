@@ -1,0 +1,161 @@
+// swgpu_internal.cuh -- device data structures shared by the evolve kernels
+// and the C ABI layer of libswgpu.so.
+//
+// Device layout (HBM): every per-triangle array is structure-of-arrays with
+// triangle index fastest, so a warp's 32 consecutive triangles read 32
+// consecutive words.  Per-edge / per-vertex data are three planes of N
+// ([i*N + k] for edge or vertex i of triangle k); normals and vertex
+// coordinates are six planes ([2i*N + k] = x, [(2i+1)*N + k] = y).
+// Indices are int32.  The caller's triangle order is kept; meshes built by
+// anuga_cuda.mesh are already Morton ordered so neighbour gathers stay local.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/swgpu.h"
+
+namespace swgpu {
+
+constexpr int kBlock = 256;
+
+// neighbour packing: interior edge -> (n << 2) | m (m = edge index in n);
+// boundary edge -> -(slot + 1), as in ANUGA's neighbours array.
+__host__ __device__ inline int pack_neighbour(int n, int m) { return (n << 2) | m; }
+
+struct DevMesh {
+    int N, Nb;
+    const int *nbr;            // [3][N] packed neighbour / boundary slot
+    const int *surr;           // [3][N] surrogate neighbours
+    const uint8_t *nb;         // [N] number_of_boundaries
+    const uint8_t *order;      // [N] flux summation order (2 bits per position)
+    const uint8_t *full;       // [N] tri_full_flag
+    const double *normals;     // [6][N]
+    const double *len;         // [3][N]
+    const double *radii;       // [N]
+    const double *areas;       // [N]
+    const double *vxy;         // [6][N]
+    const double *cxy;         // [2][N]
+    const int *bcell, *bedge, *btag;   // [Nb]
+};
+
+// FP64 state (both precisions keep the conserved centroid state in FP64).
+struct DevState {
+    double *w, *uh, *vh, *zc, *fric;          // [N] centroid values
+    double *uvel, *vvel;                      // [N] centroid velocities (extrapolation input)
+    double *wv, *uhv, *vhv, *zv, *ze;         // [3][N] vertex values; bed edge values
+    double *we, *uhe, *vhe;                   // [3][N] edge values (materialised on demand)
+    double *wb, *uhb, *vhb, *zb;              // [Nb] boundary values
+    double *ew, *euh, *evh;                   // [N] explicit_update
+    double *suh, *svh;                        // [N] semi_implicit_update
+    double *max_speed;                        // [N]
+    double *hc, *uc, *vc;                     // [N] derived centroid quantities
+    double *hb, *ub, *vb;                     // [Nb] derived boundary quantities
+    double *partials;                         // [grid] reduction scratch
+};
+
+// Mixed-precision state.  The conserved state is FP64 depth h = w - z (so
+// depth at wet/dry fronts never comes from a difference of two large
+// stages) and FP64 momentum; everything the flux, limiter and extrapolation
+// read is FP32: centroid depth and velocities, vertex depth and momentum,
+// and geometry precomputed relative to each triangle's centroid.
+struct DevMixed {
+    double *hd;                // [N] FP64 depth (conserved)
+    float *hf, *uvel, *vvel;   // [N] centroid depth and velocities
+    float *hv, *uhv, *vhv;     // [3][N] vertex depth and momentum
+    float *hbf, *uhbf, *vhbf;  // [Nb] boundary depth and momentum
+    float *ew, *euh, *evh;     // [N] explicit_update
+    float *nx, *ny, *len;      // [3][N] normals, edge lengths
+    float *inv_area, *radius;  // [N]
+    float *gc;                 // [6][N] vertex-jump coefficients (dq1, dq2 per vertex)
+    float *dzn;                // [3][N] bed centroid of surrogate j minus own
+    float *dzv;                // [3][N] bed vertex minus bed centroid
+    float *zgrad;              // [2][N] bed gradient
+    float *fric;               // [N] Manning n
+    float *zmoff;              // [N] mean(bed vertex) minus bed centroid
+    uint8_t *kind;             // [N] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat
+};
+
+struct DevParams {
+    double g, epsilon, H0, minimum_allowed_height, maximum_allowed_speed;
+    double beta_w, beta_w_dry, beta_uh, beta_uh_dry, beta_vh, beta_vh_dry;
+    double alpha_balance, CFL, evolve_max_timestep, evolve_min_timestep;
+    int tight_slope_limiters, use_centroid_velocities, optimise_dry_cells;
+    int extrapolate_velocity_second_order, use_sloped_mannings;
+    int max_smallsteps, default_order;
+};
+
+struct BcTag {
+    int type;
+    double p[4];
+};
+
+// Device-resident evolve bookkeeping.  Written by the last block of the
+// update kernel (time, order, counters) and the last block of the
+// distribute kernel (halt); read by every kernel at entry.
+struct __align__(16) Ctrl {
+    unsigned long long ftmin_bits;  // minimum flux timestep of this step (bits of a positive double)
+    double time, yieldtime, finaltime, yieldstep, timestep, flux_timestep;
+    double rec_max, rec_min, time_epsilon;
+    long long order, smallsteps, steps_since_yield, total_steps;
+    long long budget;               // steps left in this run; < 0 = unlimited
+    int halt;                       // nonzero: kernels return at entry
+    int halt_pending;               // stop reason raised by update, applied after distribute
+    int stop_reason;
+    int status;                     // first device-side failure (swgpu_status)
+    unsigned int done_update, done_distribute;
+    int pad[2];
+};
+
+enum StopReason { kStopNone = 0, kStopYield = 1, kStopFinal = 2, kStopBudget = 3, kStopError = 4 };
+
+// Kernel option flags
+enum : int {
+    kFused = 1,           // part of the device-resident loop (reads/writes Ctrl)
+    kWriteEdges = 2,      // distribute materialises edge values
+    kWriteBoundary = 4,   // distribute evaluates boundary conditions
+    kFrictionInline = 8,  // update computes Manning friction itself
+    kWriteMaxSpeed = 16,  // flux writes max_speed
+};
+
+__host__ __device__ inline double pos_inf() { return 1.0e300 * 1.0e300; }
+
+// ---------------------------------------------------------------- launches
+// FP64 path (swgpu_fp64.cu)
+void launch_prepare_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                         Ctrl *ctrl, cudaStream_t st);
+void launch_distribute_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                            const BcTag *tags, Ctrl *ctrl, int flags, cudaStream_t st);
+void launch_boundary_fp64(const DevMesh &M, const DevState &S, const BcTag *tags,
+                          Ctrl *ctrl, cudaStream_t st);
+void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                      Ctrl *ctrl, int flags, cudaStream_t st);
+void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                         cudaStream_t st);
+void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                        Ctrl *ctrl, double dt, int flags, cudaStream_t st);
+void launch_interpolate_fp64(const DevMesh &M, const DevState &S, cudaStream_t st);
+void launch_other_quantities(const DevMesh &M, const DevState &S, cudaStream_t st);
+void launch_mass(const DevMesh &M, const DevState &S, double *out, cudaStream_t st);
+
+// Mixed path (swgpu_mixed.cu)
+void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                             const DevParams &P, const BcTag *tags, Ctrl *ctrl,
+                             int flags, cudaStream_t st);
+void launch_flux_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                       const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st);
+void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                         const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st);
+// stand-alone distribute head: (optionally) depth from the FP64 stage, then
+// protect and the FP32 centroid copies
+void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                          const DevParams &P, int from_stage, cudaStream_t st);
+// FP64 stage / vertex / edge values from the mixed state, for downloads
+void launch_vertices_from_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                                cudaStream_t st);
+void launch_mass_mixed(const DevMesh &M, const DevState &S, const DevMixed &X, double *out,
+                       cudaStream_t st);
+
+inline int grid_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace swgpu

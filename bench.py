@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""bench.py -- triangle-steps/s of ANUGA's explicit shallow-water evolve step
+on one GB300, printed as one JSON line.
+
+Workload: the 4,000,000-triangle wet/dry case (1000 x 1000 rectangular_cross
+cells on 10 km x 10 km, 1:100 beach + Gaussian bumps, 2 m hump, per-triangle
+Manning n), seeded synthetic data.  A step is one Euler step of the whole
+mesh: fluxes + gravity, timestep reduction, friction + update + protect,
+extrapolation + balance + boundaries.
+
+  value       mixed-precision path, device time of K steps (CUDA events on
+              the library's stream), inputs resident in HBM; the state is
+              ~1.1 GB so every step streams from HBM (no L2 flush needed)
+  e2e         the same K steps through the public C ABI from host buffers:
+              H2D of the initial conserved state from pinned memory, evolve
+              start, K steps, D2H of the final conserved state, host clock
+  fp64        the FP64 parity path on the same K steps, and the max relative
+              stage difference mixed vs FP64 after them
+  roofline    the dominant kernel's algorithmic bytes per launch / its mean
+              CUDA-event duration, against MEASURED_PEAKS.json hbm_gbs
+  cpu_baseline  the CPU oracle (serial C restatement of the reference's
+              ANUGA C path) on a bounded sample of the same workload
+
+--impl reference times the oracle on the host cores (one process per core,
+each evolving the full workload for a bounded time) and prints the same line
+with "impl": "reference".
+
+Multi-GPU (torchrun): replicas only -- every rank evolves its own copy of the
+workload; value = total triangle-steps of all ranks / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "anuga-cuda_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "triangle-steps/s on 1 GB300 (mixed precision; FP64 alongside)"
+UNIT = "triangle-steps/s"
+
+# algorithmic bytes per triangle-step of each kernel (own arrays, neighbour
+# gathers counted as cache hits)
+MIXED_BYTES = {"flux": 116, "update": 80, "distribute": 109}
+FP64_BYTES = {"flux": 296, "update": 120, "distribute": 253}
+MODEL_BYTES = {"mixed": 368, "fp64": 568}   # whole-step byte model
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=160)
+    ap.add_argument("--warmup", type=int, default=16)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=1000, help="rectangular_cross cells per side")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if r[5 + i].lower() in ("active", "1")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return None
+
+
+def build_workload(cells):
+    from anuga_cuda import scenarios
+    return scenarios.wet_dry(m=cells)
+
+
+def run_ours(args, rank, world, local, sc):
+    import ctypes as C
+    import numpy as np
+    import anuga_cuda
+    from anuga_cuda import DEFAULT, GPU_domain, _lib
+    from anuga_cuda._lib import check, f64p, lib
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    if rank == 0:
+        anuga_cuda.build()
+    if dist is not None:
+        dist.barrier()
+    L = lib()
+    if world > 1:
+        # the library works on the current device of the calling thread
+        cudart = C.CDLL("libcudart.so")
+        cudart.cudaSetDevice(local)
+
+    N = sc.N
+    K, W = args.steps, args.warmup
+    results = {}
+    finals = {}
+    for prec in ("mixed", "fp64"):
+        d = GPU_domain(mesh=sc.mesh, parameters=DEFAULT, precision=prec)
+        sc.apply_to(d)
+        d.evolve_steps(W)                      # warm-up; builds the step graph
+        st = _lib.State_t()
+        ms = C.c_double()
+        if dist is not None:
+            dist.barrier()
+        with ClockSampler(local) as clk:
+            check(L.swgpu_evolve_run_timed(d._h, K, C.byref(st), C.byref(ms)), d._h)
+        if dist is not None:
+            t = torch.tensor([ms.value], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms_max = float(t.item())
+        else:
+            ms_max = ms.value
+        assert st.total_steps == W + K, (st.total_steps, W + K)
+        kms = (C.c_double * 3)()
+        kp = min(K, 32)
+        check(L.swgpu_profile_steps(d._h, kp, kms), d._h)
+        results[prec] = {"ms": ms_max, "clocks": clk.summary(),
+                         "kernel_ms": [kms[i] / kp for i in range(3)], "time": st.time}
+        finals[prec] = d.quantities["stage"].centroid_values
+        del d
+
+    w64 = finals["fp64"]
+    stage_err = float(np.max(np.abs(finals["mixed"] - w64)) / np.max(np.abs(w64)))
+
+    # end to end through the C ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        import torch
+        host = {q: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+                for q, a in (("w", sc.stage_centroid), ("u", sc.xmom_centroid),
+                             ("v", sc.ymom_centroid))}
+        outs = {q: torch.empty(N, dtype=torch.float64).pin_memory() for q in ("w", "u", "v")}
+        d = GPU_domain(mesh=sc.mesh, parameters=DEFAULT, precision="mixed")
+        sc.apply_to(d)
+        d.evolve_steps(W)
+
+        def ptr(t):
+            return C.cast(t.data_ptr(), _lib._f64p)
+
+        st = _lib.State_t()
+        check(L.swgpu_synchronize(d._h), d._h)
+        t0 = time.perf_counter()
+        for qid, q in ((_lib.STAGE, "w"), (_lib.XMOMENTUM, "u"), (_lib.YMOMENTUM, "v")):
+            check(L.swgpu_set_quantity(d._h, qid, ptr(host[q]), None, None), d._h)
+        check(L.swgpu_evolve_start(d._h, 0.0, 1.0e300, -1.0), d._h)
+        check(L.swgpu_evolve_run(d._h, K, C.byref(st)), d._h)
+        for qid, q in ((_lib.STAGE, "w"), (_lib.XMOMENTUM, "u"), (_lib.YMOMENTUM, "v")):
+            check(L.swgpu_get_quantity(d._h, qid, ptr(outs[q]), None, None), d._h)
+        t1 = time.perf_counter()
+        assert st.total_steps == K
+        e2e = {"value": N * K / (t1 - t0), "unit": UNIT,
+               "h2d_bytes_per_step": 3 * 8 * N / K, "d2h_bytes_per_step": 3 * 8 * N / K,
+               "wall_s": t1 - t0}
+        del d
+
+    if dist is not None:
+        dist.barrier()
+    out = {"results": results, "stage_err": stage_err, "e2e": e2e, "N": N}
+    if dist is not None:
+        dist.destroy_process_group()
+    return out
+
+
+def cpu_oracle_rate(sc, seconds=12.0, warm_steps=1):
+    """Serial CPU oracle on the same workload for a bounded time."""
+    from anuga_cuda import DEFAULT
+    from oracle import oracle as O
+    O.build(ref=False)
+    od = O.OracleDomain(sc.mesh, DEFAULT, sc.oracle_tags())
+    sc.apply_to_oracle(od)
+    od.evolve_start(1.0e300)
+    od.evolve_steps(1.0e300, None, warm_steps)
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        od.evolve_steps(1.0e300, None, 1)
+        steps += 1
+    wall = time.perf_counter() - t0
+    return sc.N * steps / wall, steps, wall
+
+
+def _ref_worker(args):
+    cells, seconds, q = args
+    sc = build_workload(cells)
+    rate, steps, wall = cpu_oracle_rate(sc, seconds)
+    q.put((rate, steps, wall))
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    try:
+        avail = int([l for l in open("/proc/meminfo") if l.startswith("MemAvailable")][0]
+                    .split()[1]) * 1024
+    except (OSError, IndexError):
+        avail = 64 << 30
+    per = 6.0e9 * (args.cells / 1000.0) ** 2     # oracle + mesh bytes per process
+    procs = max(1, min(cores, int(0.6 * avail / per), 32))
+    seconds = 30.0
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_ref_worker, args=((args.cells, seconds, q),)) for _ in range(procs)]
+    t0 = time.perf_counter()
+    for p in ps:
+        p.start()
+    res = [q.get() for _ in ps]
+    for p in ps:
+        p.join()
+    wall = time.perf_counter() - t0
+    total = sum(r[0] for r in res)
+    steps = sum(r[1] for r in res)
+    N = 4 * args.cells * args.cells
+    line = {
+        "impl": "reference", "metric": METRIC, "value": total, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * N / total,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded wet/dry scenario)",
+        "config": {"workload": f"wet_dry {args.cells}x{args.cells} rectangular_cross "
+                               f"({N} triangles)", "triangles": N},
+        "cpu_baseline": {"value": total, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{procs} processes x ~{seconds:.0f} s of full-mesh Euler "
+                                   f"steps ({steps} steps in total, {wall:.0f} s wall)"},
+        "e2e": {"value": total, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+        if line is not None:
+            print(json.dumps(line))
+        return
+    sc = build_workload(args.cells)
+    out = run_ours(args, rank, world, local, sc)
+    if rank != 0:
+        return
+    N, K, W = out["N"], args.steps, args.warmup
+    r = out["results"]
+    mixed_ms, fp64_ms = r["mixed"]["ms"], r["fp64"]["ms"]
+    value = world * N * K / (mixed_ms / 1000.0)
+    fp64_value = world * N * K / (fp64_ms / 1000.0)
+    peaks = measured_peaks()
+    peak_gbs = peaks["hbm_gbs"] if peaks else 6800.0
+    kms = r["mixed"]["kernel_ms"]
+    names = ["flux", "update", "distribute"]
+    dom = max(range(3), key=lambda i: kms[i])
+    achieved = MIXED_BYTES[names[dom]] * N / (kms[dom] / 1000.0) / 1e9
+    kms64 = r["fp64"]["kernel_ms"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": mixed_ms / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f64 mixed", "data": "synthetic (seeded wet/dry scenario)",
+        "config": {"workload": f"wet_dry {args.cells}x{args.cells} rectangular_cross ({N} triangles)",
+                   "triangles": N, "precision": "mixed", "l2": "inputs larger than L2 (state ~1.1 GB)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms / K,
+                 "kernel_ms": dict(zip(names, kms64)),
+                 "mixed_over_fp64": value / fp64_value},
+        "mixed_stage_rel_err": out["stage_err"],
+        "kernel_ms": dict(zip(names, kms)),
+        "roofline": {"bound": "hbm", "kernel": names[dom] + "_mixed", "achieved": achieved,
+                     "peak": peak_gbs, "unit": "GB/s", "frac": achieved / peak_gbs,
+                     "traffic": None,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "step_model_frac": MODEL_BYTES["mixed"] * N / (mixed_ms / K / 1000.0) / 1e9
+                     / peak_gbs},
+        "clocks": r["mixed"]["clocks"],
+        "gpu_launches": 3 * K * 2 + 3 * 32 * 2,
+    }
+    if out["e2e"]:
+        line["e2e"] = {k: out["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step",
+                                                     "d2h_bytes_per_step")}
+    if not args.no_cpu_baseline:
+        rate, steps, wall = cpu_oracle_rate(sc, seconds=12.0)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{steps} Euler steps of the full {N}-triangle mesh "
+                                          f"({wall:.1f} s) on one core"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

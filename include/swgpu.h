@@ -1,0 +1,268 @@
+/*
+ * swgpu.h -- C ABI of libswgpu.so, the GB300 (sm_103a) shallow-water evolve
+ * step for ANUGA unstructured triangle meshes.
+ *
+ * The reference (budiaji/anuga-cuda) exposes this path as a Python subclass
+ * of anuga.Domain whose overridden methods launch one PyCUDA kernel each
+ * (src/anuga_cuda/gpu_domain_advanced.py).  Each entry point below replaces
+ * one of those methods or the device-array management behind them; the
+ * comment on each names the reference code it stands in for.  The Python
+ * package anuga_cuda (GPU_domain) binds these through ctypes.
+ *
+ * Conventions
+ *   - Every function returns an int status: SWGPU_OK (0) or a SWGPU_E*
+ *     code.  swgpu_last_error() gives the message of the last failure on a
+ *     handle.  Nothing in the library aborts, traps or exits.
+ *   - Host arrays use ANUGA's layout: triangle k, edge/vertex i at [3k+i],
+ *     normals and vertex coordinates at [6k+2i] (x) and [6k+2i+1] (y),
+ *     indices as int64 (ANUGA's `long`).  The library copies them; it never
+ *     keeps a host pointer after a call returns.
+ *   - A handle owns all device memory and one CUDA stream.  It must be used
+ *     from one host thread at a time.  Several handles may share a device.
+ */
+#ifndef SWGPU_H
+#define SWGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWGPU_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------- */
+enum swgpu_status {
+    SWGPU_OK = 0,
+    SWGPU_EINVAL = 1,          /* bad argument (null pointer, size, enum)   */
+    SWGPU_ECUDA = 2,           /* a CUDA runtime call failed                */
+    SWGPU_ENOMEM = 3,          /* device allocation failed                  */
+    SWGPU_EDENOMINATOR = 4,    /* semi-implicit denominator <= 0 (_update)  */
+    SWGPU_ESMALLSTEP = 5,      /* timestep below minimum even at order 1    */
+    SWGPU_ENONFINITE = 6,      /* NaN or Inf in the flux timestep           */
+    SWGPU_EBED = 7,            /* discontinuous bed across an edge          */
+    SWGPU_EBOUNDARY = 8,       /* unknown boundary type                     */
+    SWGPU_EOVERSHOOT = 9,      /* model time overshot finaltime             */
+    SWGPU_EMESH = 10           /* inconsistent mesh arrays                  */
+};
+
+/* ---- precision of the evolve path ------------------------------------ */
+enum swgpu_precision {
+    SWGPU_FP64 = 0,   /* every operation in FP64, in the reference's order  */
+    SWGPU_MIXED = 1   /* FP32 flux/limiter/extrapolation, FP64 update, depth
+                         at wet/dry fronts, mass and model time             */
+};
+
+/* ---- quantity ids (Domain.quantities keys) --------------------------- */
+enum swgpu_quantity {
+    SWGPU_STAGE = 0,
+    SWGPU_XMOMENTUM = 1,
+    SWGPU_YMOMENTUM = 2,
+    SWGPU_ELEVATION = 3,
+    SWGPU_FRICTION = 4,
+    SWGPU_HEIGHT = 5,      /* derived: update_other_quantities */
+    SWGPU_XVELOCITY = 6,   /* derived */
+    SWGPU_YVELOCITY = 7    /* derived */
+};
+
+/* ---- boundary condition types ---------------------------------------- */
+enum swgpu_boundary_type {
+    SWGPU_BC_REFLECTIVE = 0,     /* anuga Reflective_boundary              */
+    SWGPU_BC_DIRICHLET = 1,      /* anuga Dirichlet_boundary (w, uh, vh)   */
+    SWGPU_BC_TIME_STAGE_SINE = 2 /* stage = p0 + p1*sin(2*pi*t/p2 + p3),
+                                    momentum 0, t = model time             */
+};
+
+typedef struct {
+    int64_t type;      /* swgpu_boundary_type */
+    double p[4];       /* parameters, see swgpu_boundary_type */
+} swgpu_boundary_tag;
+
+/* Mesh arrays (anuga Mesh / struct domain in src/anuga_HMPP/sw_domain.h:16-180).
+ * neighbours[3k+i] = triangle across edge i, or -(m+1) for boundary slot m.
+ * surrogate_neighbours = neighbours with boundary entries replaced by k.
+ * tri_full_flag may be NULL (all triangles full). */
+typedef struct {
+    int64_t number_of_elements;
+    int64_t number_of_boundary_elements;
+    const int64_t *neighbours;            /* [3N] */
+    const int64_t *neighbour_edges;       /* [3N] */
+    const int64_t *surrogate_neighbours;  /* [3N] */
+    const int64_t *number_of_boundaries;  /* [N]  */
+    const int64_t *tri_full_flag;         /* [N] or NULL */
+    const double *normals;                /* [6N] */
+    const double *edgelengths;            /* [3N] */
+    const double *radii;                  /* [N]  */
+    const double *areas;                  /* [N]  */
+    const double *vertex_coordinates;     /* [6N] */
+    const double *centroid_coordinates;   /* [2N] */
+    const int64_t *boundary_cells;        /* [Nb] triangle of boundary slot m */
+    const int64_t *boundary_edges;        /* [Nb] edge of boundary slot m     */
+    const int64_t *boundary_tag;          /* [Nb] index into the tag table    */
+} swgpu_mesh;
+
+/* ANUGA numerical parameters (Domain attributes; the reference reads the
+ * same set, src/anuga_HMPP/sw_domain_fun.h:57-120). */
+typedef struct {
+    double g;
+    double epsilon;
+    double H0;
+    double minimum_allowed_height;
+    double maximum_allowed_speed;
+    double beta_w, beta_w_dry, beta_uh, beta_uh_dry, beta_vh, beta_vh_dry;
+    double alpha_balance;
+    double CFL;
+    double evolve_max_timestep;
+    double evolve_min_timestep;
+    int64_t tight_slope_limiters;
+    int64_t use_centroid_velocities;
+    int64_t optimise_dry_cells;
+    int64_t extrapolate_velocity_second_order;
+    int64_t use_sloped_mannings;
+    int64_t max_smallsteps;
+    int64_t default_order;
+} swgpu_params;
+
+/* Evolve state kept on the device (Domain time bookkeeping,
+ * gpu_domain_advanced.py:2476-2675). */
+typedef struct {
+    double time;
+    double yieldtime;
+    double finaltime;          /* <= 0: none */
+    double timestep;           /* last dt */
+    double flux_timestep;      /* last CFL flux timestep (before CFL factor) */
+    double recorded_max_timestep;
+    double recorded_min_timestep;
+    int64_t order;             /* current _order_ */
+    int64_t smallsteps;
+    int64_t number_of_steps;   /* since last yield */
+    int64_t total_steps;       /* since evolve_start */
+    int64_t stop_reason;       /* 0 none, 1 yield, 2 finaltime, 3 step budget, 4 error */
+    int64_t status;            /* swgpu_status of a device-side failure */
+} swgpu_state;
+
+/* ---- lifetime --------------------------------------------------------- */
+
+/* Allocates the device copy of the mesh and all quantity arrays on the
+ * current CUDA device and renumbers nothing (the caller's triangle order is
+ * kept).  Replaces allocate_device_array + asynchronous_transfer
+ * (gpu_domain_advanced.py:582-903) and equip_kernel_functions (:186-507). */
+int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params,
+                 int precision, void **handle_out);
+
+/* Frees everything the handle owns.  No counterpart in the reference (its
+ * PyCUDA allocations are released by the garbage collector). */
+int swgpu_destroy(void *handle);
+
+/* Message for the last failing call on this handle (never NULL). */
+const char *swgpu_last_error(void *handle);
+
+/* Device and build description, e.g. "NVIDIA GB300 sm_103 (libswgpu 1)". */
+int swgpu_device_info(char *buf, int buflen);
+
+/* ---- quantities and boundaries --------------------------------------- */
+
+/* Uploads one quantity (Quantity.set_values + the H2D copy of
+ * asynchronous_transfer).  centroid may not be NULL; vertex / edge may be
+ * NULL (left unchanged).  Uploading stage or momentum marks the vertex and
+ * edge values stale until the next distribute. */
+int swgpu_set_quantity(void *handle, int quantity, const double *centroid,
+                       const double *vertex, const double *edge);
+
+/* Downloads one quantity (the reference's copy_back path).  Any output
+ * pointer may be NULL.  Derived quantities (height, velocities) are
+ * computed on demand from the conserved ones (update_other_quantities,
+ * gpu_domain_advanced.py:2114-2151). */
+int swgpu_get_quantity(void *handle, int quantity, double *centroid,
+                       double *vertex, double *edge);
+
+/* Boundary values of slot m for stage/xmomentum/ymomentum/elevation. */
+int swgpu_get_boundary_values(void *handle, int quantity, double *out);
+
+/* explicit_update (stage/xmom/ymom) or semi_implicit_update (xmom/ymom). */
+int swgpu_get_explicit_update(void *handle, int quantity, double *out);
+int swgpu_get_semi_implicit_update(void *handle, int quantity, double *out);
+
+/* Installs the boundary tag table (Domain.set_boundary).  Every tag index
+ * used by mesh->boundary_tag must be < ntags. */
+int swgpu_set_boundary_tags(void *handle, const swgpu_boundary_tag *tags,
+                            int ntags);
+
+/* ---- per-method entry points (gpu_domain_advanced.py) ---------------- */
+
+/* protect_against_infinitesimal_and_negative_heights (:1003-1055). */
+int swgpu_protect(void *handle);
+
+/* distribute_to_vertices_and_edges (:1744-2001): protect, extrapolation of
+ * the current order (extrapolate_second_order_sw :1061-1161 or
+ * extrapolate_first_order), balance_deep_and_shallow (:957-995) and
+ * interpolate_from_vertices_to_edges (:1975-1986). */
+int swgpu_distribute_to_vertices_and_edges(void *handle);
+
+/* update_boundary (:2006-2108), evaluated at the handle's model time. */
+int swgpu_update_boundary(void *handle);
+
+/* compute_fluxes (:1595-1696): central-upwind flux and gravity_wb into
+ * explicit_update; returns the minimum flux timestep (the host min of the
+ * reference's timestep_array, :1684) in *flux_timestep. */
+int swgpu_compute_fluxes(void *handle, double *flux_timestep);
+
+/* compute_forcing_terms -> manning_friction_implicit (:1255-1324). */
+int swgpu_compute_forcing_terms(void *handle);
+
+/* update_conserved_quantities (:1412-1442) with the given dt. */
+int swgpu_update_conserved_quantities(void *handle, double timestep);
+
+/* update_other_quantities (:2114-2151) materialised for download. */
+int swgpu_update_other_quantities(void *handle);
+
+/* Total water volume sum(area*(stage-elevation)) (FP64 reduction). */
+int swgpu_mass(void *handle, double *mass);
+
+/* ---- evolve (the device-resident loop) ------------------------------- */
+
+/* Read / overwrite the device-side time bookkeeping (set_time, _order_,
+ * yieldtime, ...). */
+int swgpu_get_state(void *handle, swgpu_state *state);
+int swgpu_set_state(void *handle, const swgpu_state *state);
+
+/* The set-up half of Domain.evolve (:2476-2551): distribute, time reset,
+ * counters, second distribute, update_boundary. */
+int swgpu_evolve_start(void *handle, double starttime, double yieldstep,
+                       double finaltime);
+
+/* The hot loop of Domain.evolve (:2555-2675): Euler steps with the
+ * timestep computed on the device, until the next yield time, the final
+ * time, or max_steps steps (max_steps <= 0: no limit).  Steps run as CUDA
+ * graphs of several steps; the host synchronises only between graphs.
+ * On return *state holds the device state; stop_reason says why it
+ * stopped.  After a yield, call again to continue (the library advances
+ * yieldtime by yieldstep). */
+int swgpu_evolve_run(void *handle, int64_t max_steps, swgpu_state *state);
+
+/* One Euler step exactly as evolve_one_euler_step (:2178-2191) followed
+ * by the time update, distribute and update_boundary of the loop body,
+ * issued kernel by kernel without a graph (for tests and co-testing). */
+int swgpu_evolve_one_step(void *handle, swgpu_state *state);
+
+/* swgpu_evolve_run with CUDA events recorded on the handle's stream before
+ * the first and after the last graph of the run: *elapsed_ms is the device
+ * time of the whole run.  No reference counterpart (the reference times its
+ * evolve loop with host clocks, gpu_domain_advanced.py:2418-2436, 2678-2688). */
+int swgpu_evolve_run_timed(void *handle, int64_t max_steps, swgpu_state *state,
+                           double *elapsed_ms);
+
+/* Runs nsteps Euler steps kernel by kernel (no graph) with a CUDA event
+ * between kernels and returns the summed device time of each kernel:
+ * ms[0] flux + gravity, ms[1] update, ms[2] extrapolation/balance/boundary.
+ * For per-kernel rooflines.  No reference counterpart (the reference's
+ * per-kernel times come from the legacy command-line profiler). */
+int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms);
+
+/* Synchronises the handle's stream. */
+int swgpu_synchronize(void *handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWGPU_H */

@@ -1,0 +1,85 @@
+"""The oracle's restatement against the reference's own compiled ANUGA C
+kernels on freshly generated inputs (more seeds and parameter variants than
+the golden fixtures).  Needs the reference sources, so it is skipped where
+they are absent (the golden-fixture tests cover those machines)."""
+import numpy as np
+import pytest
+
+from helpers import bits_equal
+
+VARIANTS = [
+    {},
+    {"beta_w_dry": 0.2, "beta_uh_dry": 0.1, "beta_vh_dry": 0.3},
+    {"extrapolate_velocity_second_order": 0},
+    {"tight_slope_limiters": 0, "alpha_balance": 1.5},
+    {"use_centroid_velocities": 0},
+    {"use_sloped_mannings": 1},
+    {"maximum_allowed_speed": 0.5},
+    {"optimise_dry_cells": 0},
+]
+
+
+@pytest.fixture(scope="module")
+def ref(oracle_mod):
+    if not oracle_mod.reference_available():
+        pytest.skip("reference sources not present (oracle/_ref not built)")
+    return oracle_mod.ReferenceKernels()
+
+
+def _pair(O, sc, params):
+    a = O.OracleDomain(sc.mesh, params, sc.oracle_tags())
+    b = O.OracleDomain(sc.mesh, params, sc.oracle_tags())
+    sc.apply_to_oracle(a)
+    sc.apply_to_oracle(b)
+    return a, b
+
+
+@pytest.mark.parametrize("variant", range(len(VARIANTS)))
+@pytest.mark.parametrize("seed", [3, 4])
+def test_each_kernel_bitwise(oracle_mod, ref, variant, seed):
+    from anuga_cuda import DEFAULT, scenarios
+    params = DEFAULT.replace(**VARIANTS[variant])
+    sc = scenarios.small_basin(10, 8, seed=seed)
+    a, b = _pair(oracle_mod, sc, params)
+    for step in range(6):  # a few steps so the state is no longer the initial one
+        a.protect(); ref.protect(b)
+        for q in ("stage", "xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_centroid_values"], b.arrays[q + "_centroid_values"])
+        a.extrapolate_second_order_sw(); ref.extrapolate_second_order_sw(b)
+        a.balance_deep_and_shallow(); ref.balance_deep_and_shallow(b)
+        a.interpolate_to_edges(); ref.interpolate_to_edges(b)
+        for q in ("stage", "xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_vertex_values"], b.arrays[q + "_vertex_values"]), q
+            assert bits_equal(a.arrays[q + "_edge_values"], b.arrays[q + "_edge_values"]), q
+        a.update_boundary(); b.update_boundary()
+        fa, fb = a.compute_fluxes(), ref.compute_fluxes(b)
+        assert bits_equal([fa], [fb])
+        a.gravity_wb(); ref.gravity_wb(b)
+        for q in ("stage", "xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_explicit_update"], b.arrays[q + "_explicit_update"])
+        a.manning_friction(); ref.manning_friction(b)
+        for q in ("xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_semi_implicit_update"],
+                              b.arrays[q + "_semi_implicit_update"])
+        dt = 0.9 * fa
+        assert a.update_conserved_quantities(dt) == 0 and ref.update(b, dt) == 0
+        for q in ("stage", "xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_centroid_values"], b.arrays[q + "_centroid_values"])
+
+
+def test_harbour_mesh_kernels_bitwise(oracle_mod, ref):
+    from anuga_cuda import DEFAULT, scenarios
+    sc = scenarios.tidal_harbour(target_triangles=3000, seed=5)
+    a, b = _pair(oracle_mod, sc, DEFAULT)
+    for _ in range(3):
+        a.distribute_to_vertices_and_edges()
+        ref.protect(b); ref.extrapolate_second_order_sw(b); ref.balance_deep_and_shallow(b)
+        ref.interpolate_to_edges(b)
+        a.update_boundary(); b.update_boundary()
+        fa, fb = a.compute_fluxes(), ref.compute_fluxes(b)
+        assert bits_equal([fa], [fb])
+        a.gravity_wb(); ref.gravity_wb(b)
+        a.manning_friction(); ref.manning_friction(b)
+        assert a.update_conserved_quantities(fa) == 0 and ref.update(b, fa) == 0
+        for q in ("stage", "xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_centroid_values"], b.arrays[q + "_centroid_values"])

@@ -479,9 +479,14 @@ class GPU_domain:
         device state."""
         if yieldstep is None:
             yieldstep = 1.0e300
+        if nsteps < 0:
+            raise ValueError("nsteps must be >= 0")
         check(lib().swgpu_evolve_start(self._h, self.starttime, float(yieldstep),
                                        -1.0 if finaltime is None else float(finaltime)), self._h)
         st = _lib.State_t()
+        if nsteps == 0:  # the library reads a zero budget as "no limit"
+            check(lib().swgpu_get_state(self._h, C.byref(st)), self._h)
+            return st
         check(lib().swgpu_evolve_run(self._h, int(nsteps), C.byref(st)), self._h)
         return st
 

@@ -489,6 +489,21 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
     P.use_sloped_mannings = (int)params->use_sloped_mannings;
     P.max_smallsteps = (int)params->max_smallsteps;
     P.default_order = (int)params->default_order;
+    P.f_g = (float)P.g;
+    P.f_eps = (float)P.epsilon;
+    P.f_H0 = (float)P.H0;
+    P.f_h0 = (float)(P.H0 * P.H0);
+    P.f_lim = (float)(10 * P.H0);
+    P.f_mah = (float)P.minimum_allowed_height;
+    P.f_mas = (float)P.maximum_allowed_speed;
+    P.f_max_dt = (float)std::min(P.evolve_max_timestep, 3.0e38);
+    P.f_alpha = (float)P.alpha_balance;
+    P.f_beta_w = (float)P.beta_w;
+    P.f_beta_w_dry = (float)P.beta_w_dry;
+    P.f_beta_uh = (float)P.beta_uh;
+    P.f_beta_uh_dry = (float)P.beta_uh_dry;
+    P.f_beta_vh = (float)P.beta_vh;
+    P.f_beta_vh_dry = (float)P.beta_vh_dry;
     if (!(P.evolve_max_timestep > 0) || (P.default_order != 1 && P.default_order != 2)) {
         fail(h, SWGPU_EINVAL, "evolve_max_timestep must be > 0 and default_order 1 or 2");
         g_create_error = h->err;

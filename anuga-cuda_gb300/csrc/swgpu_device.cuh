@@ -62,7 +62,7 @@ struct StepClock {
 
 // ANUGA Generic_Domain.update_timestep as restated in
 // src/anuga_HMPP/evolve.c:115-160 (finaltime clamp as finaltime - time).
-// Every thread evaluates it on the same snapshot and gets the same dt.
+// Each block evaluates it on the same snapshot and gets the same dt.
 __device__ __forceinline__ StepClock device_update_timestep(const Ctrl *c, const DevParams &P) {
     StepClock s;
     s.ftmin = __longlong_as_double((long long)c->ftmin_bits);
@@ -89,6 +89,16 @@ __device__ __forceinline__ StepClock device_update_timestep(const Ctrl *c, const
     if (c->time + dt > c->yieldtime) dt = c->yieldtime - c->time;
     s.dt = dt;
     return s;
+}
+
+// The step's clock evaluated once per block (thread 0) and broadcast through
+// shared memory: every block derives the same dt from the same snapshot.
+// Must be reached by all threads of the block.
+__device__ __forceinline__ StepClock block_step_clock(const Ctrl *c, const DevParams &P) {
+    __shared__ StepClock sclk;
+    if (threadIdx.x == 0) sclk = device_update_timestep(c, P);
+    __syncthreads();
+    return sclk;
 }
 
 // Called by thread 0 of each block after the block's work; returns true in
@@ -123,6 +133,30 @@ __device__ __forceinline__ void block_min_timestep(double t, Ctrl *ctrl) {
                 set_status(ctrl, SWGPU_ENONFINITE);  // NaN reached the timestep
             } else if (bits < *(volatile unsigned long long *)&ctrl->ftmin_bits) {
                 atomicMin(&ctrl->ftmin_bits, bits);
+            }
+        }
+    }
+}
+
+// FP32 variant for the mixed flux: the reduction stays in FP32 and only the
+// block's minimum is widened for the atomic.
+__device__ __forceinline__ void block_min_timestep_f(float t, Ctrl *ctrl) {
+    __shared__ float wminf[kBlock / 32];
+    for (int o = 16; o > 0; o >>= 1) t = ominf(t, __shfl_xor_sync(0xffffffffu, t, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wminf[warp] = t;
+    __syncthreads();
+    if (warp == 0) {
+        t = lane < (int)(blockDim.x >> 5) ? wminf[lane] : 3.0e38f;
+        for (int o = 16; o > 0; o >>= 1) t = ominf(t, __shfl_xor_sync(0xffffffffu, t, o));
+        if (lane == 0) {
+            if (!(t >= 0.0f)) {
+                set_status(ctrl, SWGPU_ENONFINITE);
+            } else {
+                const double td = (double)t;
+                const unsigned long long bits = (unsigned long long)__double_as_longlong(td);
+                if (bits < *(volatile unsigned long long *)&ctrl->ftmin_bits)
+                    atomicMin(&ctrl->ftmin_bits, bits);
             }
         }
     }

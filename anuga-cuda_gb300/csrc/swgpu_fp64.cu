@@ -11,7 +11,7 @@
 //                   centric, neighbour edge values gathered), summed in
 //                   ANUGA's order, gravity_wb, per-triangle CFL timestep ->
 //                   block min -> atomicMin into Ctrl
-//   update_fp64     update_timestep (every thread, same snapshot), Manning
+//   update_fp64     update_timestep (once per block, same snapshot), Manning
 //                   friction, the semi-implicit conserved update, protect,
 //                   centroid velocities for the next extrapolation; the last
 //                   block advances the model time
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
     if (fused && ctrl_halted(ctrl)) return;
     StepClock clk;
     if (fused) {
-        clk = device_update_timestep(ctrl, P);
+        clk = block_step_clock(ctrl, P);
     } else {
         clk.dt = dt_api;
     }

@@ -83,6 +83,10 @@ struct DevParams {
     int tight_slope_limiters, use_centroid_velocities, optimise_dry_cells;
     int extrapolate_velocity_second_order, use_sloped_mannings;
     int max_smallsteps, default_order;
+    // FP32 copies for the mixed kernels (set on the host; FP64 arithmetic
+    // on GB300 runs at 1/64 of the FP32 rate, so none is done per thread)
+    float f_g, f_eps, f_H0, f_h0, f_lim, f_mah, f_mas, f_max_dt, f_alpha;
+    float f_beta_w, f_beta_w_dry, f_beta_uh, f_beta_uh_dry, f_beta_vh, f_beta_vh_dry;
 };
 
 struct BcTag {

@@ -91,10 +91,10 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     const int N = M.N;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    float t = (float)fmin(P.evolve_max_timestep, 3.0e38);
+    float t = P.f_max_dt;
     if (k < N) {
-        const float g = (float)P.g, eps = (float)P.epsilon;
-        const float h0 = (float)(P.H0 * P.H0), lim = (float)(10 * P.H0);
+        const float g = P.f_g, eps = P.f_eps;
+        const float h0 = P.f_h0, lim = P.f_lim;
         float vh[3], vu[3], vv[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
         X.euh[k] = a1 * inv_area - g * wx * avg_h - sx * inv_area;
         X.evh[k] = a2 * inv_area - g * wy * avg_h - sy * inv_area;
     }
-    block_min_timestep((double)t, ctrl);
+    block_min_timestep_f(t, ctrl);
 }
 
 // Update in FP64: h += dt*E, q = (q + dt*E) * 1/(1 - dt*S) with the Manning
@@ -160,14 +160,14 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
 __global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, DevMixed X,
                                                        DevParams P, Ctrl *ctrl, int flags) {
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
-    const StepClock clk = device_update_timestep(ctrl, P);
+    const StepClock clk = block_step_clock(ctrl, P);
     const double dt = clk.dt;
     const float dtf = (float)dt;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int bad = 0;
     if (k < M.N) {
         double h = X.hd[k], uh = S.uh[k], vh = S.vh[k];
-        const float mah = (float)P.minimum_allowed_height;
+        const float mah = P.f_mah;
         // Manning friction on the pre-update state
         float r = 1.0f;
         const float eta = X.fric[k];
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, De
             const float hm = (float)h - X.zmoff[k];
             if (hm >= mah) {
                 const float uf = (float)uh, vf = (float)vh;
-                const float Sf = -(float)P.g * eta * eta * sqrtf(uf * uf + vf * vf) /
+                const float Sf = -P.f_g * eta * eta * sqrtf(uf * uf + vf * vf) /
                                  exp2f((7.0f / 3.0f) * log2f(hm));
                 const float den = 1.0f - dtf * Sf;
                 if (!(den > 0.0f)) bad = 1;
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, De
         vh = (vh + dt * (double)X.evh[k]) * (double)r;
         // protect (shallow_water_ext.c:1638-1705) on depth
         if (h < P.minimum_allowed_height) {
-            if (P.maximum_allowed_speed < P.epsilon) {
+            if (P.f_mas < P.f_eps) {
                 uh = 0.0;
                 vh = 0.0;
                 if (h <= 0.0) h = 0.0;
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int bad_bc = 0;
     if (k < N) {
-        const float mah = (float)P.minimum_allowed_height;
+        const float mah = P.f_mah;
         const float hc = X.hf[k];
         const float qu = X.uvel[k], qv = X.vvel[k];
         const bool vel = P.extrapolate_velocity_second_order == 1;
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                     const float h0 = X.hf[k0], h1 = X.hf[k1], h2 = X.hf[k2];
                     const float hmin = ominf(ominf(h0, ominf(h1, h2)), hc);
                     const float hmax = omaxf(h0, omaxf(h1, h2));
-                    if (P.optimise_dry_cells && hmax < (float)P.epsilon) {
+                    if (P.optimise_dry_cells && hmax < P.f_eps) {
                         keep = true;
                     } else {
                         float hfactor = 0.0f;
@@ -323,26 +323,26 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                         const float dq1 = (h1 - h0) + (z1 - z0);
                         const float dq2 = (h2 - h0) + (z2 - z0);
                         aux_jumps_f(dq0, dq1, dq2, c,
-                                    (float)(P.beta_w_dry + (P.beta_w - P.beta_w_dry) * hfactor),
+                                    P.f_beta_w_dry + (P.f_beta_w - P.f_beta_w_dry) * hfactor,
                                     dw);
                         const float u0 = vel ? X.uvel[k0] : X.uvel[k0] * omaxf(h0, mah);
                         const float u1 = vel ? X.uvel[k1] : X.uvel[k1] * omaxf(h1, mah);
                         const float u2 = vel ? X.uvel[k2] : X.uvel[k2] * omaxf(h2, mah);
                         aux_jumps_f(u0 - cu, u1 - u0, u2 - u0, c,
-                                    (float)(P.beta_uh_dry + (P.beta_uh - P.beta_uh_dry) * hfactor),
+                                    P.f_beta_uh_dry + (P.f_beta_uh - P.f_beta_uh_dry) * hfactor,
                                     du);
                         const float v0 = vel ? X.vvel[k0] : X.vvel[k0] * omaxf(h0, mah);
                         const float v1 = vel ? X.vvel[k1] : X.vvel[k1] * omaxf(h1, mah);
                         const float v2 = vel ? X.vvel[k2] : X.vvel[k2] * omaxf(h2, mah);
                         aux_jumps_f(v0 - cv, v1 - v0, v2 - v0, c,
-                                    (float)(P.beta_vh_dry + (P.beta_vh - P.beta_vh_dry) * hfactor),
+                                    P.f_beta_vh_dry + (P.f_beta_vh - P.f_beta_vh_dry) * hfactor,
                                     dv);
                     }
                 } else {
                     const int slot = (kind >> 2) & 3;
                     const int k1 = M.surr[slot * N + k];
                     const float h1 = X.hf[k1];
-                    const float beta = (float)P.beta_w;
+                    const float beta = P.f_beta_w;
                     one_jumps_f((h1 - hc) + X.dzn[slot * N + k], c, beta, dw);
                     const float u1 = vel ? X.uvel[k1] : X.uvel[k1] * omaxf(h1, mah);
                     const float v1 = vel ? X.vvel[k1] : X.vvel[k1] * omaxf(h1, mah);
@@ -392,14 +392,14 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
         }
         // balance_deep_and_shallow on depths (w_v - z_v = h_v)
         {
-            const float H0 = (float)P.H0;
+            const float H0 = P.f_H0;
             const float hmin = ominf(oh[0], ominf(oh[1], oh[2]));
             float alpha = 1.0f;
             if (P.tight_slope_limiters == 0) {
                 float dz = 0.0f;
 #pragma unroll
                 for (int i = 0; i < 3; i++) dz = omaxf(dz, fabsf(dzv[i]));
-                alpha = dz > 0.0f ? omaxf(ominf((float)P.alpha_balance * hmin / dz, 1.0f), 0.0f)
+                alpha = dz > 0.0f ? omaxf(ominf(P.f_alpha * hmin / dz, 1.0f), 0.0f)
                                   : 1.0f;
             } else if (hmin < H0) {
 #pragma unroll
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
     double h = from_stage ? S.w[k] - S.zc[k] : X.hd[k];
     double uh = S.uh[k], vh = S.vh[k];
     if (h < P.minimum_allowed_height) {
-        if (P.maximum_allowed_speed < P.epsilon) {
+        if (P.f_mas < P.f_eps) {
             uh = 0.0;
             vh = 0.0;
             if (h <= 0.0) h = 0.0;
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
     X.hd[k] = h;
     S.uh[k] = uh;
     S.vh[k] = vh;
-    const float hf = (float)h, mah = (float)P.minimum_allowed_height;
+    const float hf = (float)h, mah = P.f_mah;
     X.hf[k] = hf;
     X.uvel[k] = (float)uh / omaxf(hf, mah);
     X.vvel[k] = (float)vh / omaxf(hf, mah);

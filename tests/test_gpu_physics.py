@@ -1,0 +1,118 @@
+"""Known-answer and invariant tests on the GPU, both precisions:
+well-balanced lake at rest (the reference's only known-answer test,
+src/anuga_cuda/anuga_gpu/mytest.py:11-34, generalised to a sloping bed),
+volume conservation between reflective walls, mirror symmetry of the dam
+break, mixed-precision error against FP64, and clean error statuses."""
+import numpy as np
+import pytest
+
+from helpers import gpu_from_scenario, max_rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _lake(precision, level=0.4):
+    from anuga_cuda import DEFAULT, scenarios
+    from anuga_cuda.boundaries import Reflective_boundary
+    sc = scenarios.small_basin(10, 8, seed=0, wet_dry_front=False)
+    zc = sc.elevation_vertex.mean(axis=1)
+    sc.stage_centroid = np.maximum(zc, level)
+    sc.xmom_centroid = np.zeros(sc.N)
+    sc.ymom_centroid = np.zeros(sc.N)
+    sc.boundaries = {t: Reflective_boundary() for t in sc.mesh.tag_names}
+    return gpu_from_scenario(sc, DEFAULT, precision), sc
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lake_at_rest_stays_at_rest(precision, swgpu_built):
+    d, sc = _lake(precision)
+    w0 = d.quantities["stage"].centroid_values.copy()
+    d.evolve_steps(50)
+    w = d.quantities["stage"].centroid_values
+    u = d.quantities["xmomentum"].centroid_values
+    tol = 1e-12 if precision == "fp64" else 2e-5
+    wet = sc.stage_centroid > sc.elevation_vertex.mean(axis=1) + 1e-3
+    assert np.max(np.abs(w - w0)[wet]) < tol
+    assert np.max(np.abs(u)) < tol
+
+
+def test_four_triangle_known_answer(swgpu_built):
+    """Constant stage 1 over constant bed -1: the pressure terms cancel and
+    the central triangle's explicit update is zero."""
+    from anuga_cuda import GPU_domain
+    pts = [[0.0, 0.0], [0.0, 2.0], [2.0, 0.0], [0.0, 4.0], [2.0, 2.0], [4.0, 0.0]]
+    tris = [[1, 0, 2], [1, 2, 4], [4, 2, 5], [3, 1, 4]]
+    d = GPU_domain(pts, tris, reorder=False)
+    d.set_quantity("elevation", -1.0)
+    d.set_quantity("stage", 1.0)
+    d.distribute_to_vertices_and_edges()
+    d.update_boundary()
+    d.compute_fluxes()
+    for q in ("stage", "xmomentum", "ymomentum"):
+        assert abs(d.quantities[q].explicit_update[1]) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_volume_conserved_between_walls(precision, swgpu_built):
+    from anuga_cuda import DEFAULT, scenarios
+    sc = scenarios.dam_break(40, 40)
+    d = gpu_from_scenario(sc, DEFAULT, precision)
+    v0 = d.get_water_volume()
+    d.evolve_steps(200)
+    v1 = d.get_water_volume()
+    assert abs(v1 - v0) <= (1e-12 if precision == "fp64" else 1e-9) * abs(v0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_dam_break_mirror_symmetry(precision, swgpu_built):
+    """The rectangular_cross mesh and the dam are symmetric under y -> 100-y,
+    so stage is too and y-momentum is antisymmetric."""
+    from anuga_cuda import DEFAULT, scenarios
+    sc = scenarios.dam_break(30, 30)
+    d = gpu_from_scenario(sc, DEFAULT, precision)
+    d.evolve_steps(100)
+    c = sc.mesh.centroid_coordinates
+    key = np.round(c * 1e6).astype(np.int64)
+    index = {(x, y): i for i, (x, y) in enumerate(map(tuple, key))}
+    mirror = np.array([index[(x, 100_000_000 - y)] for x, y in map(tuple, key)])
+    w = d.quantities["stage"].centroid_values
+    vh = d.quantities["ymomentum"].centroid_values
+    tol = 1e-9 if precision == "fp64" else 1e-5
+    assert np.max(np.abs(w - w[mirror])) < tol
+    assert np.max(np.abs(vh + vh[mirror])) < tol
+
+
+def test_mixed_close_to_fp64_on_harbour(swgpu_built):
+    from anuga_cuda import DEFAULT, scenarios
+    sc = scenarios.tidal_harbour(target_triangles=6000, seed=4)
+    a = gpu_from_scenario(sc, DEFAULT, "fp64")
+    b = gpu_from_scenario(sc, DEFAULT, "mixed")
+    sa = a.evolve_steps(300)
+    sb = b.evolve_steps(300)
+    assert abs(sa.time - sb.time) <= 1e-5 * sa.time
+    err = max_rel(b.quantities["stage"].centroid_values, a.quantities["stage"].centroid_values)
+    assert err < 1e-4, err
+
+
+def test_nan_input_reports_status(swgpu_built):
+    from anuga_cuda import DEFAULT, scenarios
+    from anuga_cuda._lib import SwgpuError
+    sc = scenarios.small_basin(8, 6, seed=1, wet_dry_front=False)
+    sc.stage_centroid = sc.stage_centroid.copy()
+    sc.stage_centroid[5] = np.nan
+    d = gpu_from_scenario(sc, DEFAULT, "fp64")
+    with pytest.raises(SwgpuError) as e:
+        d.evolve_steps(5)
+    assert e.value.status in (6, 4)   # ENONFINITE (or EDENOMINATOR from a NaN)
+
+
+def test_unknown_boundary_type_rejected(swgpu_built):
+    from anuga_cuda import DEFAULT, GPU_domain, _lib, scenarios
+    from anuga_cuda._lib import SwgpuError, check, lib
+    sc = scenarios.small_basin(6, 5, seed=1)
+    d = gpu_from_scenario(sc, DEFAULT, "fp64")
+    arr = (_lib.BoundaryTag_t * len(sc.mesh.tag_names))()
+    arr[0].type = 17
+    with pytest.raises(SwgpuError):
+        check(lib().swgpu_set_boundary_tags(d._h, arr, len(sc.mesh.tag_names)), d._h)
+    _ = GPU_domain

@@ -6,7 +6,8 @@ Three translation units are compiled in parallel and linked into
 * ``csrc/swgpu_fp64.cu``  -- the FP64 parity kernels, ``--fmad=false`` so that
   no multiply-add is contracted (the reference's C kernels are built the same
   way by gcc on x86-64);
-* ``csrc/swgpu_mixed.cu`` -- the mixed-precision kernels (FMA allowed);
+* ``csrc/swgpu_mixed.cu`` -- the mixed-precision kernels (FMA allowed, FP32
+  division and square root approximate, denormals flushed);
 * ``csrc/swgpu_api.cu``   -- the C ABI, allocation and the evolve loop.
 """
 from __future__ import annotations
@@ -25,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 UNITS = {
     "swgpu_fp64.cu": ["--fmad=false"],
-    "swgpu_mixed.cu": [],
+    "swgpu_mixed.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "swgpu_api.cu": [],
 }
 

@@ -91,14 +91,15 @@ __device__ __forceinline__ StepClock device_update_timestep(const Ctrl *c, const
     return s;
 }
 
-// The step's clock evaluated once per block (thread 0) and broadcast through
-// shared memory: every block derives the same dt from the same snapshot.
-// Must be reached by all threads of the block.
-__device__ __forceinline__ StepClock block_step_clock(const Ctrl *c, const DevParams &P) {
-    __shared__ StepClock sclk;
-    if (threadIdx.x == 0) sclk = device_update_timestep(c, P);
-    __syncthreads();
-    return sclk;
+// The step's clock as published by the flux kernel's last block.
+__device__ __forceinline__ StepClock published_step_clock(const Ctrl *c) {
+    StepClock s;
+    s.dt = c->clk_dt;
+    s.ftmin = c->clk_ftmin;
+    s.order = c->clk_order;
+    s.smallsteps = c->clk_smallsteps;
+    s.small_error = c->clk_small_error;
+    return s;
 }
 
 // Called by thread 0 of each block after the block's work; returns true in
@@ -115,9 +116,21 @@ __device__ __forceinline__ bool last_block_done(unsigned int *counter) {
     return false;
 }
 
+// Last block of the flux kernel (all atomicMins of the step are done):
+// evaluate update_timestep once and publish it for the update kernel.
+__device__ __forceinline__ void publish_step_clock(Ctrl *c, const DevParams &P) {
+    const StepClock s = device_update_timestep(c, P);
+    c->clk_dt = s.dt;
+    c->clk_ftmin = s.ftmin;
+    c->clk_order = s.order;
+    c->clk_smallsteps = s.smallsteps;
+    c->clk_small_error = s.small_error;
+}
+
 // Block-wide minimum of a positive double, then one atomicMin on its bit
 // pattern (positive IEEE doubles order like their bits) only when it lowers
-// the running minimum.
+// the running minimum.  In the fused loop the last block then publishes the
+// step's clock.
 __device__ __forceinline__ void block_min_timestep(double t, Ctrl *ctrl) {
     __shared__ double wmin[kBlock / 32];
     for (int o = 16; o > 0; o >>= 1) t = omin(t, __shfl_xor_sync(0xffffffffu, t, o));

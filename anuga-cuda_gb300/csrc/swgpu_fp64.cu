@@ -11,7 +11,8 @@
 //                   centric, neighbour edge values gathered), summed in
 //                   ANUGA's order, gravity_wb, per-triangle CFL timestep ->
 //                   block min -> atomicMin into Ctrl
-//   update_fp64     update_timestep (once per block, same snapshot), Manning
+//   update_fp64     the step's update_timestep (evaluated once by the flux
+//                   kernel's last block), Manning
 //                   friction, the semi-implicit conserved update, protect,
 //                   centroid velocities for the next extrapolation; the last
 //                   block advances the model time
@@ -269,6 +270,8 @@ __global__ void __launch_bounds__(kBlock) flux_fp64(DevMesh M, DevState S, DevPa
     }
     if (bad) set_status(ctrl, SWGPU_EBED);
     block_min_timestep(t, ctrl);
+    if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
+        publish_step_clock(ctrl, P);
 }
 
 // ------------------------------------------------------------- update ---
@@ -368,13 +371,13 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
     if (fused && ctrl_halted(ctrl)) return;
     StepClock clk;
     if (fused) {
-        clk = block_step_clock(ctrl, P);
+        clk = published_step_clock(ctrl);
     } else {
         clk.dt = dt_api;
     }
     const double dt = clk.dt;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int bad = 0;
+    int bad = 0, nonfinite = 0;
     if (k < M.N) {
         double w = S.w[k], uh = S.uh[k], vh = S.vh[k];
         double su, sv;
@@ -408,11 +411,15 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
                 S.vvel[k] = vh / dk;
             }
         }
+        // NaN / Inf anywhere in the new state stops the run
+        const double big = 1.0e308;
+        if (!(fabs(w) <= big) || !(fabs(uh) <= big) || !(fabs(vh) <= big)) nonfinite = 1;
         S.w[k] = w;
         S.uh[k] = uh;
         S.vh[k] = vh;
     }
     if (bad) set_status(ctrl, SWGPU_EDENOMINATOR);
+    if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (fused) {
         __syncthreads();
         if (threadIdx.x == 0 && last_block_done(&ctrl->done_update)) commit_step(ctrl, clk, P);

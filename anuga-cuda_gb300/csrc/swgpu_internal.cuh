@@ -107,8 +107,10 @@ struct __align__(16) Ctrl {
     int halt_pending;               // stop reason raised by update, applied after distribute
     int stop_reason;
     int status;                     // first device-side failure (swgpu_status)
-    unsigned int done_update, done_distribute;
-    int pad[2];
+    unsigned int done_update, done_distribute, done_flux;
+    int clk_small_error;            // the step's update_timestep, evaluated once by
+    double clk_dt, clk_ftmin;       // the last block of the flux kernel and read
+    long long clk_order, clk_smallsteps;  // by the update kernel
 };
 
 enum StopReason { kStopNone = 0, kStopYield = 1, kStopFinal = 2, kStopBudget = 3, kStopError = 4 };

@@ -27,24 +27,38 @@
 
 namespace swgpu {
 
-__device__ __forceinline__ float limited_speed_f(float &uh, float &h, float eps, float h0,
-                                                 float lim) {
-    float u;
+// Read-only loads through the non-coherent path (the arrays a kernel reads
+// are never written by the same kernel).
+template <typename T>
+__device__ __forceinline__ T ro(const T *p) {
+    return __ldg(p);
+}
+
+// _compute_speed (shallow_water_ext.c:214-242) for both momentum components
+// of one side of an edge with a single division: for h < lim the limited
+// speed uh/(h + h0/h) is uh * h/(h*h + h0), and the momentum is reset to
+// speed * h.
+__device__ __forceinline__ void side_speed_f(float &h, float &uh, float &vh, float &u,
+                                             float eps, float h0, float lim) {
     if (h < lim) {
         if (h < eps) {
             h = 0.0f;
             u = 0.0f;
+            uh = 0.0f;
+            vh = 0.0f;
         } else {
-            u = uh / (h + h0 / h);
+            const float f = __fdividef(h, h * h + h0);
+            u = uh * f;
+            uh = u * h;
+            vh = (vh * f) * h;
         }
-        uh = u * h;
     } else {
-        u = uh / h;
+        u = __fdividef(uh, h);
     }
-    return u;
 }
 
-// Central-upwind flux on depths (rotated frame inside), FP32.
+// Central-upwind flux on depths (rotated frame inside), FP32.  The stage
+// jump equals the depth jump (bed continuous across the edge).
 __device__ __forceinline__ void central_flux_f(float hl_in, float uhl_in, float vhl_in,
                                                float hr_in, float uhr_in, float vhr_in, float n1,
                                                float n2, float g, float eps, float h0, float lim,
@@ -53,13 +67,10 @@ __device__ __forceinline__ void central_flux_f(float hl_in, float uhl_in, float 
     const float bl = -n2 * uhl_in + n1 * vhl_in;
     const float ar = n1 * uhr_in + n2 * vhr_in;
     const float br = -n2 * uhr_in + n1 * vhr_in;
-    float hl = hl_in, uhl = al;
-    const float ul = limited_speed_f(uhl, hl, eps, h0, lim);
-    float hr = hr_in, uhr = ar;
-    const float ur = limited_speed_f(uhr, hr, eps, h0, lim);
-    float vhl = bl, vhr = br;
-    limited_speed_f(vhl, hl, eps, h0, lim);
-    limited_speed_f(vhr, hr, eps, h0, lim);
+    float hl = hl_in, uhl = al, vhl = bl, ul;
+    float hr = hr_in, uhr = ar, vhr = br, ur;
+    side_speed_f(hl, uhl, vhl, ul, eps, h0, lim);
+    side_speed_f(hr, uhr, vhr, ur, eps, h0, lim);
     const float cl = sqrtf(g * hl), cr = sqrtf(g * hr);
     float smax = omaxf(ul + cl, ur + cr);
     if (smax < 0.0f) smax = 0.0f;
@@ -71,11 +82,10 @@ __device__ __forceinline__ void central_flux_f(float hl_in, float uhl_in, float 
         ms = 0.0f;
         return;
     }
-    const float inv = 1.0f / denom;
+    const float inv = __fdividef(1.0f, denom);
     const float ss = smax * smin;
     const float fl0 = ul * hl, fl1 = ul * uhl + 0.5f * g * hl * hl, fl2 = ul * vhl;
     const float fr0 = ur * hr, fr1 = ur * uhr + 0.5f * g * hr * hr, fr2 = ur * vhr;
-    // stage jump = depth jump (bed continuous across the edge)
     const float e0 = (smax * fl0 - smin * fr0 + ss * (hr_in - hl_in)) * inv;
     const float e1 = (smax * fl1 - smin * fr1 + ss * (ar - al)) * inv;
     const float e2 = (smax * fl2 - smin * fr2 + ss * (br - bl)) * inv;
@@ -98,40 +108,41 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
         float vh[3], vu[3], vv[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            vh[i] = X.hv[i * N + k];
-            vu[i] = X.uhv[i * N + k];
-            vv[i] = X.vhv[i * N + k];
+            vh[i] = ro(X.hv + i * N + k);
+            vu[i] = ro(X.uhv + i * N + k);
+            vv[i] = ro(X.vhv + i * N + k);
         }
         const float he[3] = {0.5f * (vh[1] + vh[2]), 0.5f * (vh[0] + vh[2]), 0.5f * (vh[0] + vh[1])};
         const float ue[3] = {0.5f * (vu[1] + vu[2]), 0.5f * (vu[0] + vu[2]), 0.5f * (vu[0] + vu[1])};
         const float ve[3] = {0.5f * (vv[1] + vv[2]), 0.5f * (vv[0] + vv[2]), 0.5f * (vv[0] + vv[1])};
-        const float rk = X.radius[k];
-        const float inv_area = X.inv_area[k];
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;       // flux sums
+        const float rk = ro(X.radius + k);
+        const float inv_area = ro(X.inv_area + k);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;            // flux sums
         float gx = 0.f, gy = 0.f, sx = 0.f, sy = 0.f;  // Green gradient, side term
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            const int pk = M.nbr[i * N + k];
-            const float n1 = X.nx[i * N + k], n2 = X.ny[i * N + k], L = X.len[i * N + k];
-            float hr, uhr, vhr, rn = 0.f;
-            bool interior = pk >= 0;
-            if (interior) {
+            const int pk = ro(M.nbr + i * N + k);
+            const float n1 = ro(X.nx + i * N + k), n2 = ro(X.ny + i * N + k);
+            const float L = ro(X.len + i * N + k);
+            float hr, uhr, vhr, rn = 3.0e38f;
+            if (pk >= 0) {
                 const int n = pk >> 2, m = pk & 3;
                 const int a = (m == 0) ? 1 : 0, b = (m == 2) ? 1 : 2;
-                hr = 0.5f * (X.hv[a * N + n] + X.hv[b * N + n]);
-                uhr = 0.5f * (X.uhv[a * N + n] + X.uhv[b * N + n]);
-                vhr = 0.5f * (X.vhv[a * N + n] + X.vhv[b * N + n]);
-                rn = X.radius[n];
+                hr = 0.5f * (ro(X.hv + a * N + n) + ro(X.hv + b * N + n));
+                uhr = 0.5f * (ro(X.uhv + a * N + n) + ro(X.uhv + b * N + n));
+                vhr = 0.5f * (ro(X.vhv + a * N + n) + ro(X.vhv + b * N + n));
+                rn = ro(X.radius + n);
             } else {
                 const int mb = -pk - 1;
-                hr = X.hbf[mb];
-                uhr = X.uhbf[mb];
-                vhr = X.vhbf[mb];
+                hr = ro(X.hbf + mb);
+                uhr = ro(X.uhbf + mb);
+                vhr = ro(X.vhbf + mb);
             }
             const float hl = he[i];
-            gx += hl * L * n1;
-            gy += hl * L * n2;
-            const float fact = -0.5f * g * hl * hl * L;
+            const float hlL = hl * L;
+            gx += hlL * n1;
+            gy += hlL * n2;
+            const float fact = -0.5f * g * hl * hlL;
             sx += fact * n1;
             sy += fact * n2;
             if (P.optimise_dry_cells && fabsf(hl) < eps && fabsf(hr) < eps) continue;
@@ -141,76 +152,101 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
             a1 -= f1 * L;
             a2 -= f2 * L;
             if (ms > eps) {
-                t = ominf(t, rk / ms);
-                if (interior) t = ominf(t, rn / ms);
+                // min(rk/ms, rn/ms) = min(rk, rn)/ms: one division per edge
+                t = ominf(t, __fdividef(fminf(rk, rn), ms));
             }
         }
-        const float avg_h = X.hf[k];
-        const float wx = gx * inv_area + X.zgrad[k];
-        const float wy = gy * inv_area + X.zgrad[N + k];
+        const float avg_h = ro(X.hf + k);
+        const float wx = gx * inv_area + ro(X.zgrad + k);
+        const float wy = gy * inv_area + ro(X.zgrad + N + k);
         X.ew[k] = a0 * inv_area;
         X.euh[k] = a1 * inv_area - g * wx * avg_h - sx * inv_area;
         X.evh[k] = a2 * inv_area - g * wy * avg_h - sy * inv_area;
     }
     block_min_timestep_f(t, ctrl);
+    if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
+        publish_step_clock(ctrl, P);
 }
 
-// Update in FP64: h += dt*E, q = (q + dt*E) * 1/(1 - dt*S) with the Manning
-// coefficient S and the reciprocal in FP32; protect; FP32 centroid copies.
+// Update: the conserved state stays FP64 and is advanced by increments
+// computed in FP32 (each increment is small against the value it is added
+// to, so its FP32 rounding is far below the FP32 resolution of the state;
+// the additions themselves are FP64):
+//   h  += dt*E_h
+//   q  += q*(r - 1) + dt*E_q*r,   r = 1/(1 - dt*S)  (semi-implicit Manning)
+// then protect and the FP32 centroid copies the next extrapolation reads.
 __global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, DevMixed X,
                                                        DevParams P, Ctrl *ctrl, int flags) {
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
-    const StepClock clk = block_step_clock(ctrl, P);
+    const StepClock clk = published_step_clock(ctrl);
     const double dt = clk.dt;
     const float dtf = (float)dt;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int bad = 0;
+    int bad = 0, nonfinite = 0;
     if (k < M.N) {
         double h = X.hd[k], uh = S.uh[k], vh = S.vh[k];
         const float mah = P.f_mah;
+        const float hf0 = ro(X.hf + k);  // FP32 copy of h written last step
+        const float uf = ro(X.uvel + k) * omaxf(hf0, mah);
+        const float vf = ro(X.vvel + k) * omaxf(hf0, mah);
         // Manning friction on the pre-update state
-        float r = 1.0f;
-        const float eta = X.fric[k];
+        float rm1 = 0.0f, r = 1.0f;  // r - 1 and r
+        const float eta = ro(X.fric + k);
         if (eta > mah) {
-            const float hm = (float)h - X.zmoff[k];
+            const float hm = hf0 - ro(X.zmoff + k);
             if (hm >= mah) {
-                const float uf = (float)uh, vf = (float)vh;
-                const float Sf = -P.f_g * eta * eta * sqrtf(uf * uf + vf * vf) /
-                                 exp2f((7.0f / 3.0f) * log2f(hm));
-                const float den = 1.0f - dtf * Sf;
+                const float Sf = -P.f_g * eta * eta * sqrtf(uf * uf + vf * vf) *
+                                 exp2f(-(7.0f / 3.0f) * __log2f(hm));
+                const float dS = dtf * Sf;         // <= 0
+                const float den = 1.0f - dS;
                 if (!(den > 0.0f)) bad = 1;
-                r = 1.0f / den;
+                r = __fdividef(1.0f, den);
+                rm1 = dS * r;                      // r - 1 without cancellation
             }
         }
-        h += dt * (double)X.ew[k];
-        uh = (uh + dt * (double)X.euh[k]) * (double)r;
-        vh = (vh + dt * (double)X.evh[k]) * (double)r;
+        const float dh = dtf * ro(X.ew + k);
+        const float du = uf * rm1 + dtf * ro(X.euh + k) * r;
+        const float dv = vf * rm1 + dtf * ro(X.evh + k) * r;
+        h += (double)dh;
+        uh += (double)du;
+        vh += (double)dv;
+        // FP32 copies re-derived from the FP64 state (no drift between them)
+        float hf = (float)h;
+        float uhf = (float)uh, vhf = (float)vh;
         // protect (shallow_water_ext.c:1638-1705) on depth
-        if (h < P.minimum_allowed_height) {
+        if (hf < mah) {
             if (P.f_mas < P.f_eps) {
-                uh = 0.0;
-                vh = 0.0;
-                if (h <= 0.0) h = 0.0;
+                uh = vh = 0.0;
+                uhf = vhf = 0.0f;
+                if (h <= 0.0) {
+                    h = 0.0;
+                    hf = 0.0f;
+                }
             } else if (h <= 0.0) {
-                h = 0.0;
-                uh = 0.0;
-                vh = 0.0;
+                h = uh = vh = 0.0;
+                hf = uhf = vhf = 0.0f;
             } else {
-                const double u = uh / h, v = vh / h, ms = P.maximum_allowed_speed;
-                if (fabs(u) > ms) uh = (u > 0 ? ms : -ms) * h;
-                if (fabs(v) > ms) vh = (v > 0 ? ms : -ms) * h;
+                const float u = uhf / hf, v = vhf / hf, ms = P.f_mas;
+                if (fabsf(u) > ms) uhf = (u > 0 ? ms : -ms) * hf;
+                if (fabsf(v) > ms) vhf = (v > 0 ? ms : -ms) * hf;
+                uh = (double)uhf;
+                vh = (double)vhf;
             }
         }
+        // NaN / Inf anywhere in the new state stops the run (FP32 copies:
+        // a non-finite FP64 value stays non-finite when narrowed)
+        if (!(fabsf(hf) <= 3.0e38f) || !(fabsf(uhf) <= 3.0e38f) || !(fabsf(vhf) <= 3.0e38f))
+            nonfinite = 1;
         X.hd[k] = h;
         S.uh[k] = uh;
         S.vh[k] = vh;
-        const float hf = (float)h;
         X.hf[k] = hf;
-        const float dk = omaxf(hf, mah);
-        X.uvel[k] = (float)uh / dk;
-        X.vvel[k] = (float)vh / dk;
+        const float inv = __fdividef(1.0f, omaxf(hf, mah));
+        X.uvel[k] = uhf * inv;
+        X.vvel[k] = vhf * inv;
     }
     if (bad) set_status(ctrl, SWGPU_EDENOMINATOR);
+    if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (flags & kFused) {
         __syncthreads();
         if (threadIdx.x == 0 && last_block_done(&ctrl->done_update)) commit_step(ctrl, clk, P);
@@ -286,30 +322,30 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
     int bad_bc = 0;
     if (k < N) {
         const float mah = P.f_mah;
-        const float hc = X.hf[k];
-        const float qu = X.uvel[k], qv = X.vvel[k];
+        const float hc = ro(X.hf + (k));
+        const float qu = ro(X.uvel + (k)), qv = ro(X.vvel + (k));
         const bool vel = P.extrapolate_velocity_second_order == 1;
         // centroid momentum (uvel = uh / max(h, mah))
         const float uk = qu * omaxf(hc, mah), vk = qv * omaxf(hc, mah);
         float dzv[3];
 #pragma unroll
-        for (int i = 0; i < 3; i++) dzv[i] = X.dzv[i * N + k];
+        for (int i = 0; i < 3; i++) dzv[i] = ro(X.dzv + (i * N + k));
         float oh[3], ou[3], ov[3];  // vertex depth, momentum (or velocity)
         bool flat = order == 1;
         if (order != 1) {
-            const int kind = X.kind[k];
+            const int kind = ro(X.kind + (k));
             const float cu = vel ? qu : uk, cv = vel ? qv : vk;
             if ((kind & 3) == 2) {
                 flat = true;
             } else {
                 float c[6];
 #pragma unroll
-                for (int j = 0; j < 6; j++) c[j] = X.gc[j * N + k];
+                for (int j = 0; j < 6; j++) c[j] = ro(X.gc + (j * N + k));
                 float dw[3] = {0.f, 0.f, 0.f}, du[3] = {0.f, 0.f, 0.f}, dv[3] = {0.f, 0.f, 0.f};
                 bool keep = false;  // dry neighbourhood: previous vertex values stay
                 if ((kind & 3) == 0) {
-                    const int k0 = M.surr[k], k1 = M.surr[N + k], k2 = M.surr[2 * N + k];
-                    const float h0 = X.hf[k0], h1 = X.hf[k1], h2 = X.hf[k2];
+                    const int k0 = ro(M.surr + (k)), k1 = ro(M.surr + (N + k)), k2 = ro(M.surr + (2 * N + k));
+                    const float h0 = ro(X.hf + (k0)), h1 = ro(X.hf + (k1)), h2 = ro(X.hf + (k2));
                     const float hmin = ominf(ominf(h0, ominf(h1, h2)), hc);
                     const float hmax = omaxf(h0, omaxf(h1, h2));
                     if (P.optimise_dry_cells && hmax < P.f_eps) {
@@ -317,7 +353,7 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                     } else {
                         float hfactor = 0.0f;
                         if (hmin > 0.001f) hfactor = (hmin - 0.001f) / (hmin + 0.004f);
-                        const float z0 = X.dzn[k], z1 = X.dzn[N + k], z2 = X.dzn[2 * N + k];
+                        const float z0 = ro(X.dzn + (k)), z1 = ro(X.dzn + (N + k)), z2 = ro(X.dzn + (2 * N + k));
                         // stage differences = depth differences + bed differences
                         const float dq0 = (h0 - hc) + z0;
                         const float dq1 = (h1 - h0) + (z1 - z0);
@@ -325,27 +361,27 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                         aux_jumps_f(dq0, dq1, dq2, c,
                                     P.f_beta_w_dry + (P.f_beta_w - P.f_beta_w_dry) * hfactor,
                                     dw);
-                        const float u0 = vel ? X.uvel[k0] : X.uvel[k0] * omaxf(h0, mah);
-                        const float u1 = vel ? X.uvel[k1] : X.uvel[k1] * omaxf(h1, mah);
-                        const float u2 = vel ? X.uvel[k2] : X.uvel[k2] * omaxf(h2, mah);
+                        const float u0 = vel ? ro(X.uvel + (k0)) : ro(X.uvel + (k0)) * omaxf(h0, mah);
+                        const float u1 = vel ? ro(X.uvel + (k1)) : ro(X.uvel + (k1)) * omaxf(h1, mah);
+                        const float u2 = vel ? ro(X.uvel + (k2)) : ro(X.uvel + (k2)) * omaxf(h2, mah);
                         aux_jumps_f(u0 - cu, u1 - u0, u2 - u0, c,
                                     P.f_beta_uh_dry + (P.f_beta_uh - P.f_beta_uh_dry) * hfactor,
                                     du);
-                        const float v0 = vel ? X.vvel[k0] : X.vvel[k0] * omaxf(h0, mah);
-                        const float v1 = vel ? X.vvel[k1] : X.vvel[k1] * omaxf(h1, mah);
-                        const float v2 = vel ? X.vvel[k2] : X.vvel[k2] * omaxf(h2, mah);
+                        const float v0 = vel ? ro(X.vvel + (k0)) : ro(X.vvel + (k0)) * omaxf(h0, mah);
+                        const float v1 = vel ? ro(X.vvel + (k1)) : ro(X.vvel + (k1)) * omaxf(h1, mah);
+                        const float v2 = vel ? ro(X.vvel + (k2)) : ro(X.vvel + (k2)) * omaxf(h2, mah);
                         aux_jumps_f(v0 - cv, v1 - v0, v2 - v0, c,
                                     P.f_beta_vh_dry + (P.f_beta_vh - P.f_beta_vh_dry) * hfactor,
                                     dv);
                     }
                 } else {
                     const int slot = (kind >> 2) & 3;
-                    const int k1 = M.surr[slot * N + k];
-                    const float h1 = X.hf[k1];
+                    const int k1 = ro(M.surr + (slot * N + k));
+                    const float h1 = ro(X.hf + (k1));
                     const float beta = P.f_beta_w;
-                    one_jumps_f((h1 - hc) + X.dzn[slot * N + k], c, beta, dw);
-                    const float u1 = vel ? X.uvel[k1] : X.uvel[k1] * omaxf(h1, mah);
-                    const float v1 = vel ? X.vvel[k1] : X.vvel[k1] * omaxf(h1, mah);
+                    one_jumps_f((h1 - hc) + ro(X.dzn + (slot * N + k)), c, beta, dw);
+                    const float u1 = vel ? ro(X.uvel + (k1)) : ro(X.uvel + (k1)) * omaxf(h1, mah);
+                    const float v1 = vel ? ro(X.vvel + (k1)) : ro(X.vvel + (k1)) * omaxf(h1, mah);
                     one_jumps_f(u1 - cu, c, beta, du);
                     one_jumps_f(v1 - cv, c, beta, dv);
                 }
@@ -431,22 +467,22 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
             X.uhv[i * N + k] = ou[i];
             X.vhv[i * N + k] = ov[i];
         }
-        if ((flags & kWriteBoundary) && M.nb[k] > 0) {
+        if ((flags & kWriteBoundary) && ro(M.nb + (k)) > 0) {
             const double time = ctrl->time;
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                const int pk = M.nbr[i * N + k];
+                const int pk = ro(M.nbr + (i * N + k));
                 if (pk < 0) {
                     const int mb = -pk - 1;
                     const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-                    const double ze = S.ze[i * N + k];
+                    const double ze = ro(S.ze + (i * N + k));
                     const float he = 0.5f * (oh[a] + oh[b]);
                     const double we = ze + (double)he;
                     const double uhe = 0.5 * ((double)ou[a] + (double)ou[b]);
                     const double vhe = 0.5 * ((double)ov[a] + (double)ov[b]);
                     double wb, uhb, vhb;
-                    if (!eval_boundary(tags[M.btag[mb]], time, we, uhe, vhe,
-                                       (double)X.nx[i * N + k], (double)X.ny[i * N + k], wb, uhb,
+                    if (!eval_boundary(tags[ro(M.btag + (mb))], time, we, uhe, vhe,
+                                       (double)ro(X.nx + (i * N + k)), (double)ro(X.ny + (i * N + k)), wb, uhb,
                                        vhb)) {
                         bad_bc = 1;
                         wb = we;
@@ -457,7 +493,7 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                     S.vhb[mb] = vhb;
                     S.zb[mb] = ze;
                     // reflective keeps the edge depth exactly; others from the stage
-                    X.hbf[mb] = tags[M.btag[mb]].type == SWGPU_BC_REFLECTIVE ? he
+                    X.hbf[mb] = tags[ro(M.btag + (mb))].type == SWGPU_BC_REFLECTIVE ? he
                                                                                : (float)(wb - ze);
                     X.uhbf[mb] = (float)uhb;
                     X.vhbf[mb] = (float)vhb;

@@ -435,15 +435,17 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
     } else {
         DevMixed &X = h->X;
         TRY(dalloc(h, &X.hd, n1));
+        TRY(dalloc(h, &X.wf, n1));
         TRY(dalloc(h, &X.hf, n1));
         TRY(dalloc(h, &X.uvel, n1));
         TRY(dalloc(h, &X.vvel, n1));
-        TRY(dalloc(h, &X.hv, n3));
+        TRY(dalloc(h, &X.dw, n3));
         TRY(dalloc(h, &X.uhv, n3));
         TRY(dalloc(h, &X.vhv, n3));
         TRY(dalloc(h, &X.hbf, nb1));
         TRY(dalloc(h, &X.uhbf, nb1));
         TRY(dalloc(h, &X.vhbf, nb1));
+        TRY(dalloc(h, &X.wjb, nb1));
         TRY(dalloc(h, &X.ew, n1));
         TRY(dalloc(h, &X.euh, n1));
         TRY(dalloc(h, &X.evh, n1));
@@ -453,9 +455,8 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
         TRY(dalloc(h, &X.inv_area, n1));
         TRY(dalloc(h, &X.radius, n1));
         TRY(dalloc(h, &X.gc, n6));
-        TRY(dalloc(h, &X.dzn, n3));
         TRY(dalloc(h, &X.dzv, n3));
-        TRY(dalloc(h, &X.zgrad, 2 * n1));
+        TRY(dalloc(h, &X.dze, n3));
         TRY(dalloc(h, &X.fric, n1));
         TRY(dalloc(h, &X.zmoff, n1));
         TRY(dalloc(h, &X.kind, n1));

@@ -56,24 +56,27 @@ struct DevState {
 
 // Mixed-precision state.  The conserved state is FP64 depth h = w - z (so
 // depth at wet/dry fronts never comes from a difference of two large
-// stages) and FP64 momentum; everything the flux, limiter and extrapolation
-// read is FP32: centroid depth and velocities, vertex depth and momentum,
-// and geometry precomputed relative to each triangle's centroid.
+// stages) and FP64 momentum.  Everything the flux, limiter and
+// extrapolation read is FP32 and, where the shallow-water terms cancel,
+// stored as a deviation: centroid stage and depth, vertex STAGE JUMPS from
+// the centroid (not absolute vertex values), and bed offsets from the
+// centroid bed, so that hydrostatic pressure and bed-slope terms never
+// subtract two large FP32 numbers.
 struct DevMixed {
-    double *hd;                // [N] FP64 depth (conserved)
-    float *hf, *uvel, *vvel;   // [N] centroid depth and velocities
-    float *hv, *uhv, *vhv;     // [3][N] vertex depth and momentum
-    float *hbf, *uhbf, *vhbf;  // [Nb] boundary depth and momentum
-    float *ew, *euh, *evh;     // [N] explicit_update
-    float *nx, *ny, *len;      // [3][N] normals, edge lengths
-    float *inv_area, *radius;  // [N]
-    float *gc;                 // [6][N] vertex-jump coefficients (dq1, dq2 per vertex)
-    float *dzn;                // [3][N] bed centroid of surrogate j minus own
-    float *dzv;                // [3][N] bed vertex minus bed centroid
-    float *zgrad;              // [2][N] bed gradient
-    float *fric;               // [N] Manning n
-    float *zmoff;              // [N] mean(bed vertex) minus bed centroid
-    uint8_t *kind;             // [N] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat
+    double *hd;                    // [N] FP64 depth (conserved)
+    float *wf, *hf, *uvel, *vvel;  // [N] centroid stage, depth, velocities
+    float *dw, *uhv, *vhv;         // [3][N] vertex stage jump from centroid, vertex momentum
+    float *hbf, *uhbf, *vhbf;      // [Nb] boundary depth and momentum
+    float *wjb;                    // [Nb] boundary stage minus the owner's edge stage
+    float *ew, *euh, *evh;         // [N] explicit_update
+    float *nx, *ny, *len;          // [3][N] normals, edge lengths
+    float *inv_area, *radius;      // [N]
+    float *gc;                     // [6][N] vertex-jump coefficients (dq1, dq2 per vertex)
+    float *dzv;                    // [3][N] bed vertex minus bed centroid
+    float *dze;                    // [3][N] bed edge minus bed centroid
+    float *fric;                   // [N] Manning n
+    float *zmoff;                  // [N] mean(bed vertex) minus bed centroid
+    uint8_t *kind;                 // [N] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat
 };
 
 struct DevParams {

@@ -1,23 +1,33 @@
 // swgpu_mixed.cu -- mixed-precision evolve kernels.
 //
-// The same ANUGA algorithm as the FP64 path (limiter, central-upwind flux,
-// gravity_wb, Manning friction, protect, balance), restructured for an
-// HBM-bound GB300 kernel:
-//   * conserved state is FP64 depth h (not stage) and FP64 momentum; the
-//     update h += dt*E, uh += dt*E (then the friction factor) stays FP64;
-//   * everything the limiter, extrapolation and flux read is FP32: centroid
-//     depth and velocities, vertex depth and momentum, normals, lengths,
-//     1/area, radii and per-triangle coefficients precomputed in FP64 on the
-//     host relative to the triangle's own centroid (so no FP32 arithmetic
-//     ever sees an absolute coordinate);
-//   * stage differences for the limiter are depth differences plus
-//     precomputed bed differences; the flux uses depths directly (the bed is
-//     continuous across an edge, so w_r - w_l = h_r - h_l);
-//   * the gravity term's stage gradient is the depth gradient (Green's
-//     theorem over the edge midpoints, exact for the linear reconstruction)
-//     plus the precomputed bed gradient.
+// The same ANUGA algorithm as the FP64 path (gradient limiter on the
+// auxiliary triangle, balance_deep_and_shallow, central-upwind flux,
+// gravity_wb, semi-implicit Manning friction, protect), restructured for a
+// GB300, whose FP64 pipe runs at 1/64 of the FP32 rate:
+//
+//  * The conserved state is FP64 depth h and FP64 momentum.  The update adds
+//    FP32 increments (dt*E and the friction term) to it with FP64 adds, so
+//    the state itself never loses precision to FP32.
+//  * Everything the limiter, extrapolation and flux read is FP32 and stored
+//    in deviation form: centroid stage and depth; per-vertex STAGE JUMPS from
+//    the centroid; bed offsets of vertices and edges from the centroid bed;
+//    geometry as normals, lengths, 1/area, radii and per-triangle jump
+//    coefficients computed in FP64 on the host.  No FP32 expression adds or
+//    subtracts absolute coordinates or two large depths.
+//  * Hydrostatic pressure enters as a difference: the edge flux minus the
+//    owner's edge pressure (gravity_wb's side term, folded into the flux),
+//    0.5 g (h_r - h_l)(h_r + h_l) with h_r - h_l taken from the stage jump.
+//    The stage gradient of the gravity term is the Green sum of the edge
+//    stage jumps.  In deep water both would otherwise be differences of
+//    O(g h^2) numbers, which is where FP32 loses the answer.
+//  * The mass flux is computed with unfused, correctly rounded products so
+//    that it is exactly antisymmetric: both triangles of an edge build the
+//    same edge depths from the same data, and water volume is conserved to
+//    the FP64 rounding of the reduction.
+//  * FP32 <-> FP64 conversions of the state run on the integer pipe.
+//
 // Bytes per triangle-step (own arrays; neighbour gathers hit L1/L2):
-//   distribute ~109, flux ~116, update ~80.
+//   distribute ~102, flux ~124, update ~104.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -27,11 +37,49 @@
 
 namespace swgpu {
 
-// Read-only loads through the non-coherent path (the arrays a kernel reads
-// are never written by the same kernel).
+// Read-only loads through the non-coherent path (no kernel writes an array
+// it reads this way).
 template <typename T>
 __device__ __forceinline__ T ro(const T *p) {
     return __ldg(p);
+}
+
+// Exact FP32 -> FP64 widening on the integer pipe (inputs are flushed to
+// zero when denormal, as this unit compiles with -ftz).
+__device__ __forceinline__ double widen(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned long long mant = (unsigned long long)(u & 0x7fffffu) << 29;
+    const unsigned long long ex =
+        e == 0 ? 0ull : (e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u));
+    const unsigned long long bits = e == 0 ? sign : (sign | (ex << 52) | mant);
+    return __longlong_as_double((long long)bits);
+}
+
+// FP64 -> FP32 narrowing toward zero on the integer pipe (underflow to
+// zero, overflow to infinity, NaN kept).
+__device__ __forceinline__ float narrow(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7ffu) - 896;
+    const unsigned mant = (unsigned)((b >> 29) & 0x7fffffu);
+    const bool nan = ((b >> 52) & 0x7ffu) == 0x7ffu && (b & 0xfffffffffffffull) != 0;
+    unsigned r;
+    if (e <= 0)
+        r = sign;
+    else if (e >= 255)
+        r = sign | 0x7f800000u | (nan ? 0x400000u : 0u);
+    else
+        r = sign | ((unsigned)e << 23) | mant;
+    return __uint_as_float(r);
+}
+
+// Edge depth of edge i of a triangle from its centroid depth, the stage
+// jumps of the two vertices of the edge and the bed offset of the edge.
+// Both triangles of an edge evaluate it with the same operations.
+__device__ __forceinline__ float edge_depth(float hc, float dwa, float dwb, float dze) {
+    return (hc + 0.5f * (dwa + dwb)) - dze;
 }
 
 // _compute_speed (shallow_water_ext.c:214-242) for both momentum components
@@ -48,29 +96,34 @@ __device__ __forceinline__ void side_speed_f(float &h, float &uh, float &vh, flo
             vh = 0.0f;
         } else {
             const float f = __fdividef(h, h * h + h0);
-            u = uh * f;
-            uh = u * h;
-            vh = (vh * f) * h;
+            u = __fmul_rn(uh, f);
+            uh = __fmul_rn(u, h);
+            vh = __fmul_rn(__fmul_rn(vh, f), h);
         }
     } else {
         u = __fdividef(uh, h);
     }
 }
 
-// Central-upwind flux on depths (rotated frame inside), FP32.  The stage
-// jump equals the depth jump (bed continuous across the edge).
-__device__ __forceinline__ void central_flux_f(float hl_in, float uhl_in, float vhl_in,
-                                               float hr_in, float uhr_in, float vhr_in, float n1,
-                                               float n2, float g, float eps, float h0, float lim,
-                                               float &f0, float &f1, float &f2, float &ms) {
-    const float al = n1 * uhl_in + n2 * vhl_in;
-    const float bl = -n2 * uhl_in + n1 * vhl_in;
-    const float ar = n1 * uhr_in + n2 * vhr_in;
-    const float br = -n2 * uhr_in + n1 * vhr_in;
+// Central-upwind flux (shallow_water_ext.c:302-441) of one edge seen from
+// its owner, with the owner's hydrostatic edge pressure 0.5 g hl^2 removed
+// from the normal momentum flux (that term is gravity_wb's side term,
+// shallow_water_ext.c:1990-2028).  jump = w_r - w_l.  Returns the xy fluxes.
+__device__ __forceinline__ void edge_flux_dev(float hl_in, float uhl_in, float vhl_in, float hr_in,
+                                              float uhr_in, float vhr_in, float jump, float n1,
+                                              float n2, const DevParams &P, float &f0, float &f1,
+                                              float &f2, float &ms) {
+    const float g = P.f_g, eps = P.f_eps;
+    // rotation into the edge frame with unfused products, so that the two
+    // triangles of an edge get exactly negated normal momenta
+    const float al = __fadd_rn(__fmul_rn(n1, uhl_in), __fmul_rn(n2, vhl_in));
+    const float bl = __fsub_rn(__fmul_rn(n1, vhl_in), __fmul_rn(n2, uhl_in));
+    const float ar = __fadd_rn(__fmul_rn(n1, uhr_in), __fmul_rn(n2, vhr_in));
+    const float br = __fsub_rn(__fmul_rn(n1, vhr_in), __fmul_rn(n2, uhr_in));
     float hl = hl_in, uhl = al, vhl = bl, ul;
     float hr = hr_in, uhr = ar, vhr = br, ur;
-    side_speed_f(hl, uhl, vhl, ul, eps, h0, lim);
-    side_speed_f(hr, uhr, vhr, ur, eps, h0, lim);
+    side_speed_f(hl, uhl, vhl, ul, eps, P.f_h0, P.f_lim);
+    side_speed_f(hr, uhr, vhr, ur, eps, P.f_h0, P.f_lim);
     const float cl = sqrtf(g * hl), cr = sqrtf(g * hr);
     float smax = omaxf(ul + cl, ur + cr);
     if (smax < 0.0f) smax = 0.0f;
@@ -78,24 +131,32 @@ __device__ __forceinline__ void central_flux_f(float hl_in, float uhl_in, float 
     if (smin > 0.0f) smin = 0.0f;
     const float denom = smax - smin;
     if (denom < eps) {
-        f0 = f1 = f2 = 0.0f;
+        f0 = 0.0f;
+        const float p = -0.5f * g * hl * hl;  // only the side term remains
+        f1 = n1 * p;
+        f2 = n2 * p;
         ms = 0.0f;
         return;
     }
     const float inv = __fdividef(1.0f, denom);
-    const float ss = smax * smin;
-    const float fl0 = ul * hl, fl1 = ul * uhl + 0.5f * g * hl * hl, fl2 = ul * vhl;
-    const float fr0 = ur * hr, fr1 = ur * uhr + 0.5f * g * hr * hr, fr2 = ur * vhr;
-    const float e0 = (smax * fl0 - smin * fr0 + ss * (hr_in - hl_in)) * inv;
-    const float e1 = (smax * fl1 - smin * fr1 + ss * (ar - al)) * inv;
-    const float e2 = (smax * fl2 - smin * fr2 + ss * (br - bl)) * inv;
+    const float ss = __fmul_rn(smax, smin);
+    // mass: unfused products, exactly antisymmetric under swapping sides
+    const float fl0 = __fmul_rn(ul, hl), fr0 = __fmul_rn(ur, hr);
+    f0 = __fmul_rn(__fadd_rn(__fsub_rn(__fmul_rn(smax, fl0), __fmul_rn(smin, fr0)),
+                             __fmul_rn(ss, jump)),
+                   inv);
+    // depth difference across the edge: the stage jump unless a side was
+    // zeroed by the eps limit
+    const float dH = (hl == hl_in && hr == hr_in) ? jump : hr - hl;
+    const float dP = 0.5f * g * dH * (hr + hl);  // p_r - p_l
+    const float e1 = (smax * ul * uhl - smin * ur * uhr + ss * (ar - al) - smin * dP) * inv;
+    const float e2 = (smax * ul * vhl - smin * ur * vhr + ss * (br - bl)) * inv;
     ms = omaxf(fabsf(smax), fabsf(smin));
-    f0 = e0;
     f1 = n1 * e1 - n2 * e2;
     f2 = n2 * e1 + n1 * e2;
 }
 
-// flux + gravity_wb, FP32, triangle centric.
+// Fluxes + gravity_wb, FP32, triangle centric (no atomics).
 __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevParams P,
                                                      Ctrl *ctrl, int flags) {
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
@@ -103,93 +164,117 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     float t = P.f_max_dt;
     if (k < N) {
-        const float g = P.f_g, eps = P.f_eps;
-        const float h0 = P.f_h0, lim = P.f_lim;
-        float vh[3], vu[3], vv[3];
+        const float eps = P.f_eps;
+        const float wk = ro(X.wf + k), hc = ro(X.hf + k);
+        float dw[3], vu[3], vv[3], dz[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            vh[i] = ro(X.hv + i * N + k);
+            dw[i] = ro(X.dw + i * N + k);
             vu[i] = ro(X.uhv + i * N + k);
             vv[i] = ro(X.vhv + i * N + k);
+            dz[i] = ro(X.dze + i * N + k);
         }
-        const float he[3] = {0.5f * (vh[1] + vh[2]), 0.5f * (vh[0] + vh[2]), 0.5f * (vh[0] + vh[1])};
-        const float ue[3] = {0.5f * (vu[1] + vu[2]), 0.5f * (vu[0] + vu[2]), 0.5f * (vu[0] + vu[1])};
-        const float ve[3] = {0.5f * (vv[1] + vv[2]), 0.5f * (vv[0] + vv[2]), 0.5f * (vv[0] + vv[1])};
         const float rk = ro(X.radius + k);
         const float inv_area = ro(X.inv_area + k);
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;            // flux sums
-        float gx = 0.f, gy = 0.f, sx = 0.f, sy = 0.f;  // Green gradient, side term
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // flux sums
+        float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
 #pragma unroll
         for (int i = 0; i < 3; i++) {
+            const int ia = (i == 0) ? 1 : 0, ib = (i == 2) ? 1 : 2;
             const int pk = ro(M.nbr + i * N + k);
             const float n1 = ro(X.nx + i * N + k), n2 = ro(X.ny + i * N + k);
             const float L = ro(X.len + i * N + k);
-            float hr, uhr, vhr, rn = 3.0e38f;
+            const float dwl = 0.5f * (dw[ia] + dw[ib]);
+            const float hl = edge_depth(hc, dw[ia], dw[ib], dz[i]);
+            const float uhl = 0.5f * (vu[ia] + vu[ib]);
+            const float vhl = 0.5f * (vv[ia] + vv[ib]);
+            float hr, uhr, vhr, jump, rn = 3.0e38f;
             if (pk >= 0) {
                 const int n = pk >> 2, m = pk & 3;
                 const int a = (m == 0) ? 1 : 0, b = (m == 2) ? 1 : 2;
-                hr = 0.5f * (ro(X.hv + a * N + n) + ro(X.hv + b * N + n));
+                const float dwa = ro(X.dw + a * N + n), dwb = ro(X.dw + b * N + n);
+                hr = edge_depth(ro(X.hf + n), dwa, dwb, ro(X.dze + m * N + n));
+                jump = (ro(X.wf + n) - wk) + (0.5f * (dwa + dwb) - dwl);
                 uhr = 0.5f * (ro(X.uhv + a * N + n) + ro(X.uhv + b * N + n));
                 vhr = 0.5f * (ro(X.vhv + a * N + n) + ro(X.vhv + b * N + n));
                 rn = ro(X.radius + n);
             } else {
                 const int mb = -pk - 1;
                 hr = ro(X.hbf + mb);
+                jump = ro(X.wjb + mb);
                 uhr = ro(X.uhbf + mb);
                 vhr = ro(X.vhbf + mb);
             }
-            const float hl = he[i];
-            const float hlL = hl * L;
-            gx += hlL * n1;
-            gy += hlL * n2;
-            const float fact = -0.5f * g * hl * hlL;
-            sx += fact * n1;
-            sy += fact * n2;
+            gx += dwl * L * n1;
+            gy += dwl * L * n2;
             if (P.optimise_dry_cells && fabsf(hl) < eps && fabsf(hr) < eps) continue;
             float f0, f1, f2, ms;
-            central_flux_f(hl, ue[i], ve[i], hr, uhr, vhr, n1, n2, g, eps, h0, lim, f0, f1, f2, ms);
+            edge_flux_dev(hl, uhl, vhl, hr, uhr, vhr, jump, n1, n2, P, f0, f1, f2, ms);
             a0 -= f0 * L;
             a1 -= f1 * L;
             a2 -= f2 * L;
-            if (ms > eps) {
-                // min(rk/ms, rn/ms) = min(rk, rn)/ms: one division per edge
-                t = ominf(t, __fdividef(fminf(rk, rn), ms));
-            }
+            // min(rk/ms, rn/ms) = min(rk, rn)/ms: one division per edge
+            if (ms > eps) t = ominf(t, __fdividef(fminf(rk, rn), ms));
         }
-        const float avg_h = ro(X.hf + k);
-        const float wx = gx * inv_area + ro(X.zgrad + k);
-        const float wy = gy * inv_area + ro(X.zgrad + N + k);
+        const float ghc = P.f_g * hc;
         X.ew[k] = a0 * inv_area;
-        X.euh[k] = a1 * inv_area - g * wx * avg_h - sx * inv_area;
-        X.evh[k] = a2 * inv_area - g * wy * avg_h - sy * inv_area;
+        X.euh[k] = (a1 - ghc * gx) * inv_area;
+        X.evh[k] = (a2 - ghc * gy) * inv_area;
     }
     block_min_timestep_f(t, ctrl);
     if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
         publish_step_clock(ctrl, P);
 }
 
-// Update: the conserved state stays FP64 and is advanced by increments
-// computed in FP32 (each increment is small against the value it is added
-// to, so its FP32 rounding is far below the FP32 resolution of the state;
-// the additions themselves are FP64):
-//   h  += dt*E_h
-//   q  += q*(r - 1) + dt*E_q*r,   r = 1/(1 - dt*S)  (semi-implicit Manning)
-// then protect and the FP32 centroid copies the next extrapolation reads.
+// FP32 copies of the updated state and protect (shallow_water_ext.c:
+// 1638-1705) on depth; shared by the update and the stand-alone prepare.
+__device__ __forceinline__ void finish_state(const DevParams &P, double &h, double &uh, double &vh,
+                                             double zc, float &hf, float &wf, float &uvel,
+                                             float &vvel, int &nonfinite) {
+    hf = narrow(h);
+    float uhf = narrow(uh), vhf = narrow(vh);
+    if (hf < P.f_mah) {
+        if (P.f_mas < P.f_eps) {
+            uh = vh = 0.0;
+            uhf = vhf = 0.0f;
+            if (h <= 0.0) {
+                h = 0.0;
+                hf = 0.0f;
+            }
+        } else if (h <= 0.0) {
+            h = uh = vh = 0.0;
+            hf = uhf = vhf = 0.0f;
+        } else {
+            const float u = uhf / hf, v = vhf / hf, ms = P.f_mas;
+            if (fabsf(u) > ms) uhf = (u > 0 ? ms : -ms) * hf;
+            if (fabsf(v) > ms) vhf = (v > 0 ? ms : -ms) * hf;
+            uh = widen(uhf);
+            vh = widen(vhf);
+        }
+    }
+    wf = narrow(h + zc);
+    if (!(fabsf(hf) <= 3.0e38f) || !(fabsf(uhf) <= 3.0e38f) || !(fabsf(vhf) <= 3.0e38f))
+        nonfinite = 1;
+    const float inv = __fdividef(1.0f, omaxf(hf, P.f_mah));
+    uvel = uhf * inv;
+    vvel = vhf * inv;
+}
+
+// Update: h += dt*E_h;  q += q*(r - 1) + dt*E_q*r  with r = 1/(1 - dt*S) the
+// semi-implicit Manning factor.  Increments in FP32, additions in FP64.
 __global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, DevMixed X,
                                                        DevParams P, Ctrl *ctrl, int flags) {
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     const StepClock clk = published_step_clock(ctrl);
-    const double dt = clk.dt;
-    const float dtf = (float)dt;
+    const float dtf = (float)clk.dt;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int bad = 0, nonfinite = 0;
     if (k < M.N) {
         double h = X.hd[k], uh = S.uh[k], vh = S.vh[k];
         const float mah = P.f_mah;
-        const float hf0 = ro(X.hf + k);  // FP32 copy of h written last step
+        const float hf0 = ro(X.hf + k);  // FP32 copies of the pre-update state
         const float uf = ro(X.uvel + k) * omaxf(hf0, mah);
         const float vf = ro(X.vvel + k) * omaxf(hf0, mah);
-        // Manning friction on the pre-update state
         float rm1 = 0.0f, r = 1.0f;  // r - 1 and r
         const float eta = ro(X.fric + k);
         if (eta > mah) {
@@ -197,53 +282,25 @@ __global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, De
             if (hm >= mah) {
                 const float Sf = -P.f_g * eta * eta * sqrtf(uf * uf + vf * vf) *
                                  exp2f(-(7.0f / 3.0f) * __log2f(hm));
-                const float dS = dtf * Sf;         // <= 0
+                const float dS = dtf * Sf;  // <= 0
                 const float den = 1.0f - dS;
                 if (!(den > 0.0f)) bad = 1;
                 r = __fdividef(1.0f, den);
-                rm1 = dS * r;                      // r - 1 without cancellation
+                rm1 = dS * r;  // r - 1 without cancellation
             }
         }
-        const float dh = dtf * ro(X.ew + k);
-        const float du = uf * rm1 + dtf * ro(X.euh + k) * r;
-        const float dv = vf * rm1 + dtf * ro(X.evh + k) * r;
-        h += (double)dh;
-        uh += (double)du;
-        vh += (double)dv;
-        // FP32 copies re-derived from the FP64 state (no drift between them)
-        float hf = (float)h;
-        float uhf = (float)uh, vhf = (float)vh;
-        // protect (shallow_water_ext.c:1638-1705) on depth
-        if (hf < mah) {
-            if (P.f_mas < P.f_eps) {
-                uh = vh = 0.0;
-                uhf = vhf = 0.0f;
-                if (h <= 0.0) {
-                    h = 0.0;
-                    hf = 0.0f;
-                }
-            } else if (h <= 0.0) {
-                h = uh = vh = 0.0;
-                hf = uhf = vhf = 0.0f;
-            } else {
-                const float u = uhf / hf, v = vhf / hf, ms = P.f_mas;
-                if (fabsf(u) > ms) uhf = (u > 0 ? ms : -ms) * hf;
-                if (fabsf(v) > ms) vhf = (v > 0 ? ms : -ms) * hf;
-                uh = (double)uhf;
-                vh = (double)vhf;
-            }
-        }
-        // NaN / Inf anywhere in the new state stops the run (FP32 copies:
-        // a non-finite FP64 value stays non-finite when narrowed)
-        if (!(fabsf(hf) <= 3.0e38f) || !(fabsf(uhf) <= 3.0e38f) || !(fabsf(vhf) <= 3.0e38f))
-            nonfinite = 1;
+        h += widen(dtf * ro(X.ew + k));
+        uh += widen(uf * rm1 + dtf * ro(X.euh + k) * r);
+        vh += widen(vf * rm1 + dtf * ro(X.evh + k) * r);
+        float hf, wf, uv, vv;
+        finish_state(P, h, uh, vh, ro(S.zc + k), hf, wf, uv, vv, nonfinite);
         X.hd[k] = h;
         S.uh[k] = uh;
         S.vh[k] = vh;
         X.hf[k] = hf;
-        const float inv = __fdividef(1.0f, omaxf(hf, mah));
-        X.uvel[k] = uhf * inv;
-        X.vvel[k] = vhf * inv;
+        X.wf[k] = wf;
+        X.uvel[k] = uv;
+        X.vvel[k] = vv;
     }
     if (bad) set_status(ctrl, SWGPU_EDENOMINATOR);
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
@@ -278,6 +335,7 @@ __device__ __forceinline__ void qminmax_f(float dq0, float dq1, float dq2, float
     }
 }
 
+// limit_gradient (shallow_water_ext.c:151-181)
 __device__ __forceinline__ void limit_f(float (&d)[3], float qmin, float qmax, float beta) {
     const float TINY = 1.0e-30f;
     float r = 1000.0f, r0 = 1.0f;
@@ -310,7 +368,7 @@ __device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], floa
     limit_f(d, qmin, qmax, beta);
 }
 
-// extrapolation + balance + boundary conditions, FP32 on depths.
+// Extrapolation + balance + boundary conditions, FP32, in stage jumps.
 __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S, DevMixed X,
                                                            DevParams P, const BcTag *tags,
                                                            Ctrl *ctrl, int flags) {
@@ -322,30 +380,29 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
     int bad_bc = 0;
     if (k < N) {
         const float mah = P.f_mah;
-        const float hc = ro(X.hf + (k));
-        const float qu = ro(X.uvel + (k)), qv = ro(X.vvel + (k));
+        const float wk = ro(X.wf + k), hc = ro(X.hf + k);
+        const float qu = ro(X.uvel + k), qv = ro(X.vvel + k);
         const bool vel = P.extrapolate_velocity_second_order == 1;
-        // centroid momentum (uvel = uh / max(h, mah))
-        const float uk = qu * omaxf(hc, mah), vk = qv * omaxf(hc, mah);
+        const float hk = omaxf(hc, mah);
+        const float uk = qu * hk, vk = qv * hk;  // centroid momentum
         float dzv[3];
 #pragma unroll
-        for (int i = 0; i < 3; i++) dzv[i] = ro(X.dzv + (i * N + k));
-        float oh[3], ou[3], ov[3];  // vertex depth, momentum (or velocity)
-        bool flat = order == 1;
+        for (int i = 0; i < 3; i++) dzv[i] = ro(X.dzv + i * N + k);
+        float dw[3] = {0.f, 0.f, 0.f};  // vertex stage jumps
+        float ou[3], ov[3];             // vertex momentum (or velocity)
         if (order != 1) {
-            const int kind = ro(X.kind + (k));
+            const int kind = ro(X.kind + k);
             const float cu = vel ? qu : uk, cv = vel ? qv : vk;
-            if ((kind & 3) == 2) {
-                flat = true;
-            } else {
+            float du[3] = {0.f, 0.f, 0.f}, dv[3] = {0.f, 0.f, 0.f};
+            bool keep = false;  // dry neighbourhood: previous vertex values stay
+            if ((kind & 3) != 2) {
                 float c[6];
 #pragma unroll
-                for (int j = 0; j < 6; j++) c[j] = ro(X.gc + (j * N + k));
-                float dw[3] = {0.f, 0.f, 0.f}, du[3] = {0.f, 0.f, 0.f}, dv[3] = {0.f, 0.f, 0.f};
-                bool keep = false;  // dry neighbourhood: previous vertex values stay
+                for (int j = 0; j < 6; j++) c[j] = ro(X.gc + j * N + k);
                 if ((kind & 3) == 0) {
-                    const int k0 = ro(M.surr + (k)), k1 = ro(M.surr + (N + k)), k2 = ro(M.surr + (2 * N + k));
-                    const float h0 = ro(X.hf + (k0)), h1 = ro(X.hf + (k1)), h2 = ro(X.hf + (k2));
+                    const int k0 = ro(M.surr + k), k1 = ro(M.surr + N + k),
+                              k2 = ro(M.surr + 2 * N + k);
+                    const float h0 = ro(X.hf + k0), h1 = ro(X.hf + k1), h2 = ro(X.hf + k2);
                     const float hmin = ominf(ominf(h0, ominf(h1, h2)), hc);
                     const float hmax = omaxf(h0, omaxf(h1, h2));
                     if (P.optimise_dry_cells && hmax < P.f_eps) {
@@ -353,67 +410,58 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                     } else {
                         float hfactor = 0.0f;
                         if (hmin > 0.001f) hfactor = (hmin - 0.001f) / (hmin + 0.004f);
-                        const float z0 = ro(X.dzn + (k)), z1 = ro(X.dzn + (N + k)), z2 = ro(X.dzn + (2 * N + k));
-                        // stage differences = depth differences + bed differences
-                        const float dq0 = (h0 - hc) + z0;
-                        const float dq1 = (h1 - h0) + (z1 - z0);
-                        const float dq2 = (h2 - h0) + (z2 - z0);
-                        aux_jumps_f(dq0, dq1, dq2, c,
-                                    P.f_beta_w_dry + (P.f_beta_w - P.f_beta_w_dry) * hfactor,
-                                    dw);
-                        const float u0 = vel ? ro(X.uvel + (k0)) : ro(X.uvel + (k0)) * omaxf(h0, mah);
-                        const float u1 = vel ? ro(X.uvel + (k1)) : ro(X.uvel + (k1)) * omaxf(h1, mah);
-                        const float u2 = vel ? ro(X.uvel + (k2)) : ro(X.uvel + (k2)) * omaxf(h2, mah);
+                        const float w0 = ro(X.wf + k0), w1 = ro(X.wf + k1), w2 = ro(X.wf + k2);
+                        aux_jumps_f(w0 - wk, w1 - w0, w2 - w0, c,
+                                    P.f_beta_w_dry + (P.f_beta_w - P.f_beta_w_dry) * hfactor, dw);
+                        float u0 = ro(X.uvel + k0), u1 = ro(X.uvel + k1), u2 = ro(X.uvel + k2);
+                        float v0 = ro(X.vvel + k0), v1 = ro(X.vvel + k1), v2 = ro(X.vvel + k2);
+                        if (!vel) {
+                            u0 *= omaxf(h0, mah);
+                            v0 *= omaxf(h0, mah);
+                            u1 *= omaxf(h1, mah);
+                            v1 *= omaxf(h1, mah);
+                            u2 *= omaxf(h2, mah);
+                            v2 *= omaxf(h2, mah);
+                        }
                         aux_jumps_f(u0 - cu, u1 - u0, u2 - u0, c,
-                                    P.f_beta_uh_dry + (P.f_beta_uh - P.f_beta_uh_dry) * hfactor,
-                                    du);
-                        const float v0 = vel ? ro(X.vvel + (k0)) : ro(X.vvel + (k0)) * omaxf(h0, mah);
-                        const float v1 = vel ? ro(X.vvel + (k1)) : ro(X.vvel + (k1)) * omaxf(h1, mah);
-                        const float v2 = vel ? ro(X.vvel + (k2)) : ro(X.vvel + (k2)) * omaxf(h2, mah);
+                                    P.f_beta_uh_dry + (P.f_beta_uh - P.f_beta_uh_dry) * hfactor, du);
                         aux_jumps_f(v0 - cv, v1 - v0, v2 - v0, c,
-                                    P.f_beta_vh_dry + (P.f_beta_vh - P.f_beta_vh_dry) * hfactor,
-                                    dv);
+                                    P.f_beta_vh_dry + (P.f_beta_vh - P.f_beta_vh_dry) * hfactor, dv);
                     }
                 } else {
                     const int slot = (kind >> 2) & 3;
-                    const int k1 = ro(M.surr + (slot * N + k));
-                    const float h1 = ro(X.hf + (k1));
+                    const int k1 = ro(M.surr + slot * N + k);
+                    const float h1 = ro(X.hf + k1);
                     const float beta = P.f_beta_w;
-                    one_jumps_f((h1 - hc) + ro(X.dzn + (slot * N + k)), c, beta, dw);
-                    const float u1 = vel ? ro(X.uvel + (k1)) : ro(X.uvel + (k1)) * omaxf(h1, mah);
-                    const float v1 = vel ? ro(X.vvel + (k1)) : ro(X.vvel + (k1)) * omaxf(h1, mah);
+                    one_jumps_f(ro(X.wf + k1) - wk, c, beta, dw);
+                    float u1 = ro(X.uvel + k1), v1 = ro(X.vvel + k1);
+                    if (!vel) {
+                        u1 *= omaxf(h1, mah);
+                        v1 *= omaxf(h1, mah);
+                    }
                     one_jumps_f(u1 - cu, c, beta, du);
                     one_jumps_f(v1 - cv, c, beta, dv);
                 }
-                if (keep) {
-#pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        oh[i] = X.hv[i * N + k];
-                        ou[i] = X.uhv[i * N + k];
-                        ov[i] = X.vhv[i * N + k];
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        // vertex depth = centroid depth + stage jump - bed jump
-                        oh[i] = (hc + dw[i]) - dzv[i];
-                        ou[i] = cu + du[i];
-                        ov[i] = cv + dv[i];
-                    }
-                }
             }
-            if (flat) {
+            if (keep) {
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    oh[i] = hc - dzv[i];
-                    ou[i] = cu;
-                    ov[i] = cv;
+                    dw[i] = X.dw[i * N + k];
+                    ou[i] = X.uhv[i * N + k];
+                    ov[i] = X.vhv[i * N + k];
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    ou[i] = cu + du[i];
+                    ov[i] = cv + dv[i];
                 }
             }
             if (vel) {
+                // velocity -> momentum with the vertex depth hc + dw - dzv
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    const float d = omaxf(oh[i], 0.0f);
+                    const float d = omaxf((hc + dw[i]) - dzv[i], 0.0f);
                     ou[i] *= d;
                     ov[i] *= d;
                 }
@@ -421,27 +469,29 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
         } else {
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                oh[i] = hc - dzv[i];
                 ou[i] = uk;
                 ov[i] = vk;
             }
         }
-        // balance_deep_and_shallow on depths (w_v - z_v = h_v)
+        // balance_deep_and_shallow (shallow_water_ext.c:1462-1636) with vertex
+        // depth h_i = hc + (dw_i - dzv_i); the blend keeps the form
+        // dw_i <- alpha*(dw_i - dzv_i) + dzv_i
         {
-            const float H0 = P.f_H0;
-            const float hmin = ominf(oh[0], ominf(oh[1], oh[2]));
+            float rel[3];  // h_i - hc
+#pragma unroll
+            for (int i = 0; i < 3; i++) rel[i] = dw[i] - dzv[i];
+            const float hmin = hc + ominf(rel[0], ominf(rel[1], rel[2]));
             float alpha = 1.0f;
             if (P.tight_slope_limiters == 0) {
                 float dz = 0.0f;
 #pragma unroll
                 for (int i = 0; i < 3; i++) dz = omaxf(dz, fabsf(dzv[i]));
-                alpha = dz > 0.0f ? omaxf(ominf(P.f_alpha * hmin / dz, 1.0f), 0.0f)
-                                  : 1.0f;
-            } else if (hmin < H0) {
+                alpha = dz > 0.0f ? omaxf(ominf(P.f_alpha * hmin / dz, 1.0f), 0.0f) : 1.0f;
+            } else if (hmin < P.f_H0) {
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    const float hd = hc - oh[i];
-                    if (!(hd <= 0.0f)) alpha = ominf(alpha, (hc - H0) / hd);
+                    const float hd = -rel[i];
+                    if (!(hd <= 0.0f)) alpha = ominf(alpha, (hc - P.f_H0) / hd);
                 }
                 alpha = fminf(fmaxf(alpha, 0.0f), 1.0f);
             }
@@ -450,10 +500,11 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                 const float vc = hc > 1.0e-6f ? vk / hc : 0.0f;
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    oh[i] = (1.0f - alpha) * hc + alpha * oh[i];
+                    const float r = alpha * rel[i];
+                    dw[i] = r + dzv[i];
                     if (P.use_centroid_velocities == 1) {
-                        ou[i] = uc * oh[i];
-                        ov[i] = vc * oh[i];
+                        ou[i] = uc * (hc + r);
+                        ov[i] = vc * (hc + r);
                     } else {
                         ou[i] = (1.0f - alpha) * uk + alpha * ou[i];
                         ov[i] = (1.0f - alpha) * vk + alpha * ov[i];
@@ -463,27 +514,28 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
         }
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            X.hv[i * N + k] = oh[i];
+            X.dw[i * N + k] = dw[i];
             X.uhv[i * N + k] = ou[i];
             X.vhv[i * N + k] = ov[i];
         }
-        if ((flags & kWriteBoundary) && ro(M.nb + (k)) > 0) {
+        if ((flags & kWriteBoundary) && ro(M.nb + k) > 0) {
             const double time = ctrl->time;
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                const int pk = ro(M.nbr + (i * N + k));
+                const int pk = ro(M.nbr + i * N + k);
                 if (pk < 0) {
                     const int mb = -pk - 1;
                     const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-                    const double ze = ro(S.ze + (i * N + k));
-                    const float he = 0.5f * (oh[a] + oh[b]);
-                    const double we = ze + (double)he;
-                    const double uhe = 0.5 * ((double)ou[a] + (double)ou[b]);
-                    const double vhe = 0.5 * ((double)ov[a] + (double)ov[b]);
+                    const float hle = edge_depth(hc, dw[a], dw[b], ro(X.dze + i * N + k));
+                    const double ze = ro(S.ze + i * N + k);
+                    const double we = ze + widen(hle);
+                    const float uhe = 0.5f * (ou[a] + ou[b]);
+                    const float vhe = 0.5f * (ov[a] + ov[b]);
+                    const BcTag &T = tags[ro(M.btag + mb)];
                     double wb, uhb, vhb;
-                    if (!eval_boundary(tags[ro(M.btag + (mb))], time, we, uhe, vhe,
-                                       (double)ro(X.nx + (i * N + k)), (double)ro(X.ny + (i * N + k)), wb, uhb,
-                                       vhb)) {
+                    if (!eval_boundary(T, time, we, widen(uhe), widen(vhe),
+                                       widen(ro(X.nx + i * N + k)), widen(ro(X.ny + i * N + k)),
+                                       wb, uhb, vhb)) {
                         bad_bc = 1;
                         wb = we;
                         uhb = vhb = 0.0;
@@ -492,9 +544,14 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                     S.uhb[mb] = uhb;
                     S.vhb[mb] = vhb;
                     S.zb[mb] = ze;
-                    // reflective keeps the edge depth exactly; others from the stage
-                    X.hbf[mb] = tags[ro(M.btag + (mb))].type == SWGPU_BC_REFLECTIVE ? he
-                                                                               : (float)(wb - ze);
+                    if (T.type == SWGPU_BC_REFLECTIVE) {
+                        // same depth and stage as the edge: exactly no jump
+                        X.hbf[mb] = hle;
+                        X.wjb[mb] = 0.0f;
+                    } else {
+                        X.hbf[mb] = (float)(wb - ze);
+                        X.wjb[mb] = (float)(wb - we);
+                    }
                     X.uhbf[mb] = (float)uhb;
                     X.vhbf[mb] = (float)vhb;
                 }
@@ -516,40 +573,29 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
     if (k >= M.N) return;
     double h = from_stage ? S.w[k] - S.zc[k] : X.hd[k];
     double uh = S.uh[k], vh = S.vh[k];
-    if (h < P.minimum_allowed_height) {
-        if (P.f_mas < P.f_eps) {
-            uh = 0.0;
-            vh = 0.0;
-            if (h <= 0.0) h = 0.0;
-        } else if (h <= 0.0) {
-            h = 0.0;
-            uh = 0.0;
-            vh = 0.0;
-        } else {
-            const double u = uh / h, v = vh / h, ms = P.maximum_allowed_speed;
-            if (fabs(u) > ms) uh = (u > 0 ? ms : -ms) * h;
-            if (fabs(v) > ms) vh = (v > 0 ? ms : -ms) * h;
-        }
-    }
+    float hf, wf, uv, vv;
+    int nonfinite = 0;
+    finish_state(P, h, uh, vh, S.zc[k], hf, wf, uv, vv, nonfinite);
     X.hd[k] = h;
     S.uh[k] = uh;
     S.vh[k] = vh;
-    const float hf = (float)h, mah = P.f_mah;
     X.hf[k] = hf;
-    X.uvel[k] = (float)uh / omaxf(hf, mah);
-    X.vvel[k] = (float)vh / omaxf(hf, mah);
+    X.wf[k] = wf;
+    X.uvel[k] = uv;
+    X.vvel[k] = vv;
 }
 
 // FP64 stage centroid / vertex values and momentum vertex values for
-// downloads: w = h + z.
+// downloads: w = h + z, w_v = w + (vertex stage jump).
 __global__ void __launch_bounds__(kBlock) vertices_from_mixed(DevMesh M, DevState S, DevMixed X) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = M.N;
     if (k >= N) return;
-    S.w[k] = X.hd[k] + S.zc[k];
+    const double w = X.hd[k] + S.zc[k];
+    S.w[k] = w;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        S.wv[i * N + k] = (double)X.hv[i * N + k] + S.zv[i * N + k];
+        S.wv[i * N + k] = w + (double)X.dw[i * N + k];
         S.uhv[i * N + k] = (double)X.uhv[i * N + k];
         S.vhv[i * N + k] = (double)X.vhv[i * N + k];
     }
@@ -624,8 +670,8 @@ int build_mixed_geometry(Handle *h) {
         cudaMemcpy(ze.data(), h->S.ze, n3 * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(fr.data(), h->S.fric, n1 * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
         return SWGPU_ECUDA;
-    std::vector<float> nx(n3), ny(n3), len(n3), inv_area(n1), radius(n1), gc(6 * n1), dzn(n3),
-        dzv(n3), zgrad(2 * n1), fric(n1), zmoff(n1);
+    std::vector<float> nx(n3), ny(n3), len(n3), inv_area(n1), radius(n1), gc(6 * n1), dzv(n3),
+        dze(n3), fric(n1), zmoff(n1);
     std::vector<uint8_t> kind(n1);
     const std::vector<double> &V = h->h_vxy, &C = h->h_cxy;
     for (int k = 0; k < N; k++) {
@@ -634,18 +680,12 @@ int build_mixed_geometry(Handle *h) {
             ny[i * n1 + k] = (float)h->h_normals[(2 * i + 1) * n1 + k];
             len[i * n1 + k] = (float)h->h_len[i * n1 + k];
             dzv[i * n1 + k] = (float)(zv[i * n1 + k] - zc[k]);
-            dzn[i * n1 + k] = (float)(zc[h->h_surr[i * n1 + k]] - zc[k]);
+            dze[i * n1 + k] = (float)(ze[i * n1 + k] - zc[k]);
         }
         inv_area[k] = (float)(1.0 / h->h_areas[k]);
         radius[k] = (float)h->h_radii[k];
         fric[k] = (float)fr[k];
         zmoff[k] = (float)((zv[k] + zv[n1 + k] + zv[2 * n1 + k]) / 3.0 - zc[k]);
-        const double x0 = V[0 * n1 + k], y0 = V[1 * n1 + k], x1 = V[2 * n1 + k],
-                     y1 = V[3 * n1 + k], x2 = V[4 * n1 + k], y2 = V[5 * n1 + k];
-        const double det = (y2 - y0) * (x1 - x0) - (y1 - y0) * (x2 - x0);
-        const double z0 = zv[k], z1 = zv[n1 + k], z2 = zv[2 * n1 + k];
-        zgrad[k] = (float)(((y2 - y0) * (z1 - z0) - (y1 - y0) * (z2 - z0)) / det);
-        zgrad[n1 + k] = (float)(((x1 - x0) * (z2 - z0) - (x2 - x0) * (z1 - z0)) / det);
         const double x = C[k], y = C[n1 + k];
         double dxv[3], dyv[3];
         for (int i = 0; i < 3; i++) {
@@ -694,9 +734,8 @@ int build_mixed_geometry(Handle *h) {
     put(X.inv_area, inv_area.data(), n1 * 4);
     put(X.radius, radius.data(), n1 * 4);
     put(X.gc, gc.data(), 6 * n1 * 4);
-    put(X.dzn, dzn.data(), n3 * 4);
     put(X.dzv, dzv.data(), n3 * 4);
-    put(X.zgrad, zgrad.data(), 2 * n1 * 4);
+    put(X.dze, dze.data(), n3 * 4);
     put(X.fric, fric.data(), n1 * 4);
     put(X.zmoff, zmoff.data(), n1 * 4);
     put(X.kind, kind.data(), n1);

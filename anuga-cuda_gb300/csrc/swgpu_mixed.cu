@@ -57,21 +57,31 @@ __device__ __forceinline__ double widen(float x) {
     return __longlong_as_double((long long)bits);
 }
 
-// FP64 -> FP32 narrowing toward zero on the integer pipe (underflow to
-// zero, overflow to infinity, NaN kept).
+// FP64 -> FP32 narrowing, round to nearest even, on the integer pipe
+// (results below the FP32 normal range flush to zero, overflow gives
+// infinity, NaN stays NaN).
 __device__ __forceinline__ float narrow(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned sign = (unsigned)(b >> 63) << 31;
-    const int e = (int)((b >> 52) & 0x7ffu) - 896;
-    const unsigned mant = (unsigned)((b >> 29) & 0x7fffffu);
-    const bool nan = ((b >> 52) & 0x7ffu) == 0x7ffu && (b & 0xfffffffffffffull) != 0;
+    const unsigned ed = (unsigned)((b >> 52) & 0x7ffu);
+    const int e = (int)ed - 896;
+    const unsigned long long frac = b & 0xfffffffffffffull;
     unsigned r;
-    if (e <= 0)
+    if (ed == 0x7ffu) {
+        r = sign | 0x7f800000u | (frac ? 0x400000u : 0u);
+    } else if (e <= 0) {
         r = sign;
-    else if (e >= 255)
-        r = sign | 0x7f800000u | (nan ? 0x400000u : 0u);
-    else
-        r = sign | ((unsigned)e << 23) | mant;
+    } else if (e >= 255) {
+        r = sign | 0x7f800000u;
+    } else {
+        const unsigned m = (unsigned)(frac >> 29);
+        const unsigned long long rest = frac & 0x1fffffffull;  // the 29 dropped bits
+        r = ((unsigned)e << 23) | m;
+        // round half to even; a carry out of the mantissa bumps the exponent
+        // (up to infinity) as it should
+        if (rest > 0x10000000ull || (rest == 0x10000000ull && (m & 1u))) r += 1u;
+        r |= sign;
+    }
     return __uint_as_float(r);
 }
 
@@ -335,14 +345,15 @@ __device__ __forceinline__ void qminmax_f(float dq0, float dq1, float dq2, float
     }
 }
 
-// limit_gradient (shallow_water_ext.c:151-181)
+// limit_gradient (shallow_water_ext.c:151-181); correctly rounded divisions
+// (the limiter's branch points are where FP32 error would grow)
 __device__ __forceinline__ void limit_f(float (&d)[3], float qmin, float qmax, float beta) {
     const float TINY = 1.0e-30f;
     float r = 1000.0f, r0 = 1.0f;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        if (d[i] < -TINY) r0 = qmin / d[i];
-        if (d[i] > TINY) r0 = qmax / d[i];
+        if (d[i] < -TINY) r0 = __fdiv_rn(qmin, d[i]);
+        if (d[i] > TINY) r0 = __fdiv_rn(qmax, d[i]);
         r = ominf(r0, r);
     }
     const float phi = ominf(r * beta, 1.0f);

@@ -436,6 +436,7 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
         DevMixed &X = h->X;
         TRY(dalloc(h, &X.hd, n1));
         TRY(dalloc(h, &X.wf, n1));
+        TRY(dalloc(h, &X.wlo, n1));
         TRY(dalloc(h, &X.hf, n1));
         TRY(dalloc(h, &X.uvel, n1));
         TRY(dalloc(h, &X.vvel, n1));

@@ -64,7 +64,8 @@ struct DevState {
 // subtract two large FP32 numbers.
 struct DevMixed {
     double *hd;                    // [N] FP64 depth (conserved)
-    float *wf, *hf, *uvel, *vvel;  // [N] centroid stage, depth, velocities
+    float *wf, *wlo;               // [N] centroid stage as hi + lo FP32 pair
+    float *hf, *uvel, *vvel;       // [N] centroid depth, velocities
     float *dw, *uhv, *vhv;         // [3][N] vertex stage jump from centroid, vertex momentum
     float *hbf, *uhbf, *vhbf;      // [Nb] boundary depth and momentum
     float *wjb;                    // [Nb] boundary stage minus the owner's edge stage

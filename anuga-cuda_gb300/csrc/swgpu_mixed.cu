@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
     float t = P.f_max_dt;
     if (k < N) {
         const float eps = P.f_eps;
-        const float wk = ro(X.wf + k), hc = ro(X.hf + k);
+        const float wk = ro(X.wf + k), lk = ro(X.wlo + k), hc = ro(X.hf + k);
         float dw[3], vu[3], vv[3], dz[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
                 const int a = (m == 0) ? 1 : 0, b = (m == 2) ? 1 : 2;
                 const float dwa = ro(X.dw + a * N + n), dwb = ro(X.dw + b * N + n);
                 hr = edge_depth(ro(X.hf + n), dwa, dwb, ro(X.dze + m * N + n));
-                jump = (ro(X.wf + n) - wk) + (0.5f * (dwa + dwb) - dwl);
+                jump = ((ro(X.wf + n) - wk) + (ro(X.wlo + n) - lk)) + (0.5f * (dwa + dwb) - dwl);
                 uhr = 0.5f * (ro(X.uhv + a * N + n) + ro(X.uhv + b * N + n));
                 vhr = 0.5f * (ro(X.vhv + a * N + n) + ro(X.vhv + b * N + n));
                 rn = ro(X.radius + n);
@@ -239,8 +239,8 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
 // FP32 copies of the updated state and protect (shallow_water_ext.c:
 // 1638-1705) on depth; shared by the update and the stand-alone prepare.
 __device__ __forceinline__ void finish_state(const DevParams &P, double &h, double &uh, double &vh,
-                                             double zc, float &hf, float &wf, float &uvel,
-                                             float &vvel, int &nonfinite) {
+                                             double zc, float &hf, float &wf, float &wlo,
+                                             float &uvel, float &vvel, int &nonfinite) {
     hf = narrow(h);
     float uhf = narrow(uh), vhf = narrow(vh);
     if (hf < P.f_mah) {
@@ -262,7 +262,11 @@ __device__ __forceinline__ void finish_state(const DevParams &P, double &h, doub
             vh = widen(vhf);
         }
     }
-    wf = narrow(h + zc);
+    // stage as an unevaluated FP32 sum hi + lo (~46 bits): the limiter and
+    // the flux take stage differences between neighbours from it
+    const double w = h + zc;
+    wf = narrow(w);
+    wlo = narrow(w - widen(wf));
     if (!(fabsf(hf) <= 3.0e38f) || !(fabsf(uhf) <= 3.0e38f) || !(fabsf(vhf) <= 3.0e38f))
         nonfinite = 1;
     const float inv = __fdividef(1.0f, omaxf(hf, P.f_mah));
@@ -302,13 +306,14 @@ __global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, De
         h += widen(dtf * ro(X.ew + k));
         uh += widen(uf * rm1 + dtf * ro(X.euh + k) * r);
         vh += widen(vf * rm1 + dtf * ro(X.evh + k) * r);
-        float hf, wf, uv, vv;
-        finish_state(P, h, uh, vh, ro(S.zc + k), hf, wf, uv, vv, nonfinite);
+        float hf, wf, wl, uv, vv;
+        finish_state(P, h, uh, vh, ro(S.zc + k), hf, wf, wl, uv, vv, nonfinite);
         X.hd[k] = h;
         S.uh[k] = uh;
         S.vh[k] = vh;
         X.hf[k] = hf;
         X.wf[k] = wf;
+        X.wlo[k] = wl;
         X.uvel[k] = uv;
         X.vvel[k] = vv;
     }
@@ -391,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
     int bad_bc = 0;
     if (k < N) {
         const float mah = P.f_mah;
-        const float wk = ro(X.wf + k), hc = ro(X.hf + k);
+        const float wk = ro(X.wf + k), lk = ro(X.wlo + k), hc = ro(X.hf + k);
         const float qu = ro(X.uvel + k), qv = ro(X.vvel + k);
         const bool vel = P.extrapolate_velocity_second_order == 1;
         const float hk = omaxf(hc, mah);
@@ -422,7 +427,8 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                         float hfactor = 0.0f;
                         if (hmin > 0.001f) hfactor = (hmin - 0.001f) / (hmin + 0.004f);
                         const float w0 = ro(X.wf + k0), w1 = ro(X.wf + k1), w2 = ro(X.wf + k2);
-                        aux_jumps_f(w0 - wk, w1 - w0, w2 - w0, c,
+                        const float l0 = ro(X.wlo + k0), l1 = ro(X.wlo + k1), l2 = ro(X.wlo + k2);
+                        aux_jumps_f((w0 - wk) + (l0 - lk), (w1 - w0) + (l1 - l0), (w2 - w0) + (l2 - l0), c,
                                     P.f_beta_w_dry + (P.f_beta_w - P.f_beta_w_dry) * hfactor, dw);
                         float u0 = ro(X.uvel + k0), u1 = ro(X.uvel + k1), u2 = ro(X.uvel + k2);
                         float v0 = ro(X.vvel + k0), v1 = ro(X.vvel + k1), v2 = ro(X.vvel + k2);
@@ -444,7 +450,7 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                     const int k1 = ro(M.surr + slot * N + k);
                     const float h1 = ro(X.hf + k1);
                     const float beta = P.f_beta_w;
-                    one_jumps_f(ro(X.wf + k1) - wk, c, beta, dw);
+                    one_jumps_f((ro(X.wf + k1) - wk) + (ro(X.wlo + k1) - lk), c, beta, dw);
                     float u1 = ro(X.uvel + k1), v1 = ro(X.vvel + k1);
                     if (!vel) {
                         u1 *= omaxf(h1, mah);
@@ -584,14 +590,15 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
     if (k >= M.N) return;
     double h = from_stage ? S.w[k] - S.zc[k] : X.hd[k];
     double uh = S.uh[k], vh = S.vh[k];
-    float hf, wf, uv, vv;
+    float hf, wf, wl, uv, vv;
     int nonfinite = 0;
-    finish_state(P, h, uh, vh, S.zc[k], hf, wf, uv, vv, nonfinite);
+    finish_state(P, h, uh, vh, S.zc[k], hf, wf, wl, uv, vv, nonfinite);
     X.hd[k] = h;
     S.uh[k] = uh;
     S.vh[k] = vh;
     X.hf[k] = hf;
     X.wf[k] = wf;
+    X.wlo[k] = wl;
     X.uvel[k] = uv;
     X.vvel[k] = vv;
 }

@@ -1,6 +1,6 @@
 """In-tree build of libswgpu.so for sm_103a (GB300) with nvcc.
 
-Three translation units are compiled in parallel and linked into
+Four translation units are compiled in parallel and linked into
 ``anuga_cuda/libswgpu.so`` next to this file:
 
 * ``csrc/swgpu_fp64.cu``  -- the FP64 parity kernels, ``--fmad=false`` so that
@@ -8,7 +8,8 @@ Three translation units are compiled in parallel and linked into
   way by gcc on x86-64);
 * ``csrc/swgpu_mixed.cu`` -- the mixed-precision kernels (FMA allowed, FP32
   division and square root approximate, denormals flushed);
-* ``csrc/swgpu_api.cu``   -- the C ABI, allocation and the evolve loop.
+* ``csrc/swgpu_api.cu``   -- the C ABI, allocation and the evolve loop;
+* ``csrc/swgpu_noalloc.cu`` -- the allocation-free water-volume entry point.
 """
 from __future__ import annotations
 
@@ -28,6 +29,7 @@ UNITS = {
     "swgpu_fp64.cu": ["--fmad=false"],
     "swgpu_mixed.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "swgpu_api.cu": [],
+    "swgpu_noalloc.cu": ["--fmad=false"],
 }
 
 

@@ -117,6 +117,7 @@ _SIGNATURES = [
     ("swgpu_evolve_run_timed", C.c_int, [_VP, C.c_int64, C.POINTER(State_t), _f64p]),
     ("swgpu_profile_steps", C.c_int, [_VP, C.c_int64, _f64p]),
     ("swgpu_synchronize", C.c_int, [_VP]),
+    ("swgpu_water_volume_noalloc", C.c_int, [_VP, _VP, _VP, C.c_int64, _VP, _VP]),
 ]
 EXPORTED_SYMBOLS = [name for name, _, _ in _SIGNATURES]
 

@@ -17,6 +17,9 @@ namespace swgpu {
 
 static thread_local std::string g_create_error;
 
+// Message for swgpu_last_error(NULL) from entry points that have no handle.
+void record_global_error(const char *message) { g_create_error = message; }
+
 static int fail(Handle *h, int code, const char *fmt, ...) {
     char buf[512];
     va_list ap;

@@ -262,6 +262,30 @@ int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms);
 /* Synchronises the handle's stream. */
 int swgpu_synchronize(void *handle);
 
+/* ---- allocation-free entry point -------------------------------------- */
+
+/* Water volume sum(areas[k] * (stage[k] - elevation[k])), k < n, written to
+ * *volume, for callers that cannot allocate device memory when they need it:
+ * code running inside a CUDA stream capture (cudaMalloc is not capturable),
+ * code whose device memory belongs to a pool it does not control, and
+ * time-critical loops that must avoid cudaMalloc's implicit synchronisation.
+ * No counterpart in the reference.
+ *
+ * All five pointers are DEVICE pointers owned by the caller; stream may be
+ * NULL (the legacy default stream).  The call only enqueues work: *volume is
+ * ready when the stream reaches it.  It allocates nothing: its scratch is a
+ * 128 KiB file-scope __device__ array that every GPU loading the library
+ * holds until the process exits, which limits n to 4,194,304 (larger n:
+ * SWGPU_EINVAL).  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls on a device share the one
+ * array, so calls that overlap on the GPU (different streams or threads
+ * without ordering) race; calls ordered on one stream do not.  Results are
+ * identical to swgpu_mass on the same data.  Errors: swgpu_last_error(NULL). */
+int swgpu_water_volume_noalloc(const double *areas, const double *stage,
+                               const double *elevation, int64_t n, double *volume,
+                               void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -138,7 +138,9 @@ def lib(path: str | None = None):
     global _LIB
     if _LIB is not None and path is None:
         return _LIB
-    p = path or library_path()
+    # SWGPU_LIBRARY names another build of the same library (e.g. one built
+    # with different launch parameters); it is still libswgpu
+    p = path or os.environ.get("SWGPU_LIBRARY") or library_path()
     if not os.path.exists(p):
         raise ImportError(
             f"{p} not found: build it with anuga_cuda.build() (nvcc, sm_103a); "

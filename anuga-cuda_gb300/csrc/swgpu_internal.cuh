@@ -13,7 +13,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "../../include/swgpu.h"
+#include "swgpu.h"
 
 namespace swgpu {
 

@@ -443,9 +443,10 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
         TRY(dalloc(h, &X.hf, n1));
         TRY(dalloc(h, &X.uvel, n1));
         TRY(dalloc(h, &X.vvel, n1));
-        TRY(dalloc(h, &X.dw, n3));
-        TRY(dalloc(h, &X.uhv, n3));
-        TRY(dalloc(h, &X.vhv, n3));
+        TRY(dalloc(h, &X.he, n3));
+        TRY(dalloc(h, &X.dwe, n3));
+        TRY(dalloc(h, &X.uhe, n3));
+        TRY(dalloc(h, &X.vhe, n3));
         TRY(dalloc(h, &X.hbf, nb1));
         TRY(dalloc(h, &X.uhbf, nb1));
         TRY(dalloc(h, &X.vhbf, nb1));

@@ -58,15 +58,16 @@ struct DevState {
 // depth at wet/dry fronts never comes from a difference of two large
 // stages) and FP64 momentum.  Everything the flux, limiter and
 // extrapolation read is FP32 and, where the shallow-water terms cancel,
-// stored as a deviation: centroid stage and depth, vertex STAGE JUMPS from
-// the centroid (not absolute vertex values), and bed offsets from the
+// stored as a deviation: centroid stage and depth, edge STAGE JUMPS from
+// the centroid (not absolute edge values), and bed offsets from the
 // centroid bed, so that hydrostatic pressure and bed-slope terms never
 // subtract two large FP32 numbers.
 struct DevMixed {
     double *hd;                    // [N] FP64 depth (conserved)
     float *wf, *wlo;               // [N] centroid stage as hi + lo FP32 pair
     float *hf, *uvel, *vvel;       // [N] centroid depth, velocities
-    float *dw, *uhv, *vhv;         // [3][N] vertex stage jump from centroid, vertex momentum
+    float *he, *dwe;               // [3][N] edge depth, edge stage jump from the centroid
+    float *uhe, *vhe;              // [3][N] edge momentum
     float *hbf, *uhbf, *vhbf;      // [Nb] boundary depth and momentum
     float *wjb;                    // [Nb] boundary stage minus the owner's edge stage
     float *ew, *euh, *evh;         // [N] explicit_update

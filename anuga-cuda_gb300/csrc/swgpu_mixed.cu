@@ -27,7 +27,7 @@
 //  * FP32 <-> FP64 conversions of the state run on the integer pipe.
 //
 // Bytes per triangle-step (own arrays; neighbour gathers hit L1/L2):
-//   distribute ~102, flux ~124, update ~104.
+//   distribute ~114, flux ~128, update ~104.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -176,13 +176,13 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
     if (k < N) {
         const float eps = P.f_eps;
         const float wk = ro(X.wf + k), lk = ro(X.wlo + k), hc = ro(X.hf + k);
-        float dw[3], vu[3], vv[3], dz[3];
+        float eh[3], ew[3], eu[3], ev[3];  // own edge depth, stage jump, momentum
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            dw[i] = ro(X.dw + i * N + k);
-            vu[i] = ro(X.uhv + i * N + k);
-            vv[i] = ro(X.vhv + i * N + k);
-            dz[i] = ro(X.dze + i * N + k);
+            eh[i] = ro(X.he + i * N + k);
+            ew[i] = ro(X.dwe + i * N + k);
+            eu[i] = ro(X.uhe + i * N + k);
+            ev[i] = ro(X.vhe + i * N + k);
         }
         const float rk = ro(X.radius + k);
         const float inv_area = ro(X.inv_area + k);
@@ -190,23 +190,19 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
         float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            const int ia = (i == 0) ? 1 : 0, ib = (i == 2) ? 1 : 2;
             const int pk = ro(M.nbr + i * N + k);
             const float n1 = ro(X.nx + i * N + k), n2 = ro(X.ny + i * N + k);
             const float L = ro(X.len + i * N + k);
-            const float dwl = 0.5f * (dw[ia] + dw[ib]);
-            const float hl = edge_depth(hc, dw[ia], dw[ib], dz[i]);
-            const float uhl = 0.5f * (vu[ia] + vu[ib]);
-            const float vhl = 0.5f * (vv[ia] + vv[ib]);
+            const float dwl = ew[i], hl = eh[i], uhl = eu[i], vhl = ev[i];
             float hr, uhr, vhr, jump, rn = 3.0e38f;
             if (pk >= 0) {
+                // the neighbour's stored edge state: the very numbers it uses
+                // itself, so both sides see the same two states
                 const int n = pk >> 2, m = pk & 3;
-                const int a = (m == 0) ? 1 : 0, b = (m == 2) ? 1 : 2;
-                const float dwa = ro(X.dw + a * N + n), dwb = ro(X.dw + b * N + n);
-                hr = edge_depth(ro(X.hf + n), dwa, dwb, ro(X.dze + m * N + n));
-                jump = ((ro(X.wf + n) - wk) + (ro(X.wlo + n) - lk)) + (0.5f * (dwa + dwb) - dwl);
-                uhr = 0.5f * (ro(X.uhv + a * N + n) + ro(X.uhv + b * N + n));
-                vhr = 0.5f * (ro(X.vhv + a * N + n) + ro(X.vhv + b * N + n));
+                hr = ro(X.he + m * N + n);
+                jump = ((ro(X.wf + n) - wk) + (ro(X.wlo + n) - lk)) + (ro(X.dwe + m * N + n) - dwl);
+                uhr = ro(X.uhe + m * N + n);
+                vhr = ro(X.vhe + m * N + n);
                 rn = ro(X.radius + n);
             } else {
                 const int mb = -pk - 1;
@@ -276,7 +272,7 @@ __device__ __forceinline__ void finish_state(const DevParams &P, double &h, doub
 
 // Update: h += dt*E_h;  q += q*(r - 1) + dt*E_q*r  with r = 1/(1 - dt*S) the
 // semi-implicit Manning factor.  Increments in FP32, additions in FP64.
-__global__ void __launch_bounds__(kBlock) update_mixed(DevMesh M, DevState S, DevMixed X,
+__global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S, DevMixed X,
                                                        DevParams P, Ctrl *ctrl, int flags) {
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     const StepClock clk = published_step_clock(ctrl);
@@ -385,7 +381,7 @@ __device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], floa
 }
 
 // Extrapolation + balance + boundary conditions, FP32, in stage jumps.
-__global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S, DevMixed X,
+__global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevState S, DevMixed X,
                                                            DevParams P, const BcTag *tags,
                                                            Ctrl *ctrl, int flags) {
     const bool fused = flags & kFused;
@@ -461,11 +457,21 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                 }
             }
             if (keep) {
+                // previous vertex values, from the stored edge values of the
+                // (linear) reconstruction: v_i = e_a + e_b - e_i
+                float e0[3], e1[3], e2[3];
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    dw[i] = X.dw[i * N + k];
-                    ou[i] = X.uhv[i * N + k];
-                    ov[i] = X.vhv[i * N + k];
+                    e0[i] = X.dwe[i * N + k];
+                    e1[i] = X.uhe[i * N + k];
+                    e2[i] = X.vhe[i * N + k];
+                }
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
+                    dw[i] = (e0[a] + e0[b]) - e0[i];
+                    ou[i] = (e1[a] + e1[b]) - e1[i];
+                    ov[i] = (e2[a] + e2[b]) - e2[i];
                 }
             } else {
 #pragma unroll
@@ -529,11 +535,17 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                 }
             }
         }
+        // edge values (quantity.c:687-706 interpolation) stored for the flux:
+        // depth, stage jump from the centroid, momentum
+        float hle_[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            X.dw[i * N + k] = dw[i];
-            X.uhv[i * N + k] = ou[i];
-            X.vhv[i * N + k] = ov[i];
+            const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
+            hle_[i] = edge_depth(hc, dw[a], dw[b], ro(X.dze + i * N + k));
+            X.he[i * N + k] = hle_[i];
+            X.dwe[i * N + k] = 0.5f * (dw[a] + dw[b]);
+            X.uhe[i * N + k] = 0.5f * (ou[a] + ou[b]);
+            X.vhe[i * N + k] = 0.5f * (ov[a] + ov[b]);
         }
         if ((flags & kWriteBoundary) && ro(M.nb + k) > 0) {
             const double time = ctrl->time;
@@ -543,7 +555,7 @@ __global__ void __launch_bounds__(kBlock) distribute_mixed(DevMesh M, DevState S
                 if (pk < 0) {
                     const int mb = -pk - 1;
                     const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-                    const float hle = edge_depth(hc, dw[a], dw[b], ro(X.dze + i * N + k));
+                    const float hle = hle_[i];
                     const double ze = ro(S.ze + i * N + k);
                     const double we = ze + widen(hle);
                     const float uhe = 0.5f * (ou[a] + ou[b]);
@@ -604,18 +616,27 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
 }
 
 // FP64 stage centroid / vertex values and momentum vertex values for
-// downloads: w = h + z, w_v = w + (vertex stage jump).
+// downloads: w = h + z, vertex values from the stored edge values of the
+// linear reconstruction (v_i = e_a + e_b - e_i).
 __global__ void __launch_bounds__(kBlock) vertices_from_mixed(DevMesh M, DevState S, DevMixed X) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = M.N;
     if (k >= N) return;
     const double w = X.hd[k] + S.zc[k];
     S.w[k] = w;
+    float e0[3], e1[3], e2[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        S.wv[i * N + k] = w + (double)X.dw[i * N + k];
-        S.uhv[i * N + k] = (double)X.uhv[i * N + k];
-        S.vhv[i * N + k] = (double)X.vhv[i * N + k];
+        e0[i] = X.dwe[i * N + k];
+        e1[i] = X.uhe[i * N + k];
+        e2[i] = X.vhe[i * N + k];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
+        S.wv[i * N + k] = w + (double)((e0[a] + e0[b]) - e0[i]);
+        S.uhv[i * N + k] = (double)((e1[a] + e1[b]) - e1[i]);
+        S.vhv[i * N + k] = (double)((e2[a] + e2[b]) - e2[i]);
     }
 }
 

@@ -28,7 +28,7 @@ STOP_NONE, STOP_YIELD, STOP_FINAL, STOP_BUDGET, STOP_ERROR = range(5)
 STATUS_NAMES = {
     0: "SWGPU_OK", 1: "SWGPU_EINVAL", 2: "SWGPU_ECUDA", 3: "SWGPU_ENOMEM",
     4: "SWGPU_EDENOMINATOR", 5: "SWGPU_ESMALLSTEP", 6: "SWGPU_ENONFINITE", 7: "SWGPU_EBED",
-    8: "SWGPU_EBOUNDARY", 9: "SWGPU_EOVERSHOOT", 10: "SWGPU_EMESH",
+    8: "SWGPU_EBOUNDARY", 9: "SWGPU_EOVERSHOOT", 10: "SWGPU_EMESH", 11: "SWGPU_ETIMEOUT",
 }
 
 _i64p = C.POINTER(C.c_int64)

@@ -109,6 +109,7 @@ static const char *status_text(int s) {
         case SWGPU_EBOUNDARY: return "unknown boundary type";
         case SWGPU_EOVERSHOOT: return "model time overshot finaltime";
         case SWGPU_EMESH: return "inconsistent mesh";
+        case SWGPU_ETIMEOUT: return "a bounded device-side wait ran out";
         default: return "unknown status";
     }
 }
@@ -437,34 +438,36 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
         TRY(dalloc(h, &S.max_speed, n1));
     } else {
         DevMixed &X = h->X;
-        TRY(dalloc(h, &X.hd, n1));
-        TRY(dalloc(h, &X.wf, n1));
-        TRY(dalloc(h, &X.wlo, n1));
-        TRY(dalloc(h, &X.hf, n1));
-        TRY(dalloc(h, &X.uvel, n1));
-        TRY(dalloc(h, &X.vvel, n1));
-        TRY(dalloc(h, &X.he, n3));
-        TRY(dalloc(h, &X.dwe, n3));
-        TRY(dalloc(h, &X.uhe, n3));
-        TRY(dalloc(h, &X.vhe, n3));
+        X.S = (int)(((size_t)N + 63) / 64 * 64);
+        const size_t s1 = X.S, s3 = 3 * s1, s6 = 6 * s1;
+        TRY(dalloc(h, &X.hd, s1));
+        TRY(dalloc(h, &X.wf, s1));
+        TRY(dalloc(h, &X.wlo, s1));
+        TRY(dalloc(h, &X.hf, s1));
+        TRY(dalloc(h, &X.uvel, s1));
+        TRY(dalloc(h, &X.vvel, s1));
+        TRY(dalloc(h, &X.he, s3));
+        TRY(dalloc(h, &X.dwe, s3));
+        TRY(dalloc(h, &X.uhe, s3));
+        TRY(dalloc(h, &X.vhe, s3));
         TRY(dalloc(h, &X.hbf, nb1));
         TRY(dalloc(h, &X.uhbf, nb1));
         TRY(dalloc(h, &X.vhbf, nb1));
         TRY(dalloc(h, &X.wjb, nb1));
-        TRY(dalloc(h, &X.ew, n1));
-        TRY(dalloc(h, &X.euh, n1));
-        TRY(dalloc(h, &X.evh, n1));
-        TRY(dalloc(h, &X.nx, n3));
-        TRY(dalloc(h, &X.ny, n3));
-        TRY(dalloc(h, &X.len, n3));
-        TRY(dalloc(h, &X.inv_area, n1));
-        TRY(dalloc(h, &X.radius, n1));
-        TRY(dalloc(h, &X.gc, n6));
-        TRY(dalloc(h, &X.dzv, n3));
-        TRY(dalloc(h, &X.dze, n3));
-        TRY(dalloc(h, &X.fric, n1));
-        TRY(dalloc(h, &X.zmoff, n1));
-        TRY(dalloc(h, &X.kind, n1));
+        TRY(dalloc(h, &X.ew, s1));
+        TRY(dalloc(h, &X.euh, s1));
+        TRY(dalloc(h, &X.evh, s1));
+        TRY(dalloc(h, &X.nx, s3));
+        TRY(dalloc(h, &X.ny, s3));
+        TRY(dalloc(h, &X.len, s3));
+        TRY(dalloc(h, &X.inv_area, s1));
+        TRY(dalloc(h, &X.radius, s1));
+        TRY(dalloc(h, &X.gc, s6));
+        TRY(dalloc(h, &X.dzv, s3));
+        TRY(dalloc(h, &X.dze, s3));
+        TRY(dalloc(h, &X.fric, s1));
+        TRY(dalloc(h, &X.zmoff, s1));
+        TRY(dalloc(h, &X.kind, s1));
         // FP64 vertex planes are kept for downloads (stage = depth + bed)
         TRY(dalloc(h, &S.wv, n3));
         TRY(dalloc(h, &S.uhv, n3));

@@ -153,8 +153,9 @@ __device__ __forceinline__ void block_min_timestep(double t, Ctrl *ctrl) {
 
 // FP32 variant for the mixed flux: the reduction stays in FP32 and only the
 // block's minimum is widened for the atomic.
+template <int BLOCK = kBlock>
 __device__ __forceinline__ void block_min_timestep_f(float t, Ctrl *ctrl) {
-    __shared__ float wminf[kBlock / 32];
+    __shared__ float wminf[BLOCK / 32];
     for (int o = 16; o > 0; o >>= 1) t = ominf(t, __shfl_xor_sync(0xffffffffu, t, o));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) wminf[warp] = t;

@@ -63,8 +63,11 @@ struct DevState {
 // centroid bed, so that hydrostatic pressure and bed-slope terms never
 // subtract two large FP32 numbers.
 struct DevMixed {
+    int S;                         // stride of the [3]/[6] planes: N rounded up to 64, so
+                                   // that every plane and 16-triangle tile is 64-B aligned
     double *hd;                    // [N] FP64 depth (conserved)
-    float *wf, *wlo;               // [N] centroid stage as hi + lo FP32 pair
+    float *wf, *wlo;               // [N] centroid stage as hi + lo FP32 pair (single planes
+                                   // are allocated with S elements too)
     float *hf, *uvel, *vvel;       // [N] centroid depth, velocities
     float *he, *dwe;               // [3][N] edge depth, edge stage jump from the centroid
     float *uhe, *vhe;              // [3][N] edge momentum

@@ -166,46 +166,147 @@ __device__ __forceinline__ void edge_flux_dev(float hl_in, float uhl_in, float v
     f2 = n2 * e1 + n1 * e2;
 }
 
-// Fluxes + gravity_wb, FP32, triangle centric (no atomics).
-__global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevParams P,
-                                                     Ctrl *ctrl, int flags) {
+// ---- one-dimensional TMA (cp.async.bulk) staging of a block's tile ------
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// Global -> shared bulk copy completing on the mbarrier.  dst, src 16-byte
+// aligned, bytes a multiple of 16 (planes are padded to 64 elements and
+// tiles start at multiples of 128 elements).
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes,
+                                          unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned phase) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(phase) : "memory");
+    return ok != 0;
+}
+// Bounded wait for phase 0: every thread gives up after kWaitLimit polls
+// (each poll may suspend in hardware), reports SWGPU_ETIMEOUT, and polls once
+// more as long again so that copies still in flight land before the block
+// leaves.  Returns true when the data arrived.
+constexpr int kWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, Ctrl *ctrl) {
+    for (int it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, 0)) return true;
+    set_status(ctrl, SWGPU_ETIMEOUT);
+    for (int it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, 0)) break;
+    return false;
+}
+
+constexpr int kFluxTile = 128;  // triangles per flux block (= threads)
+
+// The flux kernel's own data for one tile, filled by 26 bulk copies.
+struct __align__(128) FluxTile {
+    float wf[kFluxTile], wlo[kFluxTile], hf[kFluxTile], radius[kFluxTile], inv_area[kFluxTile];
+    float he[3][kFluxTile], dwe[3][kFluxTile], uhe[3][kFluxTile], vhe[3][kFluxTile];
+    float nx[3][kFluxTile], ny[3][kFluxTile], len[3][kFluxTile];
+};
+
+// Fluxes + gravity_wb, FP32, triangle centric (no atomics).  Each block
+// stages its tile of 128 triangles with one-dimensional TMA bulk copies into
+// shared memory; neighbours inside the tile (most of them, in Morton order)
+// are read from shared memory, the others from global memory.
+__global__ void __launch_bounds__(kFluxTile) flux_mixed(DevMesh M, DevMixed X, DevParams P,
+                                                        Ctrl *ctrl, int flags) {
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
-    const int N = M.N;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    float t = P.f_max_dt;
-    if (k < N) {
-        const float eps = P.f_eps;
-        const float wk = ro(X.wf + k), lk = ro(X.wlo + k), hc = ro(X.hf + k);
-        float eh[3], ew[3], eu[3], ev[3];  // own edge depth, stage jump, momentum
+    __shared__ FluxTile T;
+    __shared__ __align__(8) unsigned long long bar;
+    const int N = M.N, SP = X.S;
+    const int tid = threadIdx.x;
+    const int k0 = blockIdx.x * kFluxTile;
+    const int cnt = min(kFluxTile, N - k0);
+    // tile length in the padded planes (a multiple of 64 elements)
+    const int span = min(kFluxTile, SP - k0);
+    if (tid == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned bytes = (unsigned)span * 4u;
+        mbar_arrive_expect_tx(&bar, 26u * bytes);
+        bulk_load(T.wf, X.wf + k0, bytes, &bar);
+        bulk_load(T.wlo, X.wlo + k0, bytes, &bar);
+        bulk_load(T.hf, X.hf + k0, bytes, &bar);
+        bulk_load(T.radius, X.radius + k0, bytes, &bar);
+        bulk_load(T.inv_area, X.inv_area + k0, bytes, &bar);
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            eh[i] = ro(X.he + i * N + k);
-            ew[i] = ro(X.dwe + i * N + k);
-            eu[i] = ro(X.uhe + i * N + k);
-            ev[i] = ro(X.vhe + i * N + k);
+            bulk_load(T.he[i], X.he + i * SP + k0, bytes, &bar);
+            bulk_load(T.dwe[i], X.dwe + i * SP + k0, bytes, &bar);
+            bulk_load(T.uhe[i], X.uhe + i * SP + k0, bytes, &bar);
+            bulk_load(T.vhe[i], X.vhe + i * SP + k0, bytes, &bar);
+            bulk_load(T.nx[i], X.nx + i * SP + k0, bytes, &bar);
+            bulk_load(T.ny[i], X.ny + i * SP + k0, bytes, &bar);
+            bulk_load(T.len[i], X.len + i * SP + k0, bytes, &bar);
         }
-        const float rk = ro(X.radius + k);
-        const float inv_area = ro(X.inv_area + k);
+    }
+    // the neighbour indices are not padded planes: ordinary loads, issued
+    // while the bulk copies are in flight
+    const int k = k0 + tid;
+    int pk[3] = {0, 0, 0};
+    if (tid < cnt) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) pk[i] = ro(M.nbr + i * N + k);
+    }
+    const bool arrived = mbar_wait_bounded(&bar, ctrl);
+    float t = P.f_max_dt;
+    if (arrived && tid < cnt) {
+        const float eps = P.f_eps;
+        const float wk = T.wf[tid], lk = T.wlo[tid], hc = T.hf[tid];
+        const float rk = T.radius[tid];
+        const float inv_area = T.inv_area[tid];
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // flux sums
         float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            const int pk = ro(M.nbr + i * N + k);
-            const float n1 = ro(X.nx + i * N + k), n2 = ro(X.ny + i * N + k);
-            const float L = ro(X.len + i * N + k);
-            const float dwl = ew[i], hl = eh[i], uhl = eu[i], vhl = ev[i];
+            const float n1 = T.nx[i][tid], n2 = T.ny[i][tid], L = T.len[i][tid];
+            const float dwl = T.dwe[i][tid], hl = T.he[i][tid];
+            const float uhl = T.uhe[i][tid], vhl = T.vhe[i][tid];
             float hr, uhr, vhr, jump, rn = 3.0e38f;
-            if (pk >= 0) {
+            if (pk[i] >= 0) {
                 // the neighbour's stored edge state: the very numbers it uses
                 // itself, so both sides see the same two states
-                const int n = pk >> 2, m = pk & 3;
-                hr = ro(X.he + m * N + n);
-                jump = ((ro(X.wf + n) - wk) + (ro(X.wlo + n) - lk)) + (ro(X.dwe + m * N + n) - dwl);
-                uhr = ro(X.uhe + m * N + n);
-                vhr = ro(X.vhe + m * N + n);
-                rn = ro(X.radius + n);
+                const int n = pk[i] >> 2, m = pk[i] & 3;
+                const int ln = n - k0;
+                float wn, lnn, dwn;
+                if ((unsigned)ln < (unsigned)cnt) {
+                    hr = T.he[m][ln];
+                    dwn = T.dwe[m][ln];
+                    uhr = T.uhe[m][ln];
+                    vhr = T.vhe[m][ln];
+                    wn = T.wf[ln];
+                    lnn = T.wlo[ln];
+                    rn = T.radius[ln];
+                } else {
+                    hr = ro(X.he + m * SP + n);
+                    dwn = ro(X.dwe + m * SP + n);
+                    uhr = ro(X.uhe + m * SP + n);
+                    vhr = ro(X.vhe + m * SP + n);
+                    wn = ro(X.wf + n);
+                    lnn = ro(X.wlo + n);
+                    rn = ro(X.radius + n);
+                }
+                jump = ((wn - wk) + (lnn - lk)) + (dwn - dwl);
             } else {
-                const int mb = -pk - 1;
+                const int mb = -pk[i] - 1;
                 hr = ro(X.hbf + mb);
                 jump = ro(X.wjb + mb);
                 uhr = ro(X.uhbf + mb);
@@ -227,7 +328,7 @@ __global__ void __launch_bounds__(kBlock) flux_mixed(DevMesh M, DevMixed X, DevP
         X.euh[k] = (a1 - ghc * gx) * inv_area;
         X.evh[k] = (a2 - ghc * gy) * inv_area;
     }
-    block_min_timestep_f(t, ctrl);
+    block_min_timestep_f<kFluxTile>(t, ctrl);
     if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
         publish_step_clock(ctrl, P);
 }
@@ -386,7 +487,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
                                                            Ctrl *ctrl, int flags) {
     const bool fused = flags & kFused;
     if (fused && ctrl_halted(ctrl)) return;
-    const int N = M.N;
+    const int N = M.N, SP = X.S;
     const int order = (int)ctrl->order;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int bad_bc = 0;
@@ -399,7 +500,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
         const float uk = qu * hk, vk = qv * hk;  // centroid momentum
         float dzv[3];
 #pragma unroll
-        for (int i = 0; i < 3; i++) dzv[i] = ro(X.dzv + i * N + k);
+        for (int i = 0; i < 3; i++) dzv[i] = ro(X.dzv + i * SP + k);
         float dw[3] = {0.f, 0.f, 0.f};  // vertex stage jumps
         float ou[3], ov[3];             // vertex momentum (or velocity)
         if (order != 1) {
@@ -410,7 +511,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
             if ((kind & 3) != 2) {
                 float c[6];
 #pragma unroll
-                for (int j = 0; j < 6; j++) c[j] = ro(X.gc + j * N + k);
+                for (int j = 0; j < 6; j++) c[j] = ro(X.gc + j * SP + k);
                 if ((kind & 3) == 0) {
                     const int k0 = ro(M.surr + k), k1 = ro(M.surr + N + k),
                               k2 = ro(M.surr + 2 * N + k);
@@ -462,9 +563,9 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
                 float e0[3], e1[3], e2[3];
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    e0[i] = X.dwe[i * N + k];
-                    e1[i] = X.uhe[i * N + k];
-                    e2[i] = X.vhe[i * N + k];
+                    e0[i] = X.dwe[i * SP + k];
+                    e1[i] = X.uhe[i * SP + k];
+                    e2[i] = X.vhe[i * SP + k];
                 }
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
@@ -541,11 +642,11 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-            hle_[i] = edge_depth(hc, dw[a], dw[b], ro(X.dze + i * N + k));
-            X.he[i * N + k] = hle_[i];
-            X.dwe[i * N + k] = 0.5f * (dw[a] + dw[b]);
-            X.uhe[i * N + k] = 0.5f * (ou[a] + ou[b]);
-            X.vhe[i * N + k] = 0.5f * (ov[a] + ov[b]);
+            hle_[i] = edge_depth(hc, dw[a], dw[b], ro(X.dze + i * SP + k));
+            X.he[i * SP + k] = hle_[i];
+            X.dwe[i * SP + k] = 0.5f * (dw[a] + dw[b]);
+            X.uhe[i * SP + k] = 0.5f * (ou[a] + ou[b]);
+            X.vhe[i * SP + k] = 0.5f * (ov[a] + ov[b]);
         }
         if ((flags & kWriteBoundary) && ro(M.nb + k) > 0) {
             const double time = ctrl->time;
@@ -563,7 +664,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
                     const BcTag &T = tags[ro(M.btag + mb)];
                     double wb, uhb, vhb;
                     if (!eval_boundary(T, time, we, widen(uhe), widen(vhe),
-                                       widen(ro(X.nx + i * N + k)), widen(ro(X.ny + i * N + k)),
+                                       widen(ro(X.nx + i * SP + k)), widen(ro(X.ny + i * SP + k)),
                                        wb, uhb, vhb)) {
                         bad_bc = 1;
                         wb = we;
@@ -620,16 +721,16 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
 // linear reconstruction (v_i = e_a + e_b - e_i).
 __global__ void __launch_bounds__(kBlock) vertices_from_mixed(DevMesh M, DevState S, DevMixed X) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int N = M.N;
+    const int N = M.N, SP = X.S;
     if (k >= N) return;
     const double w = X.hd[k] + S.zc[k];
     S.w[k] = w;
     float e0[3], e1[3], e2[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        e0[i] = X.dwe[i * N + k];
-        e1[i] = X.uhe[i * N + k];
-        e2[i] = X.vhe[i * N + k];
+        e0[i] = X.dwe[i * SP + k];
+        e1[i] = X.uhe[i * SP + k];
+        e2[i] = X.vhe[i * SP + k];
     }
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -674,7 +775,7 @@ void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed
 }
 void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, const DevParams &P,
                        Ctrl *ctrl, int flags, cudaStream_t st) {
-    flux_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, X, P, ctrl, flags);
+    flux_mixed<<<(M.N + kFluxTile - 1) / kFluxTile, kFluxTile, 0, st>>>(M, X, P, ctrl, flags);
 }
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st) {
@@ -701,7 +802,7 @@ void launch_mass_mixed(const DevMesh &M, const DevState &S, const DevMixed &X, d
 // the host geometry and the current bed (downloaded) and friction.
 int build_mixed_geometry(Handle *h) {
     const int N = h->M.N;
-    const size_t n1 = N, n3 = 3 * (size_t)N;
+    const size_t n1 = N, n3 = 3 * (size_t)N, sp = h->X.S;
     std::vector<double> zc(n1), zv(n3), ze(n3), fr(n1);
     cudaStreamSynchronize(h->stream);
     if (cudaMemcpy(zc.data(), h->S.zc, n1 * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
@@ -709,17 +810,18 @@ int build_mixed_geometry(Handle *h) {
         cudaMemcpy(ze.data(), h->S.ze, n3 * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(fr.data(), h->S.fric, n1 * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
         return SWGPU_ECUDA;
-    std::vector<float> nx(n3), ny(n3), len(n3), inv_area(n1), radius(n1), gc(6 * n1), dzv(n3),
-        dze(n3), fric(n1), zmoff(n1);
+    // FP32 planes use the padded stride sp (see DevMixed::S)
+    std::vector<float> nx(3 * sp), ny(3 * sp), len(3 * sp), inv_area(n1), radius(n1), gc(6 * sp),
+        dzv(3 * sp), dze(3 * sp), fric(n1), zmoff(n1);
     std::vector<uint8_t> kind(n1);
     const std::vector<double> &V = h->h_vxy, &C = h->h_cxy;
     for (int k = 0; k < N; k++) {
         for (int i = 0; i < 3; i++) {
-            nx[i * n1 + k] = (float)h->h_normals[(2 * i) * n1 + k];
-            ny[i * n1 + k] = (float)h->h_normals[(2 * i + 1) * n1 + k];
-            len[i * n1 + k] = (float)h->h_len[i * n1 + k];
-            dzv[i * n1 + k] = (float)(zv[i * n1 + k] - zc[k]);
-            dze[i * n1 + k] = (float)(ze[i * n1 + k] - zc[k]);
+            nx[i * sp + k] = (float)h->h_normals[(2 * i) * n1 + k];
+            ny[i * sp + k] = (float)h->h_normals[(2 * i + 1) * n1 + k];
+            len[i * sp + k] = (float)h->h_len[i * n1 + k];
+            dzv[i * sp + k] = (float)(zv[i * n1 + k] - zc[k]);
+            dze[i * sp + k] = (float)(ze[i * n1 + k] - zc[k]);
         }
         inv_area[k] = (float)(1.0 / h->h_areas[k]);
         radius[k] = (float)h->h_radii[k];
@@ -760,21 +862,21 @@ int build_mixed_geometry(Handle *h) {
             }
         }
         kind[k] = kd;
-        for (int j = 0; j < 6; j++) gc[j * n1 + k] = (float)c[j];
+        for (int j = 0; j < 6; j++) gc[j * sp + k] = (float)c[j];
     }
     const DevMixed &X = h->X;
     cudaError_t e = cudaSuccess;
     auto put = [&](void *dst, const void *src, size_t bytes) {
         if (e == cudaSuccess) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
     };
-    put(X.nx, nx.data(), n3 * 4);
-    put(X.ny, ny.data(), n3 * 4);
-    put(X.len, len.data(), n3 * 4);
+    put(X.nx, nx.data(), 3 * sp * 4);
+    put(X.ny, ny.data(), 3 * sp * 4);
+    put(X.len, len.data(), 3 * sp * 4);
     put(X.inv_area, inv_area.data(), n1 * 4);
     put(X.radius, radius.data(), n1 * 4);
-    put(X.gc, gc.data(), 6 * n1 * 4);
-    put(X.dzv, dzv.data(), n3 * 4);
-    put(X.dze, dze.data(), n3 * 4);
+    put(X.gc, gc.data(), 6 * sp * 4);
+    put(X.dzv, dzv.data(), 3 * sp * 4);
+    put(X.dze, dze.data(), 3 * sp * 4);
     put(X.fric, fric.data(), n1 * 4);
     put(X.zmoff, zmoff.data(), n1 * 4);
     put(X.kind, kind.data(), n1);

@@ -43,7 +43,8 @@ enum swgpu_status {
     SWGPU_EBED = 7,            /* discontinuous bed across an edge          */
     SWGPU_EBOUNDARY = 8,       /* unknown boundary type                     */
     SWGPU_EOVERSHOOT = 9,      /* model time overshot finaltime             */
-    SWGPU_EMESH = 10           /* inconsistent mesh arrays                  */
+    SWGPU_EMESH = 10,          /* inconsistent mesh arrays                  */
+    SWGPU_ETIMEOUT = 11        /* a bounded device-side wait ran out        */
 };
 
 /* ---- precision of the evolve path ------------------------------------ */

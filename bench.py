@@ -49,7 +49,11 @@ UNIT = "triangle-steps/s"
 
 # algorithmic bytes per triangle-step of each kernel (own arrays, neighbour
 # gathers counted as cache hits)
-MIXED_BYTES = {"flux": 124, "update": 104, "distribute": 102}
+MIXED_BYTES = {"flux": 128, "update": 104, "distribute": 114}
+# DRAM bytes (read + write) per launch from one ncu capture of the 1,000,000-
+# triangle case (500x500 cells), scaled by 4 to the 4,000,000-triangle mesh;
+# traffic grows in proportion to the triangles a launch processes
+NCU_TRAFFIC_1M = {"flux": 122.79e6, "update": 65.57e6, "distribute": 107.50e6}
 FP64_BYTES = {"flux": 296, "update": 120, "distribute": 253}
 MODEL_BYTES = {"mixed": 368, "fp64": 568}   # whole-step byte model
 ACC_STEPS = 1000                             # steps of the mixed-vs-FP64 accuracy check
@@ -58,7 +62,7 @@ ACC_STEPS = 1000                             # steps of the mixed-vs-FP64 accura
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=160)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=16)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=1000, help="rectangular_cross cells per side")
@@ -353,12 +357,15 @@ def main():
         "kernel_ms": dict(zip(names, kms)),
         "roofline": {"bound": "hbm", "kernel": names[dom] + "_mixed", "achieved": achieved,
                      "peak": peak_gbs, "unit": "GB/s", "frac": achieved / peak_gbs,
-                     "traffic": None,
+                     "traffic": NCU_TRAFFIC_1M[names[dom]] * N / 1.0e6,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                       "1,000,000-triangle capture scaled to this mesh",
                      "peak_source": "measured" if peaks else "fallback",
                      "step_model_frac": MODEL_BYTES["mixed"] * N / (mixed_ms / K / 1000.0) / 1e9
                      / peak_gbs},
         "clocks": r["mixed"]["clocks"],
-        "gpu_launches": 3 * K * 2 + 3 * 32 * 2,
+        # the timed region launches whole graphs of 16 steps x 3 kernels
+        "gpu_launches": 3 * 16 * ((K + 15) // 16),
     }
     if out["e2e"]:
         line["e2e"] = {k: out["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step",

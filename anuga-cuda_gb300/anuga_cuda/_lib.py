@@ -18,10 +18,12 @@ __all__ = [
     "STAGE", "XMOMENTUM", "YMOMENTUM", "ELEVATION", "FRICTION", "HEIGHT", "XVELOCITY",
     "YVELOCITY", "FP64", "MIXED", "BC_REFLECTIVE", "BC_DIRICHLET", "BC_TIME_STAGE_SINE",
     "STOP_NONE", "STOP_YIELD", "STOP_FINAL", "STOP_BUDGET", "STOP_ERROR", "EXPORTED_SYMBOLS",
+    "EULER", "RK2", "RK3",
 ]
 
 STAGE, XMOMENTUM, YMOMENTUM, ELEVATION, FRICTION, HEIGHT, XVELOCITY, YVELOCITY = range(8)
 FP64, MIXED = 0, 1
+EULER, RK2, RK3 = 1, 2, 3
 BC_REFLECTIVE, BC_DIRICHLET, BC_TIME_STAGE_SINE = 0, 1, 2
 STOP_NONE, STOP_YIELD, STOP_FINAL, STOP_BUDGET, STOP_ERROR = range(5)
 
@@ -108,6 +110,9 @@ _SIGNATURES = [
     ("swgpu_compute_forcing_terms", C.c_int, [_VP]),
     ("swgpu_update_conserved_quantities", C.c_int, [_VP, C.c_double]),
     ("swgpu_update_other_quantities", C.c_int, [_VP]),
+    ("swgpu_backup_conserved_quantities", C.c_int, [_VP]),
+    ("swgpu_saxpy_conserved_quantities", C.c_int, [_VP, C.c_double, C.c_double]),
+    ("swgpu_set_timestepping_method", C.c_int, [_VP, C.c_int]),
     ("swgpu_mass", C.c_int, [_VP, _f64p]),
     ("swgpu_get_state", C.c_int, [_VP, C.POINTER(State_t)]),
     ("swgpu_set_state", C.c_int, [_VP, C.POINTER(State_t)]),

@@ -151,6 +151,7 @@ class GPU_domain:
         self.timestep = None
         self.yieldstep = None
         self.finaltime = None
+        self._timestepping_method = "euler"
         self._h = None
         self._create()
 
@@ -328,12 +329,23 @@ class GPU_domain:
         self.parameters = self.parameters.replace(default_order=n)
         self._order_ = n
 
+    _TIMESTEPPING = {"euler": _lib.EULER, "rk2": _lib.RK2, "rk3": _lib.RK3}
+
     def get_timestepping_method(self):
-        return "euler"
+        return self._timestepping_method
 
     def set_timestepping_method(self, method):
-        if method != "euler":
-            raise NotImplementedError("only euler timestepping runs on the GPU")
+        """'euler', 'rk2' or 'rk3' (or 1, 2, 3): the step that evolve runs."""
+        if isinstance(method, int):
+            names = {v: k for k, v in self._TIMESTEPPING.items()}
+            if method not in names:
+                raise ValueError(f"timestepping method {method}")
+            method = names[method]
+        if method not in self._TIMESTEPPING:
+            raise ValueError(f"timestepping method {method!r}: euler, rk2 or rk3")
+        check(lib().swgpu_set_timestepping_method(self._h, self._TIMESTEPPING[method]),
+              self._h)
+        self._timestepping_method = method
 
     def set_name(self, name):
         self.name = name
@@ -411,6 +423,46 @@ class GPU_domain:
         self.update_timestep(yieldstep, finaltime)
         self.update_conserved_quantities()
 
+    def backup_conserved_quantities(self):
+        check(lib().swgpu_backup_conserved_quantities(self._h), self._h)
+
+    def saxpy_conserved_quantities(self, a, b):
+        check(lib().swgpu_saxpy_conserved_quantities(self._h, float(a), float(b)), self._h)
+
+    def _rk_stage(self):
+        self.compute_fluxes()
+        self.compute_forcing_terms()
+        self.update_conserved_quantities()
+
+    def evolve_one_rk2_step(self, yieldstep, finaltime):
+        """ANUGA Generic_Domain.evolve_one_rk2_step (called at
+        gpu_domain_advanced.py:2198-2204), one method at a time: the second
+        stage reuses the first stage's timestep."""
+        self.backup_conserved_quantities()
+        self.evolve_one_euler_step(yieldstep, finaltime)
+        self.set_time(self.get_time() + self.timestep)
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._rk_stage()
+        self.saxpy_conserved_quantities(0.5, 0.5)
+
+    def evolve_one_rk3_step(self, yieldstep, finaltime):
+        """ANUGA Generic_Domain.evolve_one_rk3_step (called at
+        gpu_domain_advanced.py:2248-2254), one method at a time."""
+        initial_time = self.get_time()
+        self.backup_conserved_quantities()
+        self.evolve_one_euler_step(yieldstep, finaltime)
+        self.set_time(self.get_time() + self.timestep)
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._rk_stage()
+        self.saxpy_conserved_quantities(0.25, 0.75)
+        self.set_time(initial_time + self.timestep * 0.5)
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._rk_stage()
+        self.saxpy_conserved_quantities(2.0 / 3.0, 1.0 / 3.0)
+
     def update_other_quantities(self):
         check(lib().swgpu_update_other_quantities(self._h), self._h)
 
@@ -436,7 +488,8 @@ class GPU_domain:
                max_steps=None):
         """Domain.evolve as a generator (gpu_domain_advanced.py:2296-2697).
 
-        The time loop runs on the device: each Euler step is three kernels,
+        The time loop runs on the device: each Euler stage is three kernels
+        (an RK2 step two stages, an RK3 step three; set_timestepping_method),
         the timestep is reduced on the device, and steps are issued as CUDA
         graphs; the host synchronises only between graphs and at yields.
         ``max_steps`` (added) stops after that many steps in total."""
@@ -474,7 +527,7 @@ class GPU_domain:
                 return
 
     def evolve_steps(self, nsteps, yieldstep=None, finaltime=None):
-        """Start an evolve and run exactly ``nsteps`` Euler steps with no
+        """Start an evolve and run exactly ``nsteps`` steps with no
         yields in between (unless finaltime comes first); returns the final
         device state."""
         if yieldstep is None:

@@ -146,20 +146,43 @@ static void reset_ftmin(Ctrl *c, const DevParams &P) {
 
 // ----------------------------------------------------------- step issue
 
-static int issue_fused_step(Handle *h) {
-    const int fused_flux = kFused;
-    const int fused_update = kFused | kFrictionInline;
-    const int fused_dist = kFused | kWriteBoundary;
+// One stage of a fused step: flux -> update (with the stage's backup or
+// saxpy and clock bookkeeping) -> distribute with boundary values.
+static void issue_stage(Handle *h, const Stage &stg) {
+    const int flux_flags = kFused | (stg.kind == kStageMid || stg.kind == kStageLast
+                                         ? kNoTimestep : 0);
+    const int update_flags = kFused | kFrictionInline;
+    const int dist_flags = kFused | kWriteBoundary;
     if (h->precision == SWGPU_FP64) {
-        launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, fused_flux, h->stream);
-        launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, fused_update, h->stream);
-        launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl, fused_dist, h->stream);
+        launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, flux_flags, h->stream);
+        launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, update_flags, stg, h->stream);
+        launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl, dist_flags, h->stream);
     } else {
-        launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, fused_flux, h->stream);
-        launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, fused_update, h->stream);
-        launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl, fused_dist,
+        launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, flux_flags, h->stream);
+        launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, update_flags, stg, h->stream);
+        launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl, dist_flags,
                                 h->stream);
     }
+}
+
+// The stages of one step of the handle's timestepping method (ANUGA's
+// evolve_one_euler_step / evolve_one_rk2_step / evolve_one_rk3_step followed
+// by the evolve loop's set_time, distribute and update_boundary).
+static void issue_step(Handle *h) {
+    if (h->timestepping_method == SWGPU_RK2) {
+        issue_stage(h, Stage{kStageFirst, 1.0, 0.0, 1.0});
+        issue_stage(h, Stage{kStageLast, 0.5, 0.5, 1.0});
+    } else if (h->timestepping_method == SWGPU_RK3) {
+        issue_stage(h, Stage{kStageFirst, 1.0, 0.0, 1.0});
+        issue_stage(h, Stage{kStageMid, 0.25, 0.75, 0.5});
+        issue_stage(h, Stage{kStageLast, 2.0 / 3.0, 1.0 / 3.0, 1.0});
+    } else {
+        issue_stage(h, kEulerStage);
+    }
+}
+
+static int issue_fused_step(Handle *h) {
+    issue_step(h);
     return check_launch(h, "evolve step");
 }
 
@@ -167,21 +190,7 @@ static int build_graph(Handle *h) {
     if (h->graph) return SWGPU_OK;
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < kStepsPerGraph; s++) {
-        if (h->precision == SWGPU_FP64) {
-            launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, kFused, h->stream);
-            launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, kFused | kFrictionInline,
-                               h->stream);
-            launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,
-                                   kFused | kWriteBoundary, h->stream);
-        } else {
-            launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused, h->stream);
-            launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused | kFrictionInline,
-                                h->stream);
-            launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl,
-                                    kFused | kWriteBoundary, h->stream);
-        }
-    }
+    for (int s = 0; s < kStepsPerGraph; s++) issue_step(h);
     CK(cudaStreamEndCapture(h->stream, &g));
     cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
@@ -423,6 +432,9 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
     TRY(dalloc(h, &S.ub, nb1));
     TRY(dalloc(h, &S.vb, nb1));
     TRY(dalloc(h, &S.partials, (size_t)grid_for((int)N) + 1));
+    TRY(dalloc(h, &S.bw, n1));   // Runge-Kutta backups
+    TRY(dalloc(h, &S.buh, n1));
+    TRY(dalloc(h, &S.bvh, n1));
     TRY(dalloc(h, &S.we, n3));
     TRY(dalloc(h, &S.uhe, n3));
     TRY(dalloc(h, &S.vhe, n3));
@@ -800,10 +812,47 @@ int swgpu_update_conserved_quantities(void *handle, double timestep) {
     Handle *h = static_cast<Handle *>(handle);
     int rc = require_fp64(h, "update_conserved_quantities");
     if (rc) return rc;
-    launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, timestep, 0, h->stream);
+    launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, timestep, 0, kEulerStage, h->stream);
     if ((rc = check_launch(h, "update_conserved_quantities"))) return rc;
     if ((rc = sync_ctrl(h))) return rc;
     return device_status(h);
+}
+
+int swgpu_backup_conserved_quantities(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "backup_conserved_quantities");
+    if (rc) return rc;
+    const size_t bytes = sizeof(double) * (size_t)h->M.N;
+    CK(cudaMemcpyAsync(h->S.bw, h->S.w, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->S.buh, h->S.uh, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->S.bvh, h->S.vh, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+int swgpu_saxpy_conserved_quantities(void *handle, double a, double b) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "saxpy_conserved_quantities");
+    if (rc) return rc;
+    launch_saxpy_fp64(h->M, h->S, a, b, h->stream);
+    if ((rc = check_launch(h, "saxpy_conserved_quantities"))) return rc;
+    h->vertices_stale = true;
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+int swgpu_set_timestepping_method(void *handle, int method) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (method != SWGPU_EULER && method != SWGPU_RK2 && method != SWGPU_RK3)
+        return fail(h, SWGPU_EINVAL, "timestepping method %d (1 euler, 2 rk2, 3 rk3)", method);
+    if (method != h->timestepping_method && h->graph) {
+        CK(cudaStreamSynchronize(h->stream));
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;  // rebuilt with the new stages on the next run
+    }
+    h->timestepping_method = method;
+    return SWGPU_OK;
 }
 
 int swgpu_update_other_quantities(void *handle) {
@@ -956,10 +1005,10 @@ int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms) {
         CK(cudaEventRecord(ev[1], h->stream));
         if (h->precision == SWGPU_FP64)
             launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, kFused | kFrictionInline,
-                               h->stream);
+                               kEulerStage, h->stream);
         else
             launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused | kFrictionInline,
-                                h->stream);
+                                kEulerStage, h->stream);
         CK(cudaEventRecord(ev[2], h->stream));
         if (h->precision == SWGPU_FP64)
             launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,

@@ -211,6 +211,26 @@ __device__ __forceinline__ void commit_step(Ctrl *c, const StepClock &s, const D
     if (reason != kStopNone) c->halt_pending = reason;
 }
 
+// Last block of the update kernel in a fused step, per stage kind.  The
+// first Runge-Kutta stage records the step's clock (the distribute that
+// follows reads the order) and moves time to t0 + dt, the middle RK3 stage
+// to t0 + dt/2; the last stage commits the step from t0 as an Euler step
+// does (time = t0 + dt, the evolve loop's set_time(initial_time + timestep)).
+__device__ __forceinline__ void commit_stage(Ctrl *c, const StepClock &s, const DevParams &P,
+                                             const Stage &stg) {
+    if (stg.kind == kStageFirst) {
+        c->step_t0 = c->time;
+        c->order = s.order;
+        c->smallsteps = s.smallsteps;
+        c->time = c->time + s.dt;
+    } else if (stg.kind == kStageMid) {
+        c->time = c->step_t0 + s.dt * stg.tfrac;
+    } else {
+        if (stg.kind == kStageLast) c->time = c->step_t0;
+        commit_step(c, s, P);
+    }
+}
+
 // Last block of the distribute kernel: a pending stop takes effect.
 __device__ __forceinline__ void apply_pending_halt(Ctrl *c) {
     if (c->halt_pending) {

@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(kBlock) flux_fp64(DevMesh M, DevState S, DevPa
         if (flags & kWriteMaxSpeed) S.max_speed[k] = ms_own;
     }
     if (bad) set_status(ctrl, SWGPU_EBED);
+    if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
     block_min_timestep(t, ctrl);
     if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
         publish_step_clock(ctrl, P);
@@ -366,7 +367,8 @@ __device__ __forceinline__ bool semi_update(double &c, double e, double semi, do
 // extrapolation reads.  API: dt given, semi-implicit terms from
 // compute_forcing_terms, no protect.
 __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, DevParams P,
-                                                      Ctrl *ctrl, double dt_api, int flags) {
+                                                      Ctrl *ctrl, double dt_api, int flags,
+                                                      Stage stg) {
     const bool fused = flags & kFused;
     if (fused && ctrl_halted(ctrl)) return;
     StepClock clk;
@@ -380,6 +382,11 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
     int bad = 0, nonfinite = 0;
     if (k < M.N) {
         double w = S.w[k], uh = S.uh[k], vh = S.vh[k];
+        if (stg.kind == kStageFirst) {  // backup_conserved_quantities
+            S.bw[k] = w;
+            S.buh[k] = uh;
+            S.bvh[k] = vh;
+        }
         double su, sv;
         bool applied;
         if (flags & kFrictionInline) {
@@ -402,6 +409,12 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
             uh += dt * S.euh[k];
             vh += dt * S.evh[k];
         }
+        if (stg.kind == kStageMid || stg.kind == kStageLast) {
+            // saxpy_conserved_quantities (quantity.c:749-765)
+            w = stg.a * w + stg.b * S.bw[k];
+            uh = stg.a * uh + stg.b * S.buh[k];
+            vh = stg.a * vh + stg.b * S.bvh[k];
+        }
         if (fused) {
             const double zc = S.zc[k];
             protect_one(P, zc, w, uh, vh);
@@ -422,8 +435,24 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (fused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update)) commit_step(ctrl, clk, P);
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update))
+            commit_stage(ctrl, clk, P, stg);
     }
+}
+
+// saxpy_conserved_quantities (src/anuga_cuda/saxpy_centroid_values/
+// saxpy_centroid_values.cu:1-12, src/anuga_HMPP/quantity.c:749-765) on the
+// three conserved quantities: Q = a*Q + b*backup, products then sum, no
+// contraction (this unit is built with --fmad=false).
+__global__ void __launch_bounds__(kBlock) saxpy_fp64(int N, double a, double b, double *w,
+                                                     double *uh, double *vh,
+                                                     const double *bw, const double *buh,
+                                                     const double *bvh) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    w[k] = a * w[k] + b * bw[k];
+    uh[k] = a * uh[k] + b * buh[k];
+    vh[k] = a * vh[k] + b * bvh[k];
 }
 
 // protect plus the centroid velocities: the head of a stand-alone
@@ -875,8 +904,13 @@ void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P
     forcing_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P);
 }
 void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P, Ctrl *ctrl,
-                        double dt, int flags, cudaStream_t st) {
-    update_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P, ctrl, dt, flags);
+                        double dt, int flags, const Stage &stage, cudaStream_t st) {
+    update_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P, ctrl, dt, flags, stage);
+}
+void launch_saxpy_fp64(const DevMesh &M, const DevState &S, double a, double b,
+                       cudaStream_t st) {
+    saxpy_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M.N, a, b, S.w, S.uh, S.vh, S.bw, S.buh,
+                                                 S.bvh);
 }
 void launch_interpolate_fp64(const DevMesh &M, const DevState &S, cudaStream_t st) {
     interpolate_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S);

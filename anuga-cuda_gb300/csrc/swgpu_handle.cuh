@@ -15,6 +15,7 @@ constexpr int kStepsPerGraph = 16;
 struct Handle {
     int device = 0;
     int precision = SWGPU_FP64;
+    int timestepping_method = SWGPU_EULER;
     cudaStream_t stream = nullptr;
     DevMesh M{};
     DevState S{};

@@ -52,6 +52,9 @@ struct DevState {
     double *hc, *uc, *vc;                     // [N] derived centroid quantities
     double *hb, *ub, *vb;                     // [Nb] derived boundary quantities
     double *partials;                         // [grid] reduction scratch
+    double *bw, *buh, *bvh;                   // [N] backups of the conserved state for
+                                              // Runge-Kutta steps (bw: stage in FP64,
+                                              // depth in the mixed precision)
 };
 
 // Mixed-precision state.  The conserved state is FP64 depth h = w - z (so
@@ -119,6 +122,7 @@ struct __align__(16) Ctrl {
     int clk_small_error;            // the step's update_timestep, evaluated once by
     double clk_dt, clk_ftmin;       // the last block of the flux kernel and read
     long long clk_order, clk_smallsteps;  // by the update kernel
+    double step_t0;                 // time at the start of a Runge-Kutta step
 };
 
 enum StopReason { kStopNone = 0, kStopYield = 1, kStopFinal = 2, kStopBudget = 3, kStopError = 4 };
@@ -130,7 +134,24 @@ enum : int {
     kWriteBoundary = 4,   // distribute evaluates boundary conditions
     kFrictionInline = 8,  // update computes Manning friction itself
     kWriteMaxSpeed = 16,  // flux writes max_speed
+    kNoTimestep = 32,     // flux skips the timestep reduction (later Runge-Kutta stages)
 };
+
+// One stage of a fused step.  An Euler step is one stage; ANUGA's RK2 and
+// RK3 steps (Generic_Domain.evolve_one_rk2_step / evolve_one_rk3_step) are
+// two and three Euler stages that all use the dt chosen by the first, with
+// Q = a*Q + b*backup after the later ones.
+enum StageKind : int {
+    kStageEuler = 0,  // the whole step: commit it
+    kStageFirst = 1,  // back up Q before the update; then time = t0 + dt
+    kStageMid = 2,    // Q = a*Q + b*backup; then time = t0 + tfrac*dt
+    kStageLast = 3,   // Q = a*Q + b*backup; commit the step (time = t0 + dt)
+};
+struct Stage {
+    int kind;
+    double a, b, tfrac;
+};
+constexpr Stage kEulerStage = {kStageEuler, 1.0, 0.0, 1.0};
 
 __host__ __device__ inline double pos_inf() { return 1.0e300 * 1.0e300; }
 
@@ -147,7 +168,11 @@ void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
 void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                          cudaStream_t st);
 void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
-                        Ctrl *ctrl, double dt, int flags, cudaStream_t st);
+                        Ctrl *ctrl, double dt, int flags, const Stage &stage,
+                        cudaStream_t st);
+// saxpy_conserved_quantities: Q = a*Q + b*backup for stage and momenta
+void launch_saxpy_fp64(const DevMesh &M, const DevState &S, double a, double b,
+                       cudaStream_t st);
 void launch_interpolate_fp64(const DevMesh &M, const DevState &S, cudaStream_t st);
 void launch_other_quantities(const DevMesh &M, const DevState &S, cudaStream_t st);
 void launch_mass(const DevMesh &M, const DevState &S, double *out, cudaStream_t st);
@@ -159,7 +184,8 @@ void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed
 void launch_flux_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                        const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st);
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
-                         const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st);
+                         const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,
+                         cudaStream_t st);
 // stand-alone distribute head: (optionally) depth from the FP64 stage, then
 // protect and the FP32 centroid copies
 void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,

@@ -328,6 +328,7 @@ __global__ void __launch_bounds__(kFluxTile) flux_mixed(DevMesh M, DevMixed X, D
         X.euh[k] = (a1 - ghc * gx) * inv_area;
         X.evh[k] = (a2 - ghc * gy) * inv_area;
     }
+    if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
     block_min_timestep_f<kFluxTile>(t, ctrl);
     if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
         publish_step_clock(ctrl, P);
@@ -374,7 +375,8 @@ __device__ __forceinline__ void finish_state(const DevParams &P, double &h, doub
 // Update: h += dt*E_h;  q += q*(r - 1) + dt*E_q*r  with r = 1/(1 - dt*S) the
 // semi-implicit Manning factor.  Increments in FP32, additions in FP64.
 __global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S, DevMixed X,
-                                                       DevParams P, Ctrl *ctrl, int flags) {
+                                                       DevParams P, Ctrl *ctrl, int flags,
+                                                       Stage stg) {
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     const StepClock clk = published_step_clock(ctrl);
     const float dtf = (float)clk.dt;
@@ -382,6 +384,11 @@ __global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S,
     int bad = 0, nonfinite = 0;
     if (k < M.N) {
         double h = X.hd[k], uh = S.uh[k], vh = S.vh[k];
+        if (stg.kind == kStageFirst) {  // backup_conserved_quantities (depth, momenta)
+            S.bw[k] = h;
+            S.buh[k] = uh;
+            S.bvh[k] = vh;
+        }
         const float mah = P.f_mah;
         const float hf0 = ro(X.hf + k);  // FP32 copies of the pre-update state
         const float uf = ro(X.uvel + k) * omaxf(hf0, mah);
@@ -403,6 +410,13 @@ __global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S,
         h += widen(dtf * ro(X.ew + k));
         uh += widen(uf * rm1 + dtf * ro(X.euh + k) * r);
         vh += widen(vf * rm1 + dtf * ro(X.evh + k) * r);
+        if (stg.kind == kStageMid || stg.kind == kStageLast) {
+            // saxpy_conserved_quantities in FP64 on depth: with a + b = 1 it
+            // is the stage saxpy minus the (unchanged) bed
+            h = stg.a * h + stg.b * S.bw[k];
+            uh = stg.a * uh + stg.b * S.buh[k];
+            vh = stg.a * vh + stg.b * S.bvh[k];
+        }
         float hf, wf, wl, uv, vv;
         finish_state(P, h, uh, vh, ro(S.zc + k), hf, wf, wl, uv, vv, nonfinite);
         X.hd[k] = h;
@@ -418,9 +432,11 @@ __global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S,
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (flags & kFused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update)) commit_step(ctrl, clk, P);
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update))
+            commit_stage(ctrl, clk, P, stg);
     }
 }
+
 
 __device__ __forceinline__ void qminmax_f(float dq0, float dq1, float dq2, float &qmin,
                                           float &qmax) {
@@ -778,8 +794,9 @@ void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, co
     flux_mixed<<<(M.N + kFluxTile - 1) / kFluxTile, kFluxTile, 0, st>>>(M, X, P, ctrl, flags);
 }
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
-                         const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st) {
-    update_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, S, X, P, ctrl, flags);
+                         const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,
+                         cudaStream_t st) {
+    update_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, S, X, P, ctrl, flags, stage);
 }
 void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                           const DevParams &P, int from_stage, cudaStream_t st) {

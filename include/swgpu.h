@@ -54,6 +54,13 @@ enum swgpu_precision {
                          at wet/dry fronts, mass and model time             */
 };
 
+/* ---- timestepping methods (Domain.set_timestepping_method) ----------- */
+enum swgpu_timestepping {
+    SWGPU_EULER = 1,  /* forward Euler (the default)                       */
+    SWGPU_RK2 = 2,    /* two-stage Runge-Kutta, Q = Q/2 + E(E(Q))/2         */
+    SWGPU_RK3 = 3     /* three-stage strong-stability-preserving RK         */
+};
+
 /* ---- quantity ids (Domain.quantities keys) --------------------------- */
 enum swgpu_quantity {
     SWGPU_STAGE = 0,
@@ -216,6 +223,22 @@ int swgpu_update_conserved_quantities(void *handle, double timestep);
 
 /* update_other_quantities (:2114-2151) materialised for download. */
 int swgpu_update_other_quantities(void *handle);
+
+/* backup_conserved_quantities (:1449-1478): device copies of the centroid
+ * stage, xmomentum and ymomentum (FP64 handles). */
+int swgpu_backup_conserved_quantities(void *handle);
+
+/* saxpy_conserved_quantities (:1484-1519; kernel
+ * saxpy_centroid_values/saxpy_centroid_values.cu:1-12):
+ * Q = a*Q + b*backup for the three conserved quantities (FP64 handles). */
+int swgpu_saxpy_conserved_quantities(void *handle, double a, double b);
+
+/* Domain.set_timestepping_method (numbered as src/utilities/utility.py:
+ * 256-261): the steps of swgpu_evolve_run / swgpu_evolve_one_step become
+ * ANUGA's evolve_one_euler_step, evolve_one_rk2_step or evolve_one_rk3_step
+ * (dispatched at gpu_domain_advanced.py:2566-2573), every stage of an RK step
+ * with the timestep chosen by its first. */
+int swgpu_set_timestepping_method(void *handle, int method);
 
 /* Total water volume sum(area*(stage-elevation)) (FP64 reduction). */
 int swgpu_mass(void *handle, double *mass);

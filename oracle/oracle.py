@@ -88,6 +88,9 @@ _QNAMES = [
 ]
 
 
+_BACKUPS = ["stage_centroid_backup", "xmom_centroid_backup", "ymom_centroid_backup"]
+
+
 class OrcDomain(C.Structure):
     _fields_ = (
         [("params", C.POINTER(OrcParams)), ("number_of_elements", C.c_long),
@@ -104,6 +107,8 @@ class OrcDomain(C.Structure):
                                      "flux_timestep", "recorded_max_timestep",
                                      "recorded_min_timestep"]]
         + [(n, C.c_long) for n in ["order", "smallsteps", "number_of_steps", "status"]]
+        + [("timestepping_method", C.c_long)]
+        + [(n, _d) for n in _BACKUPS]
     )
 
 
@@ -131,6 +136,13 @@ def swcpu():
         L.swcpu_update_timestep.restype = None
         L.swcpu_evolve_one_euler_step.argtypes = [P, C.c_double]
         L.swcpu_evolve_one_euler_step.restype = C.c_int
+        for name in ["swcpu_evolve_one_rk2_step", "swcpu_evolve_one_rk3_step"]:
+            getattr(L, name).argtypes = [P, C.c_double]
+            getattr(L, name).restype = C.c_int
+        L.swcpu_backup_conserved_quantities.argtypes = [P]
+        L.swcpu_backup_conserved_quantities.restype = None
+        L.swcpu_saxpy_conserved_quantities.argtypes = [P, C.c_double, C.c_double]
+        L.swcpu_saxpy_conserved_quantities.restype = None
         L.swcpu_evolve_start.argtypes = [P, C.c_double]
         L.swcpu_evolve_start.restype = None
         L.swcpu_evolve_steps.argtypes = [P, C.c_double, C.c_double, C.c_long, C.c_double]
@@ -176,6 +188,8 @@ class OracleDomain:
         self.arrays["work_flags"] = np.zeros(3 * N, np.uint8)
         self.arrays["work_a"] = np.zeros(N)
         self.arrays["work_b"] = np.zeros(N)
+        for n in _BACKUPS:
+            self.arrays[n] = np.zeros(N)
         ntag = max(int(mesh.boundary_tag.max()) + 1 if Nb else 1, len(tags or []), 1)
         self._tags = (OrcTag * ntag)()
         for i, (t, p) in enumerate(tags or []):
@@ -195,6 +209,7 @@ class OracleDomain:
                 setattr(D, n, a.ctypes.data_as(_d))
         D.tags = self._tags
         D.order = params.default_order
+        D.timestepping_method = 1
         D.recorded_min_timestep = params.evolve_max_timestep
         D.recorded_max_timestep = params.evolve_min_timestep
         self.D = D
@@ -275,6 +290,23 @@ class OracleDomain:
 
     def evolve_one_euler_step(self, finaltime=-1.0):
         return self.L.swcpu_evolve_one_euler_step(self._ref(), finaltime)
+
+    _METHODS = {"euler": 1, "rk2": 2, "rk3": 3}
+
+    def set_timestepping_method(self, method):
+        self.D.timestepping_method = self._METHODS[method]
+
+    def backup_conserved_quantities(self):
+        self.L.swcpu_backup_conserved_quantities(self._ref())
+
+    def saxpy_conserved_quantities(self, a, b):
+        self.L.swcpu_saxpy_conserved_quantities(self._ref(), a, b)
+
+    def evolve_one_rk2_step(self, finaltime=-1.0):
+        return self.L.swcpu_evolve_one_rk2_step(self._ref(), finaltime)
+
+    def evolve_one_rk3_step(self, finaltime=-1.0):
+        return self.L.swcpu_evolve_one_rk3_step(self._ref(), finaltime)
 
     def evolve_start(self, yieldstep, starttime=0.0):
         self.D.starttime = starttime
@@ -525,6 +557,14 @@ class ReferenceKernels:
                                  self._ptr(A[q + "_explicit_update"]),
                                  self._ptr(A[q + "_semi_implicit_update"]))
         return rc
+
+    def saxpy_conserved_quantities(self, od: OracleDomain, a: float, b: float) -> None:
+        """_saxpy_centroid_values (src/anuga_HMPP/quantity.c:749) on the three
+        conserved quantities and their backups."""
+        A = od.arrays
+        for q in ["stage", "xmom", "ymom"]:
+            self.q._saxpy_centroid_values(od.N, a, b, self._ptr(A[q + "_centroid_values"]),
+                                          self._ptr(A[q + "_centroid_backup"]))
 
     def interpolate_to_edges(self, od: OracleDomain) -> None:
         A = od.arrays

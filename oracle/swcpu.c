@@ -819,6 +819,93 @@ int swcpu_evolve_one_euler_step(swcpu_domain *D, double finaltime)
     return D->status;
 }
 
+/* src/anuga_cuda/gpu_domain_advanced.py:1449-1478 (backup_conserved_quantities):
+ * centroid copies of stage, xmomentum and ymomentum. */
+void swcpu_backup_conserved_quantities(swcpu_domain *D)
+{
+    long k;
+    for (k = 0; k < D->number_of_elements; k++) {
+        D->stage_centroid_backup[k] = D->stage_centroid_values[k];
+        D->xmom_centroid_backup[k] = D->xmom_centroid_values[k];
+        D->ymom_centroid_backup[k] = D->ymom_centroid_values[k];
+    }
+}
+
+/* src/anuga_HMPP/quantity.c:749-765 (_saxpy_centroid_values), applied to the
+ * three conserved quantities (gpu_domain_advanced.py:1484-1519):
+ * Q = a*Q + b*backup, two products and one sum, no contraction. */
+void swcpu_saxpy_conserved_quantities(swcpu_domain *D, double a, double b)
+{
+    double *q[3] = {D->stage_centroid_values, D->xmom_centroid_values,
+                    D->ymom_centroid_values};
+    const double *qb[3] = {D->stage_centroid_backup, D->xmom_centroid_backup,
+                           D->ymom_centroid_backup};
+    long k;
+    int i;
+    for (i = 0; i < 3; i++)
+        for (k = 0; k < D->number_of_elements; k++)
+            q[i][k] = a * q[i][k] + b * qb[i][k];
+}
+
+/* One forward-Euler stage with the step's timestep already chosen: fluxes,
+ * forcing (gravity_wb and Manning friction), conserved update. */
+static int rk_stage(swcpu_domain *D)
+{
+    swcpu_compute_fluxes(D);
+    swcpu_gravity_wb(D);
+    swcpu_manning_friction(D);
+    swcpu_update_conserved_quantities(D, D->timestep);
+    return (int)D->status;
+}
+
+/* ANUGA Generic_Domain.evolve_one_rk2_step (anuga_core generic_domain.py;
+ * ANUGA is a dependency that the reference does not vendor, called at
+ * src/anuga_cuda/gpu_domain_advanced.py:2198-2204 and :2569-2570):
+ *   Q^{n+1} = 1/2 Q^n + 1/2 E(h)^2 Q^n
+ * backup; Euler stage with update_timestep; time += dt; distribute and
+ * boundaries; second Euler stage with the same dt; saxpy(1/2, 1/2).  The
+ * evolve loop then sets time = t0 + dt and distributes. */
+int swcpu_evolve_one_rk2_step(swcpu_domain *D, double finaltime)
+{
+    swcpu_backup_conserved_quantities(D);
+    if (swcpu_evolve_one_euler_step(D, finaltime))
+        return (int)D->status;
+    D->time = D->time + D->timestep;
+    swcpu_distribute_to_vertices_and_edges(D);
+    swcpu_update_boundary(D);
+    if (rk_stage(D))
+        return (int)D->status;
+    swcpu_saxpy_conserved_quantities(D, 0.5, 0.5);
+    return (int)D->status;
+}
+
+/* ANUGA Generic_Domain.evolve_one_rk3_step (same dependency; called at
+ * src/anuga_cuda/gpu_domain_advanced.py:2248-2254 and :2572-2573), the
+ * three-stage strong-stability-preserving scheme:
+ *   Q1 = E(h) Q^n;  Q2 = 3/4 Q^n + 1/4 E(h) Q1 at t0 + h/2;
+ *   Q^{n+1} = 1/3 Q^n + 2/3 E(h) Q2,
+ * every stage with the dt chosen by the first. */
+int swcpu_evolve_one_rk3_step(swcpu_domain *D, double finaltime)
+{
+    const double t0 = D->time;
+    swcpu_backup_conserved_quantities(D);
+    if (swcpu_evolve_one_euler_step(D, finaltime))
+        return (int)D->status;
+    D->time = D->time + D->timestep;
+    swcpu_distribute_to_vertices_and_edges(D);
+    swcpu_update_boundary(D);
+    if (rk_stage(D))
+        return (int)D->status;
+    swcpu_saxpy_conserved_quantities(D, 0.25, 0.75);
+    D->time = t0 + D->timestep * 0.5;
+    swcpu_distribute_to_vertices_and_edges(D);
+    swcpu_update_boundary(D);
+    if (rk_stage(D))
+        return (int)D->status;
+    swcpu_saxpy_conserved_quantities(D, 2.0 / 3.0, 1.0 / 3.0);
+    return (int)D->status;
+}
+
 /* The set-up half of src/anuga_cuda/gpu_domain_advanced.py:2476-2551:
  * distribute, reset time and counters, distribute again, boundaries. */
 void swcpu_evolve_start(swcpu_domain *D, double yieldstep)
@@ -845,7 +932,12 @@ int swcpu_evolve_steps(swcpu_domain *D, double yieldstep, double finaltime,
     long s;
     for (s = 0; s < max_steps; s++) {
         const double t0 = D->time;
-        swcpu_evolve_one_euler_step(D, finaltime);
+        if (D->timestepping_method == 2)
+            swcpu_evolve_one_rk2_step(D, finaltime);
+        else if (D->timestepping_method == 3)
+            swcpu_evolve_one_rk3_step(D, finaltime);
+        else
+            swcpu_evolve_one_euler_step(D, finaltime);
         if (D->status)
             return -1;
         D->time = t0 + D->timestep;

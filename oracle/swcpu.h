@@ -90,6 +90,12 @@ typedef struct {
     double recorded_max_timestep, recorded_min_timestep;
     long order, smallsteps, number_of_steps;
     long status;
+
+    /* Runge-Kutta stepping: 1 euler, 2 rk2, 3 rk3, and the centroid
+     * backups of the conserved quantities (N doubles each; only read and
+     * written when timestepping_method > 1 or by the backup call) */
+    long timestepping_method;
+    double *stage_centroid_backup, *xmom_centroid_backup, *ymom_centroid_backup;
 } swcpu_domain;
 
 double swcpu_compute_fluxes(swcpu_domain *D);
@@ -105,6 +111,10 @@ void swcpu_distribute_to_vertices_and_edges(swcpu_domain *D);
 void swcpu_update_boundary(swcpu_domain *D);
 void swcpu_update_timestep(swcpu_domain *D, double finaltime);
 int swcpu_evolve_one_euler_step(swcpu_domain *D, double finaltime);
+void swcpu_backup_conserved_quantities(swcpu_domain *D);
+void swcpu_saxpy_conserved_quantities(swcpu_domain *D, double a, double b);
+int swcpu_evolve_one_rk2_step(swcpu_domain *D, double finaltime);
+int swcpu_evolve_one_rk3_step(swcpu_domain *D, double finaltime);
 void swcpu_evolve_start(swcpu_domain *D, double yieldstep);
 int swcpu_evolve_steps(swcpu_domain *D, double yieldstep, double finaltime,
                        long max_steps, double time_epsilon);

@@ -13,7 +13,9 @@ extrapolation, balance, vertex-to-edge interpolation, central-upwind fluxes,
 gravity_wb, Manning friction, the semi-implicit update) and the conserved
 state and timestep after each of ``STEPS`` Euler steps driven by those
 kernels in the reference's call order (src/anuga_cuda/
-gpu_domain_advanced.py:2476-2675).  The time-step rule and the boundary
+gpu_domain_advanced.py:2476-2675), and the same after each of ``RK_STEPS``
+RK2 and RK3 steps (ANUGA's evolve_one_rk2_step / evolve_one_rk3_step driving
+the reference's kernels and its _saxpy_centroid_values).  The time-step rule and the boundary
 conditions have no C-callable counterpart in the reference and come from the
 oracle's restatement (src/anuga_HMPP/evolve.c:115-160,
 src/anuga_cuda/evaluate_segment/evaluate_segment.cu:3-115).
@@ -32,6 +34,8 @@ from oracle import oracle as O  # noqa: E402
 HERE = os.path.dirname(os.path.abspath(__file__))
 STEPS = 40
 SAVED_STEPS = (0, 1, 4, 19, 39)   # conserved state stored after these steps
+RK_STEPS = 12                      # Runge-Kutta runs (rk2, rk3)
+RK_SAVED_STEPS = (0, 3, 11)
 MESH_KEYS = ["neighbours", "neighbour_edges", "surrogate_neighbours", "number_of_boundaries",
              "tri_full_flag", "normals", "edgelengths", "radii", "areas", "vertex_coordinates",
              "centroid_coordinates", "boundary_cells", "boundary_edges", "boundary_tag"]
@@ -113,6 +117,56 @@ def ref_step(R, od, finaltime=-1.0):
     od.update_boundary()
 
 
+def ref_distribute(R, od):
+    R.protect(od)
+    if od.D.order == 1:
+        od.extrapolate_first_order()
+    else:
+        R.extrapolate_second_order_sw(od)
+    R.balance_deep_and_shallow(od)
+    R.interpolate_to_edges(od)
+    od.update_boundary()
+
+
+def ref_stage(R, od):
+    """A Runge-Kutta stage after the first: the step's dt is kept."""
+    R.compute_fluxes(od)
+    R.gravity_wb(od)
+    R.manning_friction(od)
+    assert R.update(od, od.D.timestep) == 0
+
+
+def ref_rk_step(R, od, method, finaltime=-1.0):
+    """ANUGA's evolve_one_rk2_step / evolve_one_rk3_step (restated driver)
+    on the reference's kernels, backup as a copy (the reference's
+    backup_conserved_quantities is a device memcpy) and the reference's
+    _saxpy_centroid_values, then the evolve loop's time update and
+    distribute."""
+    D = od.D
+    t0 = D.time
+    for q in ("stage", "xmom", "ymom"):
+        od.arrays[q + "_centroid_backup"][:] = od.arrays[q + "_centroid_values"]
+    ft = R.compute_fluxes(od)
+    R.gravity_wb(od)
+    R.manning_friction(od)
+    D.flux_timestep = ft
+    od.update_timestep(finaltime)
+    assert R.update(od, D.timestep) == 0
+    D.time = D.time + D.timestep
+    ref_distribute(R, od)
+    ref_stage(R, od)
+    if method == "rk2":
+        R.saxpy_conserved_quantities(od, 0.5, 0.5)
+    else:
+        R.saxpy_conserved_quantities(od, 0.25, 0.75)
+        D.time = t0 + D.timestep * 0.5
+        ref_distribute(R, od)
+        ref_stage(R, od)
+        R.saxpy_conserved_quantities(od, 2.0 / 3.0, 1.0 / 3.0)
+    D.time = t0 + D.timestep
+    ref_distribute(R, od)
+
+
 def make(name, sc, params):
     R = O.ReferenceKernels()
     od = O.OracleDomain(sc.mesh, params, sc.oracle_tags())
@@ -169,6 +223,20 @@ def make(name, sc, params):
     for q in ("stage", "xmom", "ymom"):
         out[f"run/final/{q}_vertex"] = od.arrays[q + "_vertex_values"].copy()
     out["run/final/mass"] = np.array([od.mass()])
+
+    # fresh runs of RK_STEPS Runge-Kutta steps
+    for method in ("rk2", "rk3"):
+        od = O.OracleDomain(sc.mesh, params, sc.oracle_tags())
+        sc.apply_to_oracle(od)
+        od.evolve_start(1.0e300)
+        D = od.D
+        for s in range(RK_STEPS):
+            ref_rk_step(R, od, method)
+            out[f"{method}/{s}/dt"] = np.array([D.timestep])
+            out[f"{method}/{s}/time"] = np.array([D.time])
+            if s in RK_SAVED_STEPS:
+                for q in ("stage", "xmom", "ymom"):
+                    out[f"{method}/{s}/{q}"] = od.arrays[q + "_centroid_values"].copy()
     out["params"] = np.array(params.as_tuple(), dtype=np.float64)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     print(f"{name}: N={sc.mesh.number_of_elements} final time {D.time:.6f} "

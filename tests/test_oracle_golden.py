@@ -1,6 +1,6 @@
 """The CPU oracle against the golden fixtures made by the reference's own
 ANUGA C kernels (tests/golden/make_golden.py): bit for bit, kernel by kernel
-and over 40 Euler steps.  Runs everywhere (no reference sources needed)."""
+over 40 Euler steps and over 12 RK2 and RK3 steps.  Runs everywhere (no reference sources needed)."""
 import numpy as np
 import pytest
 
@@ -59,6 +59,37 @@ def test_evolve_matches_reference_bitwise(case, oracle_mod):
     for q in ("stage", "xmom", "ymom"):
         assert bits_equal(od.arrays[q + "_vertex_values"], g[f"run/final/{q}_vertex"]), q
     assert bits_equal([od.mass()], g["run/final/mass"])
+
+
+RK_STEPS = 12
+
+
+@pytest.mark.parametrize("method", ["rk2", "rk3"])
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_runge_kutta_matches_reference_bitwise(case, method, oracle_mod):
+    """RK2 / RK3 steps: the oracle's driver and saxpy against the golden run
+    made from the reference's kernels and its _saxpy_centroid_values."""
+    g = load_golden(case)
+    od = golden_oracle(g, oracle_mod)
+    od.set_timestepping_method(method)
+    od.evolve_start(1.0e300)
+    for s in range(RK_STEPS):
+        assert od.evolve_steps(1.0e300, None, 1) == 0
+        assert od.status == 0
+        assert bits_equal([od.D.timestep], g[f"{method}/{s}/dt"]), f"dt at step {s}"
+        assert bits_equal([od.D.time], g[f"{method}/{s}/time"]), f"time at step {s}"
+        if f"{method}/{s}/stage" in g:
+            for q in ("stage", "xmom", "ymom"):
+                assert bits_equal(od.arrays[q + "_centroid_values"], g[f"{method}/{s}/{q}"]), \
+                    (q, s)
+
+
+def test_runge_kutta_differs_from_euler():
+    """The RK fixtures are not the Euler run in disguise."""
+    g = load_golden("basin_wetdry")
+    assert not bits_equal(g["rk2/11/stage"], g["rk3/11/stage"])
+    assert not np.array_equal(g["rk2/0/dt"], g["run/0/dt"]) or \
+        not bits_equal(g["rk2/0/stage"], g["run/0/stage"])
 
 
 def test_golden_cases_cover_wet_dry_and_boundaries():

@@ -83,3 +83,23 @@ def test_harbour_mesh_kernels_bitwise(oracle_mod, ref):
         assert a.update_conserved_quantities(fa) == 0 and ref.update(b, fa) == 0
         for q in ("stage", "xmom", "ymom"):
             assert bits_equal(a.arrays[q + "_centroid_values"], b.arrays[q + "_centroid_values"])
+
+
+@pytest.mark.parametrize("ab", [(0.5, 0.5), (0.25, 0.75), (2.0 / 3.0, 1.0 / 3.0), (-1.5, 3.25)])
+def test_saxpy_bitwise(oracle_mod, ref, ab):
+    """swcpu_saxpy_conserved_quantities against _saxpy_centroid_values
+    (src/anuga_HMPP/quantity.c:749)."""
+    from anuga_cuda import DEFAULT, scenarios
+    sc = scenarios.small_basin(7, 6, seed=5)
+    a, b = _pair(oracle_mod, sc, DEFAULT)
+    rng = np.random.default_rng(9)
+    for od in (a, b):
+        od.backup_conserved_quantities()
+    for q in ("stage", "xmom", "ymom"):
+        v = rng.standard_normal(a.N) * 3.0
+        a.arrays[q + "_centroid_values"][:] = v
+        b.arrays[q + "_centroid_values"][:] = v
+    a.saxpy_conserved_quantities(*ab)
+    ref.saxpy_conserved_quantities(b, *ab)
+    for q in ("stage", "xmom", "ymom"):
+        assert bits_equal(a.arrays[q + "_centroid_values"], b.arrays[q + "_centroid_values"])

@@ -17,6 +17,7 @@ __all__ = [
     "lib", "SwgpuError", "Mesh_t", "Params_t", "State_t", "BoundaryTag_t", "check",
     "STAGE", "XMOMENTUM", "YMOMENTUM", "ELEVATION", "FRICTION", "HEIGHT", "XVELOCITY",
     "YVELOCITY", "FP64", "MIXED", "BC_REFLECTIVE", "BC_DIRICHLET", "BC_TIME_STAGE_SINE",
+    "BC_TRANSMISSIVE", "BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM", "BC_INFLOW_HYDROGRAPH",
     "STOP_NONE", "STOP_YIELD", "STOP_FINAL", "STOP_BUDGET", "STOP_ERROR", "EXPORTED_SYMBOLS",
     "EULER", "RK2", "RK3",
 ]
@@ -25,6 +26,7 @@ STAGE, XMOMENTUM, YMOMENTUM, ELEVATION, FRICTION, HEIGHT, XVELOCITY, YVELOCITY =
 FP64, MIXED = 0, 1
 EULER, RK2, RK3 = 1, 2, 3
 BC_REFLECTIVE, BC_DIRICHLET, BC_TIME_STAGE_SINE = 0, 1, 2
+BC_TRANSMISSIVE, BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM, BC_INFLOW_HYDROGRAPH = 3, 4, 5
 STOP_NONE, STOP_YIELD, STOP_FINAL, STOP_BUDGET, STOP_ERROR = range(5)
 
 STATUS_NAMES = {
@@ -68,7 +70,8 @@ PARAM_FIELDS = [
     ("tight_slope_limiters", C.c_int64), ("use_centroid_velocities", C.c_int64),
     ("optimise_dry_cells", C.c_int64), ("extrapolate_velocity_second_order", C.c_int64),
     ("use_sloped_mannings", C.c_int64), ("max_smallsteps", C.c_int64),
-    ("default_order", C.c_int64),
+    ("default_order", C.c_int64), ("optimised_gradient_limiter", C.c_int64),
+    ("use_edge_limiter", C.c_int64),
 ]
 
 

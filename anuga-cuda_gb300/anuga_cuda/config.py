@@ -35,6 +35,8 @@ class Parameters:
     use_sloped_mannings: int = 0
     max_smallsteps: int = 50
     default_order: int = 2
+    optimised_gradient_limiter: int = 1
+    use_edge_limiter: int = 0
 
     def replace(self, **kw) -> "Parameters":
         return dataclasses.replace(self, **kw)

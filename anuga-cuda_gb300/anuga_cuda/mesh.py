@@ -200,6 +200,13 @@ class Mesh:
     def __len__(self):
         return self.number_of_elements
 
+    def tag_length(self, tag) -> float:
+        """Total length of the boundary edges carrying ``tag``."""
+        t = self.tag_names.index(tag)
+        sel = self.boundary_tag == t
+        L = np.asarray(self.edgelengths).reshape(-1, 3)
+        return float(L[self.boundary_cells[sel], self.boundary_edges[sel]].sum())
+
     def vertex_values(self, f):
         """Evaluate f(x, y) at the three vertices of every triangle, (N,3)."""
         V = self.vertex_coordinates.reshape(-1, 3, 2)

@@ -91,7 +91,7 @@ class Scenario:
         out = []
         for t in self.mesh.tag_names:
             b = self.boundaries.get(t) or Reflective_boundary()
-            out.append((int(b.type), tuple(b.params())))
+            out.append((int(b.type), tuple(b.params(self.mesh, t))))
         return out
 
 
@@ -280,3 +280,28 @@ def small_basin(m=12, n=10, seed=0, wet_dry_front=True):
         xmom_centroid=uh, ymom_centroid=vh, friction=rng.uniform(0.0, 0.05, N),
         boundaries={"inflow": Dirichlet_boundary([0.15, 0.0, 0.0]), "right": Reflective_boundary(),
                     "top": Reflective_boundary(), "bottom": Reflective_boundary()}, steps=50)
+
+
+def channel_inflow(m=14, n=5, seed=0, peak=0.5, rise=2.0):
+    """A sloping rectangular_cross channel fed by a triangular inflow
+    hydrograph on the left, draining through a transmissive boundary on the
+    right, with a transmissive-stage, zero-momentum top and a reflective
+    bottom; dry upstream, a shallow pool downstream."""
+    from .boundaries import (Inflow_hydrograph_boundary, Transmissive_boundary,
+                             Transmissive_stage_zero_momentum_boundary)
+    rng = np.random.default_rng(seed)
+    pts, tris, bnd = rectangular_cross(m, n, float(m), float(n))
+    mesh = Mesh(pts, tris, bnd)
+    V = mesh.vertex_coordinates.reshape(-1, 3, 2)
+    z = 0.4 - 0.05 * V[..., 0] + 0.02 * np.cos(1.3 * V[..., 1]) * np.sin(0.7 * V[..., 0])
+    zc = z.mean(axis=1)
+    N = mesh.number_of_elements
+    w = np.maximum(zc, 0.05 + 0.01 * rng.standard_normal(N))
+    return Scenario(
+        name=f"channel_inflow_{m}x{n}", mesh=mesh, elevation_vertex=z, stage_centroid=w,
+        xmom_centroid=np.zeros(N), ymom_centroid=np.zeros(N),
+        friction=rng.uniform(0.01, 0.04, N),
+        boundaries={"left": Inflow_hydrograph_boundary(peak=peak, rise=rise),
+                    "right": Transmissive_boundary(),
+                    "top": Transmissive_stage_zero_momentum_boundary(),
+                    "bottom": Reflective_boundary()}, steps=50)

@@ -510,6 +510,9 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
     P.use_sloped_mannings = (int)params->use_sloped_mannings;
     P.max_smallsteps = (int)params->max_smallsteps;
     P.default_order = (int)params->default_order;
+    P.limiter = params->use_edge_limiter ? kLimiterEdge
+                : params->optimised_gradient_limiter ? kLimiterOptimised
+                                                     : kLimiterVertex;
     P.f_g = (float)P.g;
     P.f_eps = (float)P.epsilon;
     P.f_H0 = (float)P.H0;
@@ -527,6 +530,14 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
     P.f_beta_vh_dry = (float)P.beta_vh_dry;
     if (!(P.evolve_max_timestep > 0) || (P.default_order != 1 && P.default_order != 2)) {
         fail(h, SWGPU_EINVAL, "evolve_max_timestep must be > 0 and default_order 1 or 2");
+        g_create_error = h->err;
+        swgpu_destroy(h);
+        return SWGPU_EINVAL;
+    }
+    if (P.limiter != kLimiterOptimised && precision != SWGPU_FP64) {
+        fail(h, SWGPU_EINVAL,
+             "the per-quantity vertex / edge limiters (optimised_gradient_limiter = 0 or "
+             "use_edge_limiter = 1) run in FP64 precision only");
         g_create_error = h->err;
         swgpu_destroy(h);
         return SWGPU_EINVAL;
@@ -584,11 +595,15 @@ int swgpu_set_boundary_tags(void *handle, const swgpu_boundary_tag *tags, int nt
         return fail(h, SWGPU_EINVAL, "mesh uses %d boundary tags, %d given", h->ntags, ntags);
     std::vector<BcTag> t((size_t)ntags);
     for (int i = 0; i < ntags; i++) {
-        if (tags[i].type < SWGPU_BC_REFLECTIVE || tags[i].type > SWGPU_BC_TIME_STAGE_SINE)
+        if (tags[i].type < SWGPU_BC_REFLECTIVE || tags[i].type > SWGPU_BC_INFLOW_HYDROGRAPH)
             return fail(h, SWGPU_EBOUNDARY, "tag %d: unknown boundary type %lld", i,
                         (long long)tags[i].type);
         if (tags[i].type == SWGPU_BC_TIME_STAGE_SINE && !(tags[i].p[2] != 0.0))
             return fail(h, SWGPU_EINVAL, "tag %d: sine boundary needs a nonzero period", i);
+        if (tags[i].type == SWGPU_BC_INFLOW_HYDROGRAPH &&
+            !(tags[i].p[0] >= 0.0 && tags[i].p[1] > 0.0 && tags[i].p[2] > 0.0))
+            return fail(h, SWGPU_EINVAL,
+                        "tag %d: hydrograph needs peak >= 0 and positive rise and fall", i);
         t[i].type = (int)tags[i].type;
         for (int j = 0; j < 4; j++) t[i].p[j] = tags[i].p[j];
     }
@@ -773,7 +788,7 @@ int swgpu_update_boundary(void *handle) {
     if (h->precision == SWGPU_MIXED && !h->mixed_from_stage) {
         launch_vertices_from_mixed(h->M, h->S, h->X, h->stream);
     }
-    launch_boundary_fp64(h->M, h->S, h->d_tags, h->d_ctrl, h->stream);
+    launch_boundary_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl, h->stream);
     int rc = check_launch(h, "update_boundary");
     if (rc) return rc;
     if ((rc = sync_ctrl(h))) return rc;

@@ -19,14 +19,27 @@ __device__ __forceinline__ void set_status(Ctrl *ctrl, int code) {
     atomicCAS(&ctrl->status, 0, code);
 }
 
+// Unit discharge of a triangular hydrograph (peak, rise, fall, start): 0
+// before start, linear to peak over rise, linear back to 0 over fall.
+__device__ __forceinline__ double hydrograph(const double p[4], double t) {
+    const double s = t - p[3];
+    if (s <= 0.0) return 0.0;
+    if (s < p[1]) return p[0] * (s / p[1]);
+    if (s < p[1] + p[2]) return p[0] * (1.0 - (s - p[1]) / p[2]);
+    return 0.0;
+}
+
 // Boundary value of one boundary edge from the owning triangle's edge
 // values (reflective: src/anuga_cuda/evaluate_segment/evaluate_segment.cu:3-76;
-// Dirichlet: :80-115; the time-dependent stage has no reference GPU
-// counterpart).  Returns false for an unknown type.
+// Dirichlet: :80-115; ANUGA's transmissive boundaries: the inside edge
+// values, with or without momentum; the time-dependent stage and the inflow
+// hydrograph have no reference GPU counterpart: the hydrograph's unit
+// discharge q(t) enters along the inward normal at critical depth
+// (q^2/g)^(1/3) above the edge bed ze).  Returns false for an unknown type.
 __device__ __forceinline__ bool eval_boundary(const BcTag &T, double time, double we,
                                               double uhe, double vhe, double n1,
-                                              double n2, double &wb, double &uhb,
-                                              double &vhb) {
+                                              double n2, double ze, double g, double &wb,
+                                              double &uhb, double &vhb) {
     if (T.type == SWGPU_BC_REFLECTIVE) {
         const double r1 = -uhe * n1 - vhe * n2;
         const double r2 = -uhe * n2 + vhe * n1;
@@ -48,7 +61,32 @@ __device__ __forceinline__ bool eval_boundary(const BcTag &T, double time, doubl
         vhb = 0.0;
         return true;
     }
+    if (T.type == SWGPU_BC_TRANSMISSIVE) {
+        wb = we;
+        uhb = uhe;
+        vhb = vhe;
+        return true;
+    }
+    if (T.type == SWGPU_BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM) {
+        wb = we;
+        uhb = 0.0;
+        vhb = 0.0;
+        return true;
+    }
+    if (T.type == SWGPU_BC_INFLOW_HYDROGRAPH) {
+        const double q = hydrograph(T.p, time);
+        wb = ze + cbrt(q * q / g);
+        uhb = -q * n1;
+        vhb = -q * n2;
+        return true;
+    }
     return false;
+}
+
+// Boundary types whose stage is the edge's own (no stage jump across the edge).
+__host__ __device__ inline bool boundary_keeps_edge_stage(int type) {
+    return type == SWGPU_BC_REFLECTIVE || type == SWGPU_BC_TRANSMISSIVE ||
+           type == SWGPU_BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM;
 }
 
 // Snapshot of the time bookkeeping taken at kernel entry.

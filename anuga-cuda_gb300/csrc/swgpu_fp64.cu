@@ -565,6 +565,90 @@ __device__ __forceinline__ void one_nbr_jumps(double qk, double q1, double dx2, 
 // extrapolate_first_order.cu:3-30), balance_deep_and_shallow
 // (shallow_water_ext.c:1462-1636), vertex values stored; optionally the edge
 // values (quantity.c:687-706) and the boundary values of k's boundary edges.
+// Quantity.extrapolate_second_order_and_limit_by_vertex / _by_edge for one
+// quantity q of triangle k, vertex values to out: the centroid gradient from
+// the surrogate neighbours (src/anuga_HMPP/quantity.c:24-95 with the plane
+// gradients of util_ext.h:66-162; no true neighbour leaves it zero),
+// extrapolation to vertices and edge midpoints (quantity.c:130-172), then
+// one limiter phi over the three vertices (:298-361) or the three edges
+// (:363-447) against the min/max of the true neighbours' centroids.
+// Returns false where the surrogate neighbours repeat (the reference's
+// _compute_gradients gives up there).
+__device__ __forceinline__ bool limit_by_neighbours(const DevMesh &M, const double *q, int k,
+                                                    double beta, bool by_edge, double out[3]) {
+    const int N = M.N;
+    const int nbk = M.nb[k];
+    const double qk = q[k];
+    const double x = M.cxy[k], y = M.cxy[N + k];
+    double a = 0.0, b = 0.0;
+    bool ok = true;
+    if (nbk < 2) {
+        const int k0 = M.surr[k], k1 = M.surr[N + k], k2 = M.surr[2 * N + k];
+        if (k0 == k1 || k1 == k2) {
+            ok = false;
+        } else {
+            const double x0 = M.cxy[k0], y0 = M.cxy[N + k0];
+            const double x1 = M.cxy[k1], y1 = M.cxy[N + k1];
+            const double x2 = M.cxy[k2], y2 = M.cxy[N + k2];
+            const double q0 = q[k0], q1 = q[k1], q2 = q[k2];
+            const double det = (y2 - y0) * (x1 - x0) - (y1 - y0) * (x2 - x0);
+            a = (y2 - y0) * (q1 - q0) - (y1 - y0) * (q2 - q0);
+            a /= det;
+            b = (x1 - x0) * (q2 - q0) - (x2 - x0) * (q1 - q0);
+            b /= det;
+        }
+    } else if (nbk == 2) {
+        int k0 = k;
+        for (int i = 0; i < 3 && k0 == k; i++) k0 = M.surr[i * N + k];
+        if (k0 == k) {
+            ok = false;
+        } else {
+            const double xx = x - M.cxy[k0], yy = y - M.cxy[N + k0], qq = qk - q[k0];
+            const double det = xx * xx + yy * yy;
+            a = xx * qq / det;
+            b = yy * qq / det;
+        }
+    }
+    double v[3], e[3], dqa[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+        v[i] = qk + a * (M.vxy[(2 * i) * N + k] - x) + b * (M.vxy[(2 * i + 1) * N + k] - y);
+    e[0] = 0.5 * (v[1] + v[2]);
+    e[1] = 0.5 * (v[2] + v[0]);
+    e[2] = 0.5 * (v[0] + v[1]);
+    double qmin = qk, qmax = qk;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int pk = M.nbr[i * N + k];
+        if (pk >= 0) {
+            const double qn = q[pk >> 2];
+            qmin = omin(qmin, qn);
+            qmax = omax(qmax, qn);
+        }
+    }
+    double phi = 1.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        double r = 1.0;
+        const double dq = (by_edge ? e[i] : v[i]) - qk;
+        dqa[i] = dq;
+        if (dq > 0.0) r = (qmax - qk) / dq;
+        if (dq < 0.0) r = (qmin - qk) / dq;
+        phi = omin(omin(r * beta, 1.0), phi);
+    }
+    if (by_edge) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) e[i] = qk + phi * dqa[i];
+        out[0] = e[1] + e[2] - e[0];
+        out[1] = e[2] + e[0] - e[1];
+        out[2] = e[0] + e[1] - e[2];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; i++) out[i] = qk + phi * dqa[i];
+    }
+    return ok;
+}
+
 __global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S, DevParams P,
                                                           const BcTag *tags, Ctrl *ctrl,
                                                           int flags) {
@@ -588,6 +672,12 @@ __global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S,
                 ou[i] = uk;
                 ov[i] = vk;
             }
+        } else if (P.limiter != kLimiterOptimised) {
+            const bool by_edge = P.limiter == kLimiterEdge;
+            bool ok = limit_by_neighbours(M, S.w, k, P.beta_w, by_edge, ow);
+            ok &= limit_by_neighbours(M, S.uh, k, P.beta_uh, by_edge, ou);
+            ok &= limit_by_neighbours(M, S.vh, k, P.beta_vh, by_edge, ov);
+            if (!ok) no_nbr = 1;
         } else {
             const bool vel = P.extrapolate_velocity_second_order == 1;
             // centroid values being extrapolated (velocity or momentum)
@@ -770,7 +860,8 @@ __global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S,
                     double wb, uhb, vhb;
                     if (!eval_boundary(tags[M.btag[mb]], time, we, uhe, vhe,
                                        M.normals[(2 * i) * N + k],
-                                       M.normals[(2 * i + 1) * N + k], wb, uhb, vhb)) {
+                                       M.normals[(2 * i + 1) * N + k], S.ze[i * N + k], P.g,
+                                       wb, uhb, vhb)) {
                         bad_bc = 1;
                         wb = uhb = vhb = 0.0;
                     }
@@ -792,7 +883,7 @@ __global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S,
 
 // update_boundary as a stand-alone pass over boundary slots, from the
 // stored vertex values (gpu_domain_advanced.py:2006-2108).
-__global__ void __launch_bounds__(kBlock) boundary_fp64(DevMesh M, DevState S,
+__global__ void __launch_bounds__(kBlock) boundary_fp64(DevMesh M, DevState S, double g,
                                                         const BcTag *tags, Ctrl *ctrl) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M.Nb) return;
@@ -804,7 +895,7 @@ __global__ void __launch_bounds__(kBlock) boundary_fp64(DevMesh M, DevState S,
     const double vhe = 0.5 * (S.vhv[a * N + k] + S.vhv[b * N + k]);
     double wb, uhb, vhb;
     if (!eval_boundary(tags[M.btag[m]], ctrl->time, we, uhe, vhe, M.normals[(2 * i) * N + k],
-                       M.normals[(2 * i + 1) * N + k], wb, uhb, vhb)) {
+                       M.normals[(2 * i + 1) * N + k], S.ze[i * N + k], g, wb, uhb, vhb)) {
         set_status(ctrl, SWGPU_EBOUNDARY);
         wb = uhb = vhb = 0.0;
     }
@@ -891,9 +982,10 @@ void launch_distribute_fp64(const DevMesh &M, const DevState &S, const DevParams
                             const BcTag *tags, Ctrl *ctrl, int flags, cudaStream_t st) {
     distribute_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P, tags, ctrl, flags);
 }
-void launch_boundary_fp64(const DevMesh &M, const DevState &S, const BcTag *tags, Ctrl *ctrl,
+void launch_boundary_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                          const BcTag *tags, Ctrl *ctrl,
                           cudaStream_t st) {
-    if (M.Nb > 0) boundary_fp64<<<grid_for(M.Nb), kBlock, 0, st>>>(M, S, tags, ctrl);
+    if (M.Nb > 0) boundary_fp64<<<grid_for(M.Nb), kBlock, 0, st>>>(M, S, P.g, tags, ctrl);
 }
 void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P, Ctrl *ctrl,
                       int flags, cudaStream_t st) {

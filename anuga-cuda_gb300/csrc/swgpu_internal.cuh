@@ -94,6 +94,7 @@ struct DevParams {
     int tight_slope_limiters, use_centroid_velocities, optimise_dry_cells;
     int extrapolate_velocity_second_order, use_sloped_mannings;
     int max_smallsteps, default_order;
+    int limiter;  // kLimiterOptimised, kLimiterVertex or kLimiterEdge
     // FP32 copies for the mixed kernels (set on the host; FP64 arithmetic
     // on GB300 runs at 1/64 of the FP32 rate, so none is done per thread)
     float f_g, f_eps, f_H0, f_h0, f_lim, f_mah, f_mas, f_max_dt, f_alpha;
@@ -153,6 +154,14 @@ struct Stage {
 };
 constexpr Stage kEulerStage = {kStageEuler, 1.0, 0.0, 1.0};
 
+// second-order reconstruction of distribute_to_vertices_and_edges
+// (gpu_domain_advanced.py:1815-1943)
+enum Limiter : int {
+    kLimiterOptimised = 0,  // extrapolate_second_order_sw (optimised_gradient_limiter)
+    kLimiterVertex = 1,     // per quantity, extrapolate_second_order_and_limit_by_vertex
+    kLimiterEdge = 2,       // per quantity, ..._and_limit_by_edge (use_edge_limiter)
+};
+
 __host__ __device__ inline double pos_inf() { return 1.0e300 * 1.0e300; }
 
 // ---------------------------------------------------------------- launches
@@ -161,7 +170,8 @@ void launch_prepare_fp64(const DevMesh &M, const DevState &S, const DevParams &P
                          Ctrl *ctrl, cudaStream_t st);
 void launch_distribute_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                             const BcTag *tags, Ctrl *ctrl, int flags, cudaStream_t st);
-void launch_boundary_fp64(const DevMesh &M, const DevState &S, const BcTag *tags,
+void launch_boundary_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                          const BcTag *tags,
                           Ctrl *ctrl, cudaStream_t st);
 void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                       Ctrl *ctrl, int flags, cudaStream_t st);

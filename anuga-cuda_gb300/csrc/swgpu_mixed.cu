@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
                     double wb, uhb, vhb;
                     if (!eval_boundary(T, time, we, widen(uhe), widen(vhe),
                                        widen(ro(X.nx + i * SP + k)), widen(ro(X.ny + i * SP + k)),
-                                       wb, uhb, vhb)) {
+                                       ze, P.g, wb, uhb, vhb)) {
                         bad_bc = 1;
                         wb = we;
                         uhb = vhb = 0.0;
@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
                     S.uhb[mb] = uhb;
                     S.vhb[mb] = vhb;
                     S.zb[mb] = ze;
-                    if (T.type == SWGPU_BC_REFLECTIVE) {
+                    if (boundary_keeps_edge_stage(T.type)) {
                         // same depth and stage as the edge: exactly no jump
                         X.hbf[mb] = hle;
                         X.wjb[mb] = 0.0f;

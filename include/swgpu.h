@@ -77,8 +77,18 @@ enum swgpu_quantity {
 enum swgpu_boundary_type {
     SWGPU_BC_REFLECTIVE = 0,     /* anuga Reflective_boundary              */
     SWGPU_BC_DIRICHLET = 1,      /* anuga Dirichlet_boundary (w, uh, vh)   */
-    SWGPU_BC_TIME_STAGE_SINE = 2 /* stage = p0 + p1*sin(2*pi*t/p2 + p3),
+    SWGPU_BC_TIME_STAGE_SINE = 2, /* stage = p0 + p1*sin(2*pi*t/p2 + p3),
                                     momentum 0, t = model time             */
+    SWGPU_BC_TRANSMISSIVE = 3,   /* anuga Transmissive_boundary: the inside
+                                    edge's stage and momentum              */
+    SWGPU_BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM = 4, /* anuga
+                                    Transmissive_stage_zero_momentum_boundary */
+    SWGPU_BC_INFLOW_HYDROGRAPH = 5 /* triangular hydrograph of unit discharge
+                                    q(t) (p0 peak in m^2/s, p1 rise, p2 fall,
+                                    p3 start time) entering along the inward
+                                    normal at critical depth (q^2/g)^(1/3)
+                                    above the edge bed; no reference
+                                    counterpart                            */
 };
 
 typedef struct {
@@ -129,6 +139,12 @@ typedef struct {
     int64_t use_sloped_mannings;
     int64_t max_smallsteps;
     int64_t default_order;
+    int64_t optimised_gradient_limiter;  /* nonzero: extrapolate_second_order_sw
+                                            (the default); 0: per-quantity
+                                            limit by vertex (FP64 only) */
+    int64_t use_edge_limiter;            /* nonzero: per-quantity limit by edge
+                                            (FP64 only; gpu_domain_advanced.py:
+                                            1815-1860) */
 } swgpu_params;
 
 /* Evolve state kept on the device (Domain time bookkeeping,

@@ -63,7 +63,8 @@ class OrcParams(C.Structure):
         ("tight_slope_limiters", C.c_long), ("use_centroid_velocities", C.c_long),
         ("optimise_dry_cells", C.c_long), ("extrapolate_velocity_second_order", C.c_long),
         ("use_sloped_mannings", C.c_long), ("max_smallsteps", C.c_long),
-        ("default_order", C.c_long),
+        ("default_order", C.c_long), ("optimised_gradient_limiter", C.c_long),
+        ("use_edge_limiter", C.c_long),
     ]
 
 
@@ -139,6 +140,8 @@ def swcpu():
         for name in ["swcpu_evolve_one_rk2_step", "swcpu_evolve_one_rk3_step"]:
             getattr(L, name).argtypes = [P, C.c_double]
             getattr(L, name).restype = C.c_int
+        L.swcpu_extrapolate_and_limit_by_neighbours.argtypes = [P, C.c_int]
+        L.swcpu_extrapolate_and_limit_by_neighbours.restype = C.c_int
         L.swcpu_backup_conserved_quantities.argtypes = [P]
         L.swcpu_backup_conserved_quantities.restype = None
         L.swcpu_saxpy_conserved_quantities.argtypes = [P, C.c_double, C.c_double]
@@ -271,6 +274,9 @@ class OracleDomain:
 
     def extrapolate_first_order(self):
         self.L.swcpu_extrapolate_first_order(self._ref())
+
+    def extrapolate_and_limit_by_neighbours(self, by_edge):
+        return self.L.swcpu_extrapolate_and_limit_by_neighbours(self._ref(), int(by_edge))
 
     def balance_deep_and_shallow(self):
         self.L.swcpu_balance_deep_and_shallow(self._ref())
@@ -411,6 +417,13 @@ class ReferenceKernels:
         self.q._interpolate_from_vertices_to_edges.restype = C.c_int
         self.q._saxpy_centroid_values.argtypes = [C.c_int, C.c_double, C.c_double, _d, _d]
         self.q._saxpy_centroid_values.restype = C.c_int
+        self.q._compute_gradients.argtypes = [C.c_int, _d, _d, _l, _l, _d, _d]
+        self.q._compute_gradients.restype = C.c_int
+        self.q._extrapolate_from_gradient.argtypes = [C.c_int] + [_d] * 7
+        self.q._extrapolate_from_gradient.restype = C.c_int
+        for name in ("_limit_vertices_by_all_neighbours", "_limit_edges_by_all_neighbours"):
+            getattr(self.q, name).argtypes = [C.c_int, C.c_double, _d, _d, _d, _l, _d, _d]
+            getattr(self.q, name).restype = C.c_int
         # gravity_wb exists in the reference only as a Python-C entry point
         # taking a domain object; the module's numpy C API is set up by its
         # init function.
@@ -565,6 +578,33 @@ class ReferenceKernels:
         for q in ["stage", "xmom", "ymom"]:
             self.q._saxpy_centroid_values(od.N, a, b, self._ptr(A[q + "_centroid_values"]),
                                           self._ptr(A[q + "_centroid_backup"]))
+
+    def limit_by_neighbours(self, od: OracleDomain, by_edge: bool) -> int:
+        """Quantity.extrapolate_second_order_and_limit_by_vertex / _by_edge on
+        stage, xmomentum and ymomentum (betas beta_w, beta_uh, beta_vh):
+        _compute_gradients, _extrapolate_from_gradient and
+        _limit_vertices_by_all_neighbours / _limit_edges_by_all_neighbours
+        (src/anuga_HMPP/quantity.c:24, :130, :298, :363), with each
+        quantity's gradients starting from zero."""
+        A, N, p = od.arrays, od.N, od.params
+        limit = (self.q._limit_edges_by_all_neighbours if by_edge
+                 else self.q._limit_vertices_by_all_neighbours)
+        rc = 0
+        for q, beta in (("stage", p.beta_w), ("xmom", p.beta_uh), ("ymom", p.beta_vh)):
+            gx, gy = np.zeros(N), np.zeros(N)
+            qc, qv, qe = (A[q + s] for s in ("_centroid_values", "_vertex_values",
+                                              "_edge_values"))
+            rc |= self.q._compute_gradients(N, self._ptr(A["centroid_coordinates"]),
+                                            self._ptr(qc), self._ptr(A["number_of_boundaries"]),
+                                            self._ptr(A["surrogate_neighbours"]), self._ptr(gx),
+                                            self._ptr(gy))
+            rc |= self.q._extrapolate_from_gradient(
+                N, self._ptr(A["centroid_coordinates"]), self._ptr(qc),
+                self._ptr(A["vertex_coordinates"]), self._ptr(qv), self._ptr(qe),
+                self._ptr(gx), self._ptr(gy))
+            rc |= limit(N, beta, self._ptr(qc), self._ptr(qv), self._ptr(qe),
+                        self._ptr(A["neighbours"]), self._ptr(gx), self._ptr(gy))
+        return rc
 
     def interpolate_to_edges(self, od: OracleDomain) -> None:
         A = od.arrays

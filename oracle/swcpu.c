@@ -717,13 +717,139 @@ void swcpu_interpolate_to_edges(swcpu_domain *D)
 
 /* src/anuga_cuda/gpu_domain_advanced.py:1884-1986: protect, then first- or
  * second-order extrapolation, balance, and vertex-to-edge interpolation. */
+/* Gradient of the plane through three points, src/anuga_HMPP/util_ext.h:66-108. */
+static void gradient3(double x0, double y0, double x1, double y1, double x2, double y2,
+                      double q0, double q1, double q2, double *a, double *b)
+{
+    const double det = (y2 - y0) * (x1 - x0) - (y1 - y0) * (x2 - x0);
+    *a = (y2 - y0) * (q1 - q0) - (y1 - y0) * (q2 - q0);
+    *a /= det;
+    *b = (x1 - x0) * (q2 - q0) - (x2 - x0) * (q1 - q0);
+    *b /= det;
+}
+
+/* Two-point gradient, constant across the line, util_ext.h:111-162. */
+static void gradient2(double x0, double y0, double x1, double y1, double q0, double q1,
+                      double *a, double *b)
+{
+    const double xx = x1 - x0, yy = y1 - y0, qq = q1 - q0;
+    const double det = xx * xx + yy * yy;
+    *a = xx * qq / det;
+    *b = yy * qq / det;
+}
+
+/* Quantity.extrapolate_second_order_and_limit_by_vertex / _by_edge for one
+ * quantity: _compute_gradients (src/anuga_HMPP/quantity.c:24-95; no true
+ * neighbour leaves the gradient at zero), _extrapolate_from_gradient
+ * (:130-172) and _limit_vertices_by_all_neighbours (:298-361) or
+ * _limit_edges_by_all_neighbours (:363-447).  Writes vertex and edge values.
+ * Returns nonzero where _compute_gradients would stop (repeated surrogate). */
+static int limit_one_quantity(const swcpu_domain *D, const double *qc, double *qv, double *qe,
+                              double beta, int by_edge)
+{
+    const long N = D->number_of_elements;
+    const double *C = D->centroid_coordinates, *X = D->vertex_coordinates;
+    long k;
+    int i, err = 0;
+    for (k = 0; k < N; k++) {
+        const long *s = D->surrogate_neighbours + 3 * k;
+        const long nb = D->number_of_boundaries[k];
+        double a = 0.0, b = 0.0, v[3], e[3], dqa[3], qmin, qmax, phi = 1.0;
+        const double q = qc[k], x = C[2 * k], y = C[2 * k + 1];
+        if (nb < 2) {
+            if (s[0] == s[1] || s[1] == s[2]) {
+                err = 1;
+            } else {
+                gradient3(C[2 * s[0]], C[2 * s[0] + 1], C[2 * s[1]], C[2 * s[1] + 1],
+                          C[2 * s[2]], C[2 * s[2] + 1], qc[s[0]], qc[s[1]], qc[s[2]], &a, &b);
+            }
+        } else if (nb == 2) {
+            long k0 = k;
+            for (i = 0; i < 3 && k0 == k; i++)
+                k0 = s[i];
+            if (k0 == k)
+                err = 1;
+            else
+                gradient2(C[2 * k0], C[2 * k0 + 1], x, y, qc[k0], q, &a, &b);
+        }
+        for (i = 0; i < 3; i++)
+            v[i] = q + a * (X[6 * k + 2 * i] - x) + b * (X[6 * k + 2 * i + 1] - y);
+        e[0] = 0.5 * (v[1] + v[2]);
+        e[1] = 0.5 * (v[2] + v[0]);
+        e[2] = 0.5 * (v[0] + v[1]);
+        qmin = qmax = q;
+        for (i = 0; i < 3; i++) {
+            const long n = D->neighbours[3 * k + i];
+            if (n >= 0) {
+                qmin = omin(qmin, qc[n]);
+                qmax = omax(qmax, qc[n]);
+            }
+        }
+        for (i = 0; i < 3; i++) {
+            double r = 1.0;
+            const double dq = (by_edge ? e[i] : v[i]) - q;
+            dqa[i] = dq;
+            if (dq > 0.0)
+                r = (qmax - q) / dq;
+            if (dq < 0.0)
+                r = (qmin - q) / dq;
+            phi = omin(omin(r * beta, 1.0), phi);
+        }
+        if (by_edge) {
+            for (i = 0; i < 3; i++)
+                e[i] = q + phi * dqa[i];
+            v[0] = e[1] + e[2] - e[0];
+            v[1] = e[2] + e[0] - e[1];
+            v[2] = e[0] + e[1] - e[2];
+        } else {
+            for (i = 0; i < 3; i++)
+                v[i] = q + phi * dqa[i];
+            e[0] = 0.5 * (v[1] + v[2]);
+            e[1] = 0.5 * (v[2] + v[0]);
+            e[2] = 0.5 * (v[0] + v[1]);
+        }
+        for (i = 0; i < 3; i++) {
+            qv[3 * k + i] = v[i];
+            qe[3 * k + i] = e[i];
+        }
+    }
+    return err;
+}
+
+/* The per-quantity limiter branch of distribute_to_vertices_and_edges
+ * (src/anuga_cuda/gpu_domain_advanced.py:1815-1860 by edge, :1918-1943 by
+ * vertex): stage, xmomentum and ymomentum each with its own beta. */
+int swcpu_extrapolate_and_limit_by_neighbours(swcpu_domain *D, int by_edge)
+{
+    const swcpu_params *P = D->params;
+    int err = 0;
+    err |= limit_one_quantity(D, D->stage_centroid_values, D->stage_vertex_values,
+                              D->stage_edge_values, P->beta_w, by_edge);
+    err |= limit_one_quantity(D, D->xmom_centroid_values, D->xmom_vertex_values,
+                              D->xmom_edge_values, P->beta_uh, by_edge);
+    err |= limit_one_quantity(D, D->ymom_centroid_values, D->ymom_vertex_values,
+                              D->ymom_edge_values, P->beta_vh, by_edge);
+    if (err)
+        D->status |= SWCPU_ERR_NO_INTERIOR_NEIGHBOUR;
+    return err;
+}
+
+/* src/anuga_cuda/gpu_domain_advanced.py:1744-2001: protect, then first
+ * order, the per-quantity edge limiter (use_edge_limiter), the optimised
+ * shallow-water extrapolation (optimised_gradient_limiter) or the
+ * per-quantity vertex limiter; then balance and edge interpolation. */
 void swcpu_distribute_to_vertices_and_edges(swcpu_domain *D)
 {
+    const swcpu_params *P = D->params;
     swcpu_protect(D);
     if (D->order == 1)
         swcpu_extrapolate_first_order(D);
-    else
+    else if (P->use_edge_limiter)
+        swcpu_extrapolate_and_limit_by_neighbours(D, 1);
+    else if (P->optimised_gradient_limiter)
         swcpu_extrapolate_second_order_sw(D);
+    else
+        swcpu_extrapolate_and_limit_by_neighbours(D, 0);
     swcpu_balance_deep_and_shallow(D);
     swcpu_interpolate_to_edges(D);
 }
@@ -739,6 +865,21 @@ void swcpu_distribute_to_vertices_and_edges(swcpu_domain *D)
  * for any other boundary type, gpu_domain_advanced.py:2099-2100):
  * stage = mean + amplitude*sin(2*pi*t/period + phase), momentum 0, evaluated
  * at the model time when update_boundary runs. */
+/* Unit discharge of a triangular hydrograph with parameters (peak, rise,
+ * fall, start): 0 before start, linear to peak over rise, linear to 0 over
+ * fall, then 0. */
+double swcpu_hydrograph(const double p[4], double t)
+{
+    const double s = t - p[3];
+    if (s <= 0.0)
+        return 0.0;
+    if (s < p[1])
+        return p[0] * (s / p[1]);
+    if (s < p[1] + p[2])
+        return p[0] * (1.0 - (s - p[1]) / p[2]);
+    return 0.0;
+}
+
 void swcpu_update_boundary(swcpu_domain *D)
 {
     const long Nb = D->number_of_boundary_elements;
@@ -766,6 +907,25 @@ void swcpu_update_boundary(swcpu_domain *D)
                 T->p[0] + T->p[1] * sin(two_pi * D->time / T->p[2] + T->p[3]);
             D->xmom_boundary_values[m] = 0.0;
             D->ymom_boundary_values[m] = 0.0;
+        } else if (T->type == SWCPU_BC_TRANSMISSIVE) {
+            /* anuga Transmissive_boundary: the inside edge values */
+            D->stage_boundary_values[m] = D->stage_edge_values[ki];
+            D->xmom_boundary_values[m] = D->xmom_edge_values[ki];
+            D->ymom_boundary_values[m] = D->ymom_edge_values[ki];
+        } else if (T->type == SWCPU_BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM) {
+            /* anuga Transmissive_stage_zero_momentum_boundary */
+            D->stage_boundary_values[m] = D->stage_edge_values[ki];
+            D->xmom_boundary_values[m] = 0.0;
+            D->ymom_boundary_values[m] = 0.0;
+        } else if (T->type == SWCPU_BC_INFLOW_HYDROGRAPH) {
+            /* triangular hydrograph of unit discharge q(t) entering through
+             * the edge at critical depth (q^2/g)^(1/3) above the edge bed */
+            const double q = swcpu_hydrograph(T->p, D->time);
+            const double h = cbrt(q * q / D->params->g);
+            const double n1 = D->normals[2 * ki], n2 = D->normals[2 * ki + 1];
+            D->stage_boundary_values[m] = D->bed_edge_values[ki] + h;
+            D->xmom_boundary_values[m] = -q * n1;
+            D->ymom_boundary_values[m] = -q * n2;
         } else {
             D->status |= SWCPU_ERR_BOUNDARY_TYPE;
         }

@@ -17,6 +17,9 @@ enum {
     SWCPU_BC_REFLECTIVE = 0,
     SWCPU_BC_DIRICHLET = 1,
     SWCPU_BC_TIME_STAGE_SINE = 2,
+    SWCPU_BC_TRANSMISSIVE = 3,
+    SWCPU_BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM = 4,
+    SWCPU_BC_INFLOW_HYDROGRAPH = 5,
 };
 
 enum {
@@ -47,11 +50,14 @@ typedef struct {
     long use_sloped_mannings;
     long max_smallsteps;
     long default_order;
+    long optimised_gradient_limiter; /* 1: extrapolate_second_order_sw */
+    long use_edge_limiter;           /* 1: per-quantity limit by edge */
 } swcpu_params;
 
 typedef struct {
     long type;     /* SWCPU_BC_* */
-    double p[4];   /* Dirichlet: stage, xmom, ymom; sine: mean, amp, period, phase */
+    double p[4];   /* Dirichlet: stage, xmom, ymom; sine: mean, amp, period, phase;
+                      hydrograph: peak unit discharge, rise, fall, start time */
 } swcpu_boundary_tag;
 
 typedef struct {
@@ -105,10 +111,12 @@ int swcpu_update_conserved_quantities(swcpu_domain *D, double dt);
 void swcpu_protect(swcpu_domain *D);
 void swcpu_extrapolate_second_order_sw(swcpu_domain *D);
 void swcpu_extrapolate_first_order(swcpu_domain *D);
+int swcpu_extrapolate_and_limit_by_neighbours(swcpu_domain *D, int by_edge);
 void swcpu_balance_deep_and_shallow(swcpu_domain *D);
 void swcpu_interpolate_to_edges(swcpu_domain *D);
 void swcpu_distribute_to_vertices_and_edges(swcpu_domain *D);
 void swcpu_update_boundary(swcpu_domain *D);
+double swcpu_hydrograph(const double p[4], double t);
 void swcpu_update_timestep(swcpu_domain *D, double finaltime);
 int swcpu_evolve_one_euler_step(swcpu_domain *D, double finaltime);
 void swcpu_backup_conserved_quantities(swcpu_domain *D);

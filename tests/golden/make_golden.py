@@ -94,6 +94,10 @@ def cases():
         extrapolate_velocity_second_order=0, tight_slope_limiters=0,
         use_centroid_velocities=0, use_sloped_mannings=1)
     yield "harbour_small", scenarios.tidal_harbour(target_triangles=1500, seed=11), DEFAULT
+    yield "basin_edge_limiter", scenarios.small_basin(9, 7, seed=8), DEFAULT.replace(
+        use_edge_limiter=1, beta_w=0.8, beta_uh=1.1, beta_vh=1.3)
+    yield "channel_vertex_limiter", scenarios.channel_inflow(14, 5, seed=1), DEFAULT.replace(
+        optimised_gradient_limiter=0)
 
 
 def ref_step(R, od, finaltime=-1.0):
@@ -107,22 +111,22 @@ def ref_step(R, od, finaltime=-1.0):
     rc = R.update(od, D.timestep)
     assert rc == 0
     D.time = t0 + D.timestep
-    R.protect(od)
-    if D.order == 1:
-        od.extrapolate_first_order()
-    else:
-        R.extrapolate_second_order_sw(od)
-    R.balance_deep_and_shallow(od)
-    R.interpolate_to_edges(od)
-    od.update_boundary()
+    ref_distribute(R, od)
 
 
 def ref_distribute(R, od):
+    """distribute_to_vertices_and_edges (gpu_domain_advanced.py:1744-2001)
+    with the reference's kernels, then the boundary values."""
+    p = od.params
     R.protect(od)
     if od.D.order == 1:
         od.extrapolate_first_order()
-    else:
+    elif p.use_edge_limiter:
+        assert R.limit_by_neighbours(od, True) == 0
+    elif p.optimised_gradient_limiter:
         R.extrapolate_second_order_sw(od)
+    else:
+        assert R.limit_by_neighbours(od, False) == 0
     R.balance_deep_and_shallow(od)
     R.interpolate_to_edges(od)
     od.update_boundary()

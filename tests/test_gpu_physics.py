@@ -116,3 +116,51 @@ def test_unknown_boundary_type_rejected(swgpu_built):
     with pytest.raises(SwgpuError):
         check(lib().swgpu_set_boundary_tags(d._h, arr, len(sc.mesh.tag_names)), d._h)
     _ = GPU_domain
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_inflow_hydrograph_volume(precision, swgpu_built):
+    """Water entering through the hydrograph boundary of a channel that is
+    otherwise walled: the volume gained follows the integral of Q(t) while
+    the inflow cells stay shallow (critical-depth inflow)."""
+    from anuga_cuda import DEFAULT, scenarios
+    from anuga_cuda.boundaries import Reflective_boundary
+    sc = scenarios.channel_inflow(28, 10, seed=3, peak=0.4, rise=3.0)
+    for t in ("right", "top"):
+        sc.boundaries[t] = Reflective_boundary()
+    d = gpu_from_scenario(sc, DEFAULT, precision)
+    v0 = d.get_water_volume()
+    times = list(d.evolve(yieldstep=1.0, finaltime=4.0))
+    assert times[-1] == 4.0
+    q = sc.boundaries["left"]
+    ts = np.linspace(0.0, 4.0, 4001)
+    qs = np.array([q.discharge(t) for t in ts])
+    expect = float(np.sum(0.5 * (qs[1:] + qs[:-1]) * np.diff(ts)))
+    gained = d.get_water_volume() - v0
+    assert abs(gained - expect) < 0.1 * expect, (gained, expect)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_transmissive_outflow_and_mixed_close(precision, swgpu_built):
+    """The channel with all its open boundaries: runs clean in both
+    precisions, and the mixed precision stays within 1e-4 of FP64."""
+    from anuga_cuda import DEFAULT, scenarios
+    sc = scenarios.channel_inflow(40, 12, seed=4, peak=1.0, rise=2.0)
+    runs = {}
+    for prec in ("fp64", precision):
+        d = gpu_from_scenario(sc, DEFAULT, prec)
+        st = d.evolve_steps(400)
+        assert st.status == 0
+        runs[prec] = d.quantities["stage"].centroid_values
+    assert max_rel(runs[precision], runs["fp64"]) < 1e-4
+
+
+def test_limiter_variants_need_fp64(swgpu_built):
+    from anuga_cuda import DEFAULT, scenarios
+    from anuga_cuda._lib import SwgpuError
+    sc = scenarios.small_basin(8, 6, seed=1)
+    for kw in ({"use_edge_limiter": 1}, {"optimised_gradient_limiter": 0}):
+        with pytest.raises(SwgpuError):
+            gpu_from_scenario(sc, DEFAULT.replace(**kw), "mixed")
+        d = gpu_from_scenario(sc, DEFAULT.replace(**kw), "fp64")
+        assert d.evolve_steps(20).status == 0

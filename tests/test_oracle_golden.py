@@ -99,6 +99,10 @@ def test_golden_cases_cover_wet_dry_and_boundaries():
     assert set(g["tags/type"].tolist()) >= {0, 1}, "reflective and Dirichlet boundaries"
     hs = load_golden("harbour_small")
     assert 2 in hs["tags/type"].tolist(), "time-dependent stage boundary"
+    ch = load_golden("channel_vertex_limiter")
+    assert set(ch["tags/type"].tolist()) >= {3, 4, 5}, "transmissive and inflow boundaries"
+    assert ch["params"][-2] == 0, "per-quantity vertex limiter"
+    assert load_golden("basin_edge_limiter")["params"][-1] == 1, "edge limiter"
     nb = np.concatenate([load_golden(c)["mesh/number_of_boundaries"] for c in GOLDEN_CASES])
     assert set(nb.tolist()) == {0, 1, 2, 3}, "every number_of_boundaries branch"
     assert np.isfinite(g["run/final/mass"]).all()

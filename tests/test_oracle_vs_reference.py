@@ -103,3 +103,19 @@ def test_saxpy_bitwise(oracle_mod, ref, ab):
     ref.saxpy_conserved_quantities(b, *ab)
     for q in ("stage", "xmom", "ymom"):
         assert bits_equal(a.arrays[q + "_centroid_values"], b.arrays[q + "_centroid_values"])
+
+
+@pytest.mark.parametrize("by_edge", [False, True])
+@pytest.mark.parametrize("seed", [2, 6])
+def test_limit_by_neighbours_bitwise(oracle_mod, ref, by_edge, seed):
+    """The per-quantity vertex / edge limiters against the reference's
+    _compute_gradients + _extrapolate_from_gradient + _limit_*_by_all_neighbours."""
+    from anuga_cuda import DEFAULT, scenarios
+    params = DEFAULT.replace(beta_w=0.7, beta_uh=1.2, beta_vh=1.6)
+    for sc in (scenarios.small_basin(10, 8, seed=seed), scenarios.channel_inflow(seed=seed)):
+        a, b = _pair(oracle_mod, sc, params)
+        assert a.extrapolate_and_limit_by_neighbours(by_edge) == 0
+        assert ref.limit_by_neighbours(b, by_edge) == 0
+        for q in ("stage", "xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_vertex_values"], b.arrays[q + "_vertex_values"]), q
+            assert bits_equal(a.arrays[q + "_edge_values"], b.arrays[q + "_edge_values"]), q

@@ -15,6 +15,7 @@ in or reads out uses the caller's own triangle order.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -145,6 +146,10 @@ class GPU_domain:
         # Mesh's own order when a Mesh is passed in
         self._perm = mesh.permutation if built_here else np.arange(mesh.number_of_elements)
         self._identity = bool(np.all(self._perm == np.arange(len(self._perm))))
+        # triangles the Mesh turned counter-clockwise (vertices, and so edges,
+        # 1 and 2 swapped) in the caller's order
+        flip = getattr(mesh, "flipped", None) if built_here else None
+        self._flip = np.nonzero(flip)[0] if flip is not None and np.any(flip) else None
         self.boundary_map = {t: None for t in mesh.tag_names}
         self.quantities = {n: Quantity(self, n) for n in _QID}
         self.flux_timestep = None
@@ -152,6 +157,11 @@ class GPU_domain:
         self.yieldstep = None
         self.finaltime = None
         self._timestepping_method = "euler"
+        self.name = "domain"
+        self.datadir = "."
+        self.store = False
+        self.smooth = True           # SWW values averaged onto mesh nodes
+        self.writer = None
         self._h = None
         self._create()
 
@@ -202,14 +212,24 @@ class GPU_domain:
             self._h = None
 
     # -- index order ----------------------------------------------------
+    def _swap12(self, a):
+        """Swap columns 1 and 2 of the flipped rows of a caller-order (N, 3)
+        array (vertex or edge values, triangle vertex indices)."""
+        if self._flip is None or a.ndim != 2 or a.shape[1] != 3:
+            return a
+        a = a.copy()
+        a[self._flip, 1], a[self._flip, 2] = a[self._flip, 2].copy(), a[self._flip, 1].copy()
+        return a
+
     def _to_user(self, a):
         if self._identity:
-            return a
+            return self._swap12(a)
         out = np.empty_like(a)
         out[self._perm] = a
-        return out
+        return self._swap12(out)
 
     def _to_internal(self, a):
+        a = self._swap12(np.asarray(a))
         if self._identity:
             return np.ascontiguousarray(a)
         return np.ascontiguousarray(a[self._perm])
@@ -287,7 +307,7 @@ class GPU_domain:
         arr = (_lib.BoundaryTag_t * max(len(names), 1))()
         for i, t in enumerate(names):
             b = self.boundary_map.get(t) or Reflective_boundary(self)
-            arr[i] = b.tag_struct()
+            arr[i] = b.tag_struct(self.mesh, t)
         check(lib().swgpu_set_boundary_tags(self._h, arr, len(names)), self._h)
 
     # -- time -------------------------------------------------------------
@@ -349,12 +369,42 @@ class GPU_domain:
 
     def set_name(self, name):
         self.name = name
+        self.writer = None
 
-    def set_store(self, flag):
-        self.store = flag
+    def get_name(self):
+        return self.name
+
+    def set_store(self, flag=True):
+        """Write an SWW time slice at every yield of evolve."""
+        self.store = bool(flag)
 
     def set_datadir(self, path):
         self.datadir = path
+        self.writer = None
+
+    def get_datadir(self):
+        return self.datadir
+
+    def set_store_vertices_uniquely(self, flag=True):
+        """SWW points per triangle vertex (True) or smoothed onto the mesh
+        nodes (False, the default)."""
+        self.smooth = not flag
+        self.writer = None
+
+    def store_timestep(self):
+        """Copy the vertex values back and append one SWW time slice
+        (gpu_domain_advanced.py:2167-2172).  The file is
+        <datadir>/<name>.sww, created at the first call."""
+        from .io import SWWWriter, sww_path
+        if self.writer is None:
+            os.makedirs(self.datadir or ".", exist_ok=True)
+            tris = self._to_user(np.asarray(self.mesh.triangles))
+            fric = np.repeat(self.quantities["friction"].centroid_values[:, None], 3, axis=1)
+            self.writer = SWWWriter(sww_path(self.datadir, self.name), self.mesh.points, tris,
+                                    self.quantities["elevation"].vertex_values, fric,
+                                    smooth=self.smooth, starttime=self.starttime)
+        self.writer.store_timestep(self.get_time(), {
+            n: self.quantities[n].vertex_values for n in ("stage", "xmomentum", "ymomentum")})
 
     def check_integrity(self):
         return True
@@ -507,6 +557,8 @@ class GPU_domain:
         check(lib().swgpu_evolve_start(self._h, start, self.yieldstep,
                                        -1.0 if finaltime is None else float(finaltime)), self._h)
         if not skip_initial_step:
+            if self.store:
+                self.store_timestep()
             yield self.get_time()
         remaining = max_steps
         st = _lib.State_t()
@@ -518,6 +570,8 @@ class GPU_domain:
             check(lib().swgpu_evolve_run(self._h, budget, C.byref(st)), self._h)
             if remaining is not None:
                 remaining -= st.total_steps - steps_before
+            if st.stop_reason in (_lib.STOP_FINAL, _lib.STOP_YIELD) and self.store:
+                self.store_timestep()
             if st.stop_reason == _lib.STOP_FINAL:
                 yield st.time
                 return

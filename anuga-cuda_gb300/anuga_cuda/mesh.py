@@ -79,6 +79,7 @@ class Mesh:
         if np.any(signed == 0):
             raise ValueError("degenerate (zero-area) triangle")
         cw = signed < 0
+        self.flipped = cw            # caller's order: vertices 1 and 2 swapped
         if cw.any():
             tri[cw, 1], tri[cw, 2] = tri[cw, 2].copy(), tri[cw, 1].copy()
             swap = {1: 2, 2: 1, 0: 0}

@@ -97,6 +97,12 @@ class BoundaryTag_t(C.Structure):
 _VP = C.c_void_p
 _SIGNATURES = [
     ("swgpu_create", C.c_int, [C.POINTER(Mesh_t), C.POINTER(Params_t), C.c_int, C.POINTER(_VP)]),
+    ("swgpu_create_ensemble", C.c_int, [C.POINTER(Mesh_t), _i64p, C.c_int,
+                                        C.POINTER(Params_t), C.c_int, C.POINTER(_VP)]),
+    ("swgpu_ensemble_size", C.c_int, [_VP, C.POINTER(C.c_int)]),
+    ("swgpu_ensemble_get_state", C.c_int, [_VP, C.c_int, C.POINTER(State_t)]),
+    ("swgpu_ensemble_set_finaltimes", C.c_int, [_VP, _f64p]),
+    ("swgpu_ensemble_mass", C.c_int, [_VP, _f64p]),
     ("swgpu_destroy", C.c_int, [_VP]),
     ("swgpu_last_error", C.c_char_p, [_VP]),
     ("swgpu_device_info", C.c_int, [C.c_char_p, C.c_int]),

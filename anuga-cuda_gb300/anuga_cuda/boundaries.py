@@ -125,8 +125,9 @@ class Inflow_hydrograph_boundary(Boundary):
     over ``rise`` seconds and falls back to 0 over ``fall`` seconds (default
     ``2*rise``).  Q is spread evenly over the tag's edge length ``width``
     (taken from the mesh when not given) as unit discharge q = Q/width,
-    entering along the inward normal at critical depth (q^2/g)^(1/3) above
-    the edge bed."""
+    entering along the inward normal with the inside edge's stage, or at
+    critical depth (q^2/g)^(1/3) above the edge bed where that is higher
+    (a dry or shallow inflow edge)."""
 
     type = _lib.BC_INFLOW_HYDROGRAPH
 

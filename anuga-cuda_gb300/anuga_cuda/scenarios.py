@@ -305,3 +305,87 @@ def channel_inflow(m=14, n=5, seed=0, peak=0.5, rise=2.0):
                     "right": Transmissive_boundary(),
                     "top": Transmissive_stage_zero_momentum_boundary(),
                     "bottom": Reflective_boundary()}, steps=50)
+
+
+def jittered_points(width, height, target_triangles, seed, jitter=0.3):
+    """About target_triangles/2 points in [0,width] x [0,height]: a
+    hexagonal lattice with uniform jitter of +-jitter spacings (a fast
+    stand-in for Poisson-disk sampling at large sizes), plus evenly spaced
+    points on the rectangle's edges."""
+    rng = np.random.default_rng(seed)
+    P = target_triangles / 2.0
+    d = np.sqrt(2.0 * width * height / (np.sqrt(3.0) * P))
+    dy = d * np.sqrt(3.0) / 2.0
+    ny = max(int(round(height / dy)), 1)
+    nx = max(int(round(width / d)), 1)
+    dx, dy = width / nx, height / ny
+    jj, ii = np.meshgrid(np.arange(1, ny), np.arange(1, nx), indexing="ij")
+    x = (ii + 0.5 * (jj % 2) - 0.25) * dx
+    y = jj * dy
+    x = x.ravel() + rng.uniform(-jitter, jitter, x.size) * dx
+    y = y.ravel() + rng.uniform(-jitter, jitter, y.size) * dy
+    keep = (x > 0.2 * dx) & (x < width - 0.2 * dx)
+    inner = np.stack([x[keep], y[keep]], axis=1)
+    bx = np.linspace(0.0, width, nx + 1)
+    by = np.linspace(0.0, height, ny + 1)[1:-1]
+    edge = np.concatenate([np.stack([bx, np.zeros_like(bx)], 1),
+                           np.stack([bx, np.full_like(bx, height)], 1),
+                           np.stack([np.zeros_like(by), by], 1),
+                           np.stack([np.full_like(by, width), by], 1)])
+    return np.concatenate([edge, inner])
+
+
+def inflow_harbour(target_triangles=45000, seed=4, peak=200.0, rise=900.0, friction=0.025,
+                   width=2000.0, height=1000.0, fast_points=True):
+    """The tidal harbour's extent, Delaunay mesh and Gaussian-random-field
+    bed (mean -5 m, sd 3 m, correlation 100 m, clipped at +1 m), water at
+    rest at level 0, fed through its west edge by a triangular inflow
+    hydrograph (``peak`` m^3/s after ``rise`` s, back to 0 after another
+    2*rise s), walls elsewhere, uniform Manning ``friction``.  Jittered
+    lattice points by default (fast at 10^5 triangles)."""
+    from scipy.spatial import Delaunay
+    from .boundaries import Inflow_hydrograph_boundary
+    if fast_points:
+        pts = jittered_points(width, height, target_triangles, seed)
+    else:
+        P = target_triangles / 2.0
+        pts = poisson_disk(width, height, np.sqrt(0.70 * width * height / P), seed)
+    tri = Delaunay(pts).simplices
+    V = pts[tri]
+    area = 0.5 * np.abs((V[:, 1, 0] - V[:, 0, 0]) * (V[:, 2, 1] - V[:, 0, 1]) -
+                        (V[:, 2, 0] - V[:, 0, 0]) * (V[:, 1, 1] - V[:, 0, 1]))
+    tri = tri[area > 1e-6 * np.median(area)]
+    tmp = Mesh(pts, tri, None, reorder=False)
+    keys = list(tmp.boundary)
+    kk = np.array(keys, dtype=np.int64).reshape(-1, 2)
+    a = tmp.triangles[kk[:, 0], (kk[:, 1] + 1) % 3]
+    b = tmp.triangles[kk[:, 0], (kk[:, 1] + 2) % 3]
+    west = (pts[a, 0] == 0.0) & (pts[b, 0] == 0.0)
+    boundary = {k: ("west" if w else "wall") for k, w in zip(keys, west.tolist())}
+    mesh = Mesh(pts, tmp.triangles, boundary)
+    spacing = 10.0
+    field = gaussian_random_field((int(width / spacing) + 2, int(height / spacing) + 2), spacing,
+                                  100.0, -5.0, 3.0, seed)
+    V = mesh.vertex_coordinates.reshape(-1, 3, 2)
+    z = np.minimum(_bilinear(field, spacing, V[..., 0], V[..., 1]), 1.0)
+    zc = z.mean(axis=1)
+    N = mesh.number_of_elements
+    return Scenario(
+        name=f"inflow_harbour_{N}", mesh=mesh, elevation_vertex=z,
+        stage_centroid=np.maximum(0.0, zc), xmom_centroid=np.zeros(N),
+        ymom_centroid=np.zeros(N), friction=np.full(N, float(friction)),
+        boundaries={"west": Inflow_hydrograph_boundary(peak=peak, rise=rise),
+                    "wall": Reflective_boundary()}, finaltime=3600.0)
+
+
+def ensemble_harbours(count=256, seed=4, nmin=5000, nmax=200000):
+    """Ensemble scenarios: ``count`` inflow harbours with triangle counts
+    log-uniform in [nmin, nmax], hydrograph peak U[50, 500] m^3/s, rise
+    U[300, 1800] s and Manning n U[0.01, 0.05], all drawn from ``seed``."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), count))
+    peaks = rng.uniform(50.0, 500.0, count)
+    rises = rng.uniform(300.0, 1800.0, count)
+    frics = rng.uniform(0.01, 0.05, count)
+    return [inflow_harbour(int(n), seed=int(seed * 100003 + i), peak=p, rise=r, friction=f)
+            for i, (n, p, r, f) in enumerate(zip(sizes, peaks, rises, frics))]

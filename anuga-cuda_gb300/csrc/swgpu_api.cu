@@ -85,13 +85,15 @@ static int check_launch(Handle *h, const char *what) {
 }
 
 static int sync_ctrl(Handle *h) {
-    CK(cudaMemcpyAsync(h->h_ctrl, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->h_ctrl, h->d_ctrl, sizeof(Ctrl) * h->nscen, cudaMemcpyDeviceToHost,
+                       h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return SWGPU_OK;
 }
 
 static int push_ctrl(Handle *h) {
-    CK(cudaMemcpyAsync(h->d_ctrl, h->h_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_ctrl, h->h_ctrl, sizeof(Ctrl) * h->nscen, cudaMemcpyHostToDevice,
+                       h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return SWGPU_OK;
 }
@@ -116,10 +118,23 @@ static const char *status_text(int s) {
 
 // Device-side failures recorded in Ctrl.status become the call's status.
 static int device_status(Handle *h) {
-    if (h->h_ctrl->status != 0) {
-        const int s = h->h_ctrl->status;
-        return fail(h, s, "device reported: %s", status_text(s));
+    for (int i = 0; i < h->nscen; i++) {
+        if (h->h_ctrl[i].status != 0) {
+            const int s = h->h_ctrl[i].status;
+            if (h->nscen > 1)
+                return fail(h, s, "scenario %d: device reported: %s", i, status_text(s));
+            return fail(h, s, "device reported: %s", status_text(s));
+        }
     }
+    return SWGPU_OK;
+}
+
+// Per-method calls that reduce one timestep over the whole mesh have no
+// meaning for an ensemble of independent scenarios.
+static int require_single(Handle *h, const char *what) {
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (h->nscen > 1)
+        return fail(h, SWGPU_EINVAL, "%s: not available on an ensemble handle", what);
     return SWGPU_OK;
 }
 
@@ -243,8 +258,10 @@ int swgpu_device_info(char *buf, int buflen) {
     return SWGPU_OK;
 }
 
-int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precision,
-                 void **handle_out) {
+// Shared by swgpu_create (offsets == nullptr, one scenario) and
+// swgpu_create_ensemble.
+static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int precision,
+                       const int64_t *offsets, int nscen, void **handle_out) {
     Handle *h = nullptr;
     if (!mesh || !params || !handle_out) return fail(nullptr, SWGPU_EINVAL, "null argument");
     *handle_out = nullptr;
@@ -259,6 +276,33 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
         !mesh->areas || !mesh->vertex_coordinates || !mesh->centroid_coordinates ||
         (Nb > 0 && (!mesh->boundary_cells || !mesh->boundary_edges || !mesh->boundary_tag)))
         return fail(nullptr, SWGPU_EINVAL, "null mesh array");
+
+    // ---- scenarios of an ensemble: 256-aligned ranges with no neighbour
+    // across a range boundary
+    std::vector<int> tri_scen;
+    if (offsets) {
+        if (nscen < 1 || offsets[0] != 0 || offsets[nscen] != N)
+            return fail(nullptr, SWGPU_EINVAL,
+                        "scenario offsets must start at 0 and end at the triangle count");
+        tri_scen.resize((size_t)N);
+        for (int s = 0; s < nscen; s++) {
+            if (offsets[s + 1] <= offsets[s] || offsets[s] % 256 != 0 || offsets[s + 1] % 256 != 0)
+                return fail(nullptr, SWGPU_EINVAL,
+                            "scenario %d: range [%lld, %lld) must be non-empty and 256-aligned",
+                            s, (long long)offsets[s], (long long)offsets[s + 1]);
+            for (int64_t k = offsets[s]; k < offsets[s + 1]; k++) tri_scen[(size_t)k] = s;
+        }
+        for (int64_t k = 0; k < N; k++)
+            for (int i = 0; i < 3; i++) {
+                const int64_t n = mesh->neighbours[3 * k + i];
+                const int64_t sn = mesh->surrogate_neighbours[3 * k + i];
+                if ((n >= 0 && n < N && tri_scen[(size_t)n] != tri_scen[(size_t)k]) ||
+                    (sn >= 0 && sn < N && tri_scen[(size_t)sn] != tri_scen[(size_t)k]))
+                    return fail(nullptr, SWGPU_EMESH,
+                                "triangle %lld has a neighbour in another scenario",
+                                (long long)k);
+            }
+    }
 
     // ---- validate and pack the topology on the host
     std::vector<int> nbr((size_t)3 * N), surr((size_t)3 * N);
@@ -544,11 +588,23 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
     }
 
     h->ntags = (int)(maxtag + 1);
+    h->nscen = offsets ? nscen : 1;
     TRY(dalloc(h, &h->d_tags, (size_t)std::max(h->ntags, 1)));  // zero = reflective
-    TRY(dalloc(h, &h->d_ctrl, 1));
+    TRY(dalloc(h, &h->d_ctrl, (size_t)h->nscen));
+    TRY(dalloc(h, &h->d_summary, 1));
     TRY(dalloc(h, &h->d_scalar, 4));
+    if (offsets) {
+        const int64_t nblk = N / 256;
+        std::vector<int> blk((size_t)nblk);
+        for (int64_t b = 0; b < nblk; b++) blk[(size_t)b] = tri_scen[(size_t)(b * 256)];
+        TRY(dalloc(h, &h->d_blk_scen, (size_t)nblk));
+        TRY(upload(h, h->d_blk_scen, blk.data(), (size_t)nblk));
+        M.blk_scen = h->d_blk_scen;
+        h->scen_offsets.assign(offsets, offsets + nscen + 1);
+    }
     {
-        cudaError_t e = cudaMallocHost((void **)&h->h_ctrl, sizeof(Ctrl));
+        cudaError_t e = cudaMallocHost((void **)&h->h_ctrl, sizeof(Ctrl) * h->nscen);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_summary, sizeof(RunSummary));
         if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_scalar, 4 * sizeof(double));
         if (e != cudaSuccess) {
             fail(h, SWGPU_ENOMEM, "pinned host allocation: %s", cudaGetErrorString(e));
@@ -557,22 +613,43 @@ int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precisi
             return SWGPU_ENOMEM;
         }
     }
-    std::memset(h->h_ctrl, 0, sizeof(Ctrl));
-    Ctrl *c = h->h_ctrl;
-    c->order = P.default_order;
-    c->finaltime = -1.0;
-    c->yieldtime = 1.0e300;
-    c->yieldstep = 1.0e300;
-    c->time_epsilon = params->epsilon;
-    c->rec_max = P.evolve_min_timestep;
-    c->rec_min = P.evolve_max_timestep;
-    c->budget = -1;
-    reset_ftmin(c, P);
+    std::memset(h->h_ctrl, 0, sizeof(Ctrl) * h->nscen);
+    std::memset(h->h_summary, 0, sizeof(RunSummary));
+    const int flux_tile = precision == SWGPU_MIXED ? 128 : kBlock;
+    for (int i = 0; i < h->nscen; i++) {
+        Ctrl *c = &h->h_ctrl[i];
+        const int64_t n = offsets ? offsets[i + 1] - offsets[i] : N;
+        c->order = P.default_order;
+        c->finaltime = -1.0;
+        c->yieldtime = 1.0e300;
+        c->yieldstep = 1.0e300;
+        c->time_epsilon = params->epsilon;
+        c->rec_max = P.evolve_min_timestep;
+        c->rec_min = P.evolve_max_timestep;
+        c->budget = -1;
+        c->blocks_flux = (unsigned)((n + flux_tile - 1) / flux_tile);
+        c->blocks_256 = (unsigned)((n + kBlock - 1) / kBlock);
+        c->summary = h->d_summary;
+        reset_ftmin(c, P);
+    }
     TRY(push_ctrl(h));
+    TRY(upload(h, h->d_summary, h->h_summary, 1));
     if (precision == SWGPU_MIXED) TRY(build_mixed_geometry(h) ? fail(h, SWGPU_ECUDA, "mixed geometry upload") : SWGPU_OK);
     *handle_out = h;
 #undef TRY
     return SWGPU_OK;
+}
+
+int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params, int precision,
+                 void **handle_out) {
+    return create_impl(mesh, params, precision, nullptr, 1, handle_out);
+}
+
+int swgpu_create_ensemble(const swgpu_mesh *mesh, const int64_t *scenario_offsets, int nscen,
+                          const swgpu_params *params, int precision, void **handle_out) {
+    if (!scenario_offsets || nscen < 1)
+        return fail(nullptr, SWGPU_EINVAL, "an ensemble needs scenario offsets");
+    return create_impl(mesh, params, precision, scenario_offsets, nscen, handle_out);
 }
 
 int swgpu_destroy(void *handle) {
@@ -582,6 +659,7 @@ int swgpu_destroy(void *handle) {
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (void *p : h->allocs) cudaFree(p);
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
+    if (h->h_summary) cudaFreeHost(h->h_summary);
     if (h->h_scalar) cudaFreeHost(h->h_scalar);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -799,6 +877,7 @@ int swgpu_compute_fluxes(void *handle, double *flux_timestep) {
     Handle *h = static_cast<Handle *>(handle);
     int rc = require_fp64(h, "compute_fluxes");
     if (rc) return rc;
+    if ((rc = require_single(h, "compute_fluxes"))) return rc;
     if ((rc = sync_ctrl(h))) return rc;
     reset_ftmin(h->h_ctrl, h->P);
     if ((rc = push_ctrl(h))) return rc;
@@ -827,6 +906,7 @@ int swgpu_update_conserved_quantities(void *handle, double timestep) {
     Handle *h = static_cast<Handle *>(handle);
     int rc = require_fp64(h, "update_conserved_quantities");
     if (rc) return rc;
+    if ((rc = require_single(h, "update_conserved_quantities"))) return rc;
     launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, timestep, 0, kEulerStage, h->stream);
     if ((rc = check_launch(h, "update_conserved_quantities"))) return rc;
     if ((rc = sync_ctrl(h))) return rc;
@@ -901,6 +981,69 @@ int swgpu_get_state(void *handle, swgpu_state *state) {
     return SWGPU_OK;
 }
 
+int swgpu_ensemble_get_state(void *handle, int scenario, swgpu_state *state) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !state) return fail(h, SWGPU_EINVAL, "null argument");
+    if (scenario < 0 || scenario >= h->nscen)
+        return fail(h, SWGPU_EINVAL, "scenario %d of %d", scenario, h->nscen);
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    fill_state(&h->h_ctrl[scenario], state);
+    return SWGPU_OK;
+}
+
+int swgpu_ensemble_set_finaltimes(void *handle, const double *finaltimes) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !finaltimes) return fail(h, SWGPU_EINVAL, "null argument");
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    for (int i = 0; i < h->nscen; i++) {
+        if (finaltimes[i] > 0 && finaltimes[i] < h->h_ctrl[i].time)
+            return fail(h, SWGPU_EINVAL, "scenario %d: finaltime before its time", i);
+        h->h_ctrl[i].finaltime = finaltimes[i] > 0 ? finaltimes[i] : -1.0;
+    }
+    return push_ctrl(h);
+}
+
+// Water volume of every scenario: the block partials of swgpu_mass summed
+// per scenario in the order of the device's final reduction (strided
+// per-thread sums over 256 threads, then a pairwise tree), so that each
+// equals swgpu_mass of the scenario run alone.
+int swgpu_ensemble_mass(void *handle, double *masses) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !masses) return fail(h, SWGPU_EINVAL, "null argument");
+    if (h->precision == SWGPU_MIXED && !h->mixed_from_stage)
+        launch_mass_partials_mixed(h->M, h->S, h->X, h->stream);
+    else
+        launch_mass_partials(h->M, h->S, h->stream);
+    int rc = check_launch(h, "ensemble mass");
+    if (rc) return rc;
+    const int nblk = grid_for(h->M.N);
+    std::vector<double> part((size_t)nblk);
+    if ((rc = download(h, part.data(), h->S.partials, (size_t)nblk))) return rc;
+    for (int i = 0; i < h->nscen; i++) {
+        const int64_t b0 = h->nscen > 1 ? h->scen_offsets[i] / kBlock : 0;
+        const int64_t nb = h->nscen > 1 ? h->scen_offsets[i + 1] / kBlock - b0 : nblk;
+        double sh[kBlock];
+        for (int t = 0; t < kBlock; t++) {
+            double acc = 0.0;
+            for (int64_t j = t; j < nb; j += kBlock) acc += part[(size_t)(b0 + j)];
+            sh[t] = acc;
+        }
+        for (int w = kBlock / 2; w > 0; w >>= 1)
+            for (int t = 0; t < w; t++) sh[t] += sh[t + w];
+        masses[i] = sh[0];
+    }
+    return SWGPU_OK;
+}
+
+int swgpu_ensemble_size(void *handle, int *nscen) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !nscen) return fail(h, SWGPU_EINVAL, "null argument");
+    *nscen = h->nscen;
+    return SWGPU_OK;
+}
+
 int swgpu_set_state(void *handle, const swgpu_state *s) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || !s) return fail(h, SWGPU_EINVAL, "null argument");
@@ -935,23 +1078,25 @@ int swgpu_evolve_start(void *handle, double starttime, double yieldstep, double 
     // first distribute with the current order (gpu_domain_advanced.py:2476)
     if ((rc = issue_distribute(h, false))) return rc;
     if ((rc = sync_ctrl(h))) return rc;
-    Ctrl *c = h->h_ctrl;
-    c->time = starttime;
-    c->order = h->P.default_order;
-    c->finaltime = finaltime > 0 ? finaltime : -1.0;
-    c->yieldstep = yieldstep;
-    c->yieldtime = starttime + yieldstep;
-    c->rec_min = h->P.evolve_max_timestep;
-    c->rec_max = h->P.evolve_min_timestep;
-    c->steps_since_yield = 0;
-    c->total_steps = 0;
-    c->halt = 0;
-    c->halt_pending = 0;
-    c->stop_reason = kStopNone;
-    c->status = 0;
-    c->budget = -1;
-    c->done_update = c->done_distribute = 0;
-    reset_ftmin(c, h->P);
+    for (int i = 0; i < h->nscen; i++) {
+        Ctrl *c = &h->h_ctrl[i];
+        c->time = starttime;
+        c->order = h->P.default_order;
+        c->finaltime = finaltime > 0 ? finaltime : -1.0;
+        c->yieldstep = yieldstep;
+        c->yieldtime = starttime + yieldstep;
+        c->rec_min = h->P.evolve_max_timestep;
+        c->rec_max = h->P.evolve_min_timestep;
+        c->steps_since_yield = 0;
+        c->total_steps = 0;
+        c->halt = 0;
+        c->halt_pending = 0;
+        c->stop_reason = kStopNone;
+        c->status = 0;
+        c->budget = -1;
+        c->done_update = c->done_distribute = 0;
+        reset_ftmin(c, h->P);
+    }
     if ((rc = push_ctrl(h))) return rc;
     // update_ghosts (no-op), distribute, update_boundary (:2540-2543)
     if ((rc = issue_distribute(h, true))) return rc;
@@ -960,32 +1105,45 @@ int swgpu_evolve_start(void *handle, double starttime, double yieldstep, double 
     return device_status(h);
 }
 
+// Before a run: every scenario that has not reached its finaltime runs;
+// those that stopped at a yield move to the next yield point
+// (gpu_domain_advanced.py:2649-2654).
 static int prepare_run(Handle *h, int64_t max_steps) {
     int rc = sync_ctrl(h);
     if (rc) return rc;
-    Ctrl *c = h->h_ctrl;
-    if (c->status) return device_status(h);
-    if (c->stop_reason == kStopFinal)
-        return fail(h, SWGPU_EINVAL, "evolve already reached finaltime");
-    if (h->resume_after_yield) {
-        // the generator resumed after a yield (gpu_domain_advanced.py:2649-2654)
-        c->yieldtime += c->yieldstep;
-        c->rec_min = h->P.evolve_max_timestep;
-        c->rec_max = h->P.evolve_min_timestep;
-        c->steps_since_yield = 0;
-        h->resume_after_yield = false;
+    if ((rc = device_status(h))) return rc;
+    int running = 0;
+    for (int i = 0; i < h->nscen; i++) {
+        Ctrl *c = &h->h_ctrl[i];
+        if (c->stop_reason == kStopFinal) {
+            c->halt = 1;  // stays halted; counts as halted for the run
+            continue;
+        }
+        if (h->resume_after_yield && c->stop_reason == kStopYield) {
+            c->yieldtime += c->yieldstep;
+            c->rec_min = h->P.evolve_max_timestep;
+            c->rec_max = h->P.evolve_min_timestep;
+            c->steps_since_yield = 0;
+        }
+        c->halt = 0;
+        c->halt_pending = 0;
+        c->stop_reason = kStopNone;
+        c->budget = max_steps > 0 ? max_steps : -1;
+        running++;
     }
-    c->halt = 0;
-    c->halt_pending = 0;
-    c->stop_reason = kStopNone;
-    c->budget = max_steps > 0 ? max_steps : -1;
+    h->resume_after_yield = false;
+    if (running == 0) return fail(h, SWGPU_EINVAL, "evolve already reached finaltime");
+    h->h_summary->halted = h->nscen - running;
+    h->h_summary->status = 0;
+    if ((rc = upload(h, h->d_summary, h->h_summary, 1))) return rc;
     return push_ctrl(h);
 }
 
 static int finish_run(Handle *h, swgpu_state *state) {
     int rc = sync_ctrl(h);
     if (rc) return rc;
-    if (h->h_ctrl->stop_reason == kStopYield) h->resume_after_yield = true;
+    for (int i = 0; i < h->nscen; i++)
+        if (h->h_ctrl[i].stop_reason == kStopYield) h->resume_after_yield = true;
     if (state) fill_state(h->h_ctrl, state);
     return device_status(h);
 }
@@ -1069,7 +1227,7 @@ static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *
     while (!halted && launched < max_graphs) {
         e = cudaGraphLaunch(h->graph, h->stream);
         if (e != cudaSuccess) break;
-        e = cudaMemcpyAsync(&h->h_ctrl->halt, &h->d_ctrl->halt, sizeof(int) * 4,
+        e = cudaMemcpyAsync(h->h_summary, h->d_summary, sizeof(RunSummary),
                             cudaMemcpyDeviceToHost, h->stream);
         if (e != cudaSuccess) break;
         e = cudaEventRecord(ev[slot], h->stream);
@@ -1081,7 +1239,7 @@ static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *
             e = cudaEventSynchronize(ev[slot]);  // the older of the two
             if (e != cudaSuccess) break;
             inflight--;
-            if (h->h_ctrl->halt || h->h_ctrl->status) halted = true;
+            if (h->h_summary->halted >= h->nscen || h->h_summary->status) halted = true;
         }
     }
     if (e == cudaSuccess) e = cudaEventRecord(t1, h->stream);

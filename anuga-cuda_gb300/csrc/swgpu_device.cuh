@@ -34,8 +34,10 @@ __device__ __forceinline__ double hydrograph(const double p[4], double t) {
 // Dirichlet: :80-115; ANUGA's transmissive boundaries: the inside edge
 // values, with or without momentum; the time-dependent stage and the inflow
 // hydrograph have no reference GPU counterpart: the hydrograph's unit
-// discharge q(t) enters along the inward normal at critical depth
-// (q^2/g)^(1/3) above the edge bed ze).  Returns false for an unknown type.
+// discharge q(t) enters along the inward normal with the inside edge's
+// stage, or critical depth (q^2/g)^(1/3) above the edge bed ze where that
+// is higher, i.e. on a dry or shallow edge).  Returns false for an unknown
+// type.
 __device__ __forceinline__ bool eval_boundary(const BcTag &T, double time, double we,
                                               double uhe, double vhe, double n1,
                                               double n2, double ze, double g, double &wb,
@@ -75,7 +77,7 @@ __device__ __forceinline__ bool eval_boundary(const BcTag &T, double time, doubl
     }
     if (T.type == SWGPU_BC_INFLOW_HYDROGRAPH) {
         const double q = hydrograph(T.p, time);
-        wb = ze + cbrt(q * q / g);
+        wb = omax(we, ze + cbrt(q * q / g));
         uhb = -q * n1;
         vhb = -q * n2;
         return true;
@@ -140,13 +142,20 @@ __device__ __forceinline__ StepClock published_step_clock(const Ctrl *c) {
     return s;
 }
 
+// The control block of the scenario that owns this block's triangles
+// (the block's first triangle is blockIdx.x * blockDim.x).
+__device__ __forceinline__ Ctrl *block_ctrl(Ctrl *base, const DevMesh &M) {
+    return M.blk_scen ? base + M.blk_scen[(blockIdx.x * blockDim.x) >> 8] : base;
+}
+
 // Called by thread 0 of each block after the block's work; returns true in
-// exactly one block, the last to finish (all other blocks' writes are then
-// visible).  The counter is reset for the next launch.
-__device__ __forceinline__ bool last_block_done(unsigned int *counter) {
+// exactly one of the scenario's `blocks` blocks, the last to finish (all
+// other blocks' writes are then visible).  The counter is reset for the
+// next launch.
+__device__ __forceinline__ bool last_block_done(unsigned int *counter, unsigned int blocks) {
     __threadfence();
     const unsigned int prev = atomicAdd(counter, 1u);
-    if (prev == gridDim.x - 1) {
+    if (prev == blocks - 1) {
         __threadfence();
         *counter = 0;
         return true;
@@ -275,6 +284,9 @@ __device__ __forceinline__ void apply_pending_halt(Ctrl *c) {
         c->stop_reason = c->halt_pending;
         c->halt = 1;
         c->halt_pending = 0;
+        if (c->status) atomicCAS(&c->summary->status, 0, c->status);
+        __threadfence();
+        atomicAdd(&c->summary->halted, 1);
     }
 }
 

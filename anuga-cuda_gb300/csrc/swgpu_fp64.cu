@@ -187,6 +187,7 @@ __device__ __forceinline__ void pick(int i, const EdgeFlux &a, const EdgeFlux &b
 // the +flux(n,m) that ANUGA's edge loop adds, and the sums agree bitwise.
 __global__ void __launch_bounds__(kBlock) flux_fp64(DevMesh M, DevState S, DevParams P,
                                                     Ctrl *ctrl, int flags) {
+    ctrl = block_ctrl(ctrl, M);
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     const int N = M.N;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(kBlock) flux_fp64(DevMesh M, DevState S, DevPa
     if (bad) set_status(ctrl, SWGPU_EBED);
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
     block_min_timestep(t, ctrl);
-    if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
+    if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
         publish_step_clock(ctrl, P);
 }
 
@@ -370,6 +371,7 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
                                                       Ctrl *ctrl, double dt_api, int flags,
                                                       Stage stg) {
     const bool fused = flags & kFused;
+    ctrl = block_ctrl(ctrl, M);
     if (fused && ctrl_halted(ctrl)) return;
     StepClock clk;
     if (fused) {
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (fused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update))
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_256))
             commit_stage(ctrl, clk, P, stg);
     }
 }
@@ -653,6 +655,7 @@ __global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S,
                                                           const BcTag *tags, Ctrl *ctrl,
                                                           int flags) {
     const bool fused = flags & kFused;
+    ctrl = block_ctrl(ctrl, M);
     if (fused && ctrl_halted(ctrl)) return;
     const int N = M.N;
     const int order = (int)ctrl->order;
@@ -877,7 +880,7 @@ __global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S,
     if (no_nbr) set_status(ctrl, SWGPU_EMESH);
     if (fused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute)) apply_pending_halt(ctrl);
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_256)) apply_pending_halt(ctrl);
     }
 }
 
@@ -889,6 +892,7 @@ __global__ void __launch_bounds__(kBlock) boundary_fp64(DevMesh M, DevState S, d
     if (m >= M.Nb) return;
     const int N = M.N;
     const int k = M.bcell[m], i = M.bedge[m];
+    if (M.blk_scen) ctrl += M.blk_scen[k >> 8];  // the owning scenario's time
     const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
     const double we = 0.5 * (S.wv[a * N + k] + S.wv[b * N + k]);
     const double uhe = 0.5 * (S.uhv[a * N + k] + S.uhv[b * N + k]);
@@ -1010,6 +1014,9 @@ void launch_interpolate_fp64(const DevMesh &M, const DevState &S, cudaStream_t s
 void launch_other_quantities(const DevMesh &M, const DevState &S, cudaStream_t st) {
     const int n = M.N > M.Nb ? M.N : M.Nb;
     other_quantities<<<grid_for(n), kBlock, 0, st>>>(M, S);
+}
+void launch_mass_partials(const DevMesh &M, const DevState &S, cudaStream_t st) {
+    mass_partials<<<grid_for(M.N), kBlock, 0, st>>>(M, S);
 }
 void launch_mass(const DevMesh &M, const DevState &S, double *out, cudaStream_t st) {
     const int g = grid_for(M.N);

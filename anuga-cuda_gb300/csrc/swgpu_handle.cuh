@@ -23,8 +23,13 @@ struct Handle {
     DevParams P{};
     BcTag *d_tags = nullptr;
     int ntags = 0;
-    Ctrl *d_ctrl = nullptr;
-    Ctrl *h_ctrl = nullptr;      // pinned mirror
+    int nscen = 1;               // scenarios (Ctrl blocks); > 1 for an ensemble
+    std::vector<int64_t> scen_offsets;  // ensemble: first triangle of each scenario, + N
+    int *d_blk_scen = nullptr;   // ensemble: scenario of each 256-triangle block
+    Ctrl *d_ctrl = nullptr;      // [nscen]
+    Ctrl *h_ctrl = nullptr;      // pinned mirror [nscen]
+    RunSummary *d_summary = nullptr;
+    RunSummary *h_summary = nullptr;  // pinned
     double *d_scalar = nullptr;  // mass / misc
     double *h_scalar = nullptr;  // pinned
     std::vector<void *> allocs;

@@ -37,6 +37,9 @@ struct DevMesh {
     const double *vxy;         // [6][N]
     const double *cxy;         // [2][N]
     const int *bcell, *bedge, *btag;   // [Nb]
+    // ensembles: scenario of each 256-triangle block (scenarios start on
+    // 256-triangle boundaries); nullptr for a single mesh
+    const int *blk_scen;
 };
 
 // FP64 state (both precisions keep the conserved centroid state in FP64).
@@ -106,7 +109,14 @@ struct BcTag {
     double p[4];
 };
 
-// Device-resident evolve bookkeeping.  Written by the last block of the
+// Whole-run summary for the host's polling: how many scenarios (Ctrl
+// blocks) have halted, and the first device status among them.
+struct RunSummary {
+    int halted;
+    int status;
+};
+
+// Device-resident evolve bookkeeping, one per scenario.  Written by the last block of the
 // update kernel (time, order, counters) and the last block of the
 // distribute kernel (halt); read by every kernel at entry.
 struct __align__(16) Ctrl {
@@ -124,6 +134,9 @@ struct __align__(16) Ctrl {
     double clk_dt, clk_ftmin;       // the last block of the flux kernel and read
     long long clk_order, clk_smallsteps;  // by the update kernel
     double step_t0;                 // time at the start of a Runge-Kutta step
+    unsigned int blocks_flux;       // blocks of this scenario in one flux launch
+    unsigned int blocks_256;        // ... in one update / distribute launch
+    RunSummary *summary;            // shared by all scenarios of a handle
 };
 
 enum StopReason { kStopNone = 0, kStopYield = 1, kStopFinal = 2, kStopBudget = 3, kStopError = 4 };
@@ -186,6 +199,8 @@ void launch_saxpy_fp64(const DevMesh &M, const DevState &S, double a, double b,
 void launch_interpolate_fp64(const DevMesh &M, const DevState &S, cudaStream_t st);
 void launch_other_quantities(const DevMesh &M, const DevState &S, cudaStream_t st);
 void launch_mass(const DevMesh &M, const DevState &S, double *out, cudaStream_t st);
+// one volume partial per 256-triangle block into S.partials
+void launch_mass_partials(const DevMesh &M, const DevState &S, cudaStream_t st);
 
 // Mixed path (swgpu_mixed.cu)
 void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
@@ -205,6 +220,8 @@ void launch_vertices_from_mixed(const DevMesh &M, const DevState &S, const DevMi
                                 cudaStream_t st);
 void launch_mass_mixed(const DevMesh &M, const DevState &S, const DevMixed &X, double *out,
                        cudaStream_t st);
+void launch_mass_partials_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                                cudaStream_t st);
 
 inline int grid_for(int n) { return (n + kBlock - 1) / kBlock; }
 

@@ -228,6 +228,7 @@ struct __align__(128) FluxTile {
 // are read from shared memory, the others from global memory.
 __global__ void __launch_bounds__(kFluxTile) flux_mixed(DevMesh M, DevMixed X, DevParams P,
                                                         Ctrl *ctrl, int flags) {
+    ctrl = block_ctrl(ctrl, M);
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     __shared__ FluxTile T;
     __shared__ __align__(8) unsigned long long bar;
@@ -330,7 +331,7 @@ __global__ void __launch_bounds__(kFluxTile) flux_mixed(DevMesh M, DevMixed X, D
     }
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
     block_min_timestep_f<kFluxTile>(t, ctrl);
-    if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux))
+    if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
         publish_step_clock(ctrl, P);
 }
 
@@ -377,6 +378,7 @@ __device__ __forceinline__ void finish_state(const DevParams &P, double &h, doub
 __global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S, DevMixed X,
                                                        DevParams P, Ctrl *ctrl, int flags,
                                                        Stage stg) {
+    ctrl = block_ctrl(ctrl, M);
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     const StepClock clk = published_step_clock(ctrl);
     const float dtf = (float)clk.dt;
@@ -432,7 +434,7 @@ __global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S,
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (flags & kFused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update))
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_256))
             commit_stage(ctrl, clk, P, stg);
     }
 }
@@ -502,6 +504,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
                                                            DevParams P, const BcTag *tags,
                                                            Ctrl *ctrl, int flags) {
     const bool fused = flags & kFused;
+    ctrl = block_ctrl(ctrl, M);
     if (fused && ctrl_halted(ctrl)) return;
     const int N = M.N, SP = X.S;
     const int order = (int)ctrl->order;
@@ -707,7 +710,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
     if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
     if (fused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute)) apply_pending_halt(ctrl);
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_256)) apply_pending_halt(ctrl);
     }
 }
 
@@ -805,6 +808,10 @@ void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X
 void launch_vertices_from_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                                 cudaStream_t st) {
     vertices_from_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, S, X);
+}
+void launch_mass_partials_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                                cudaStream_t st) {
+    mass_partials_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, S, X);
 }
 void launch_mass_mixed(const DevMesh &M, const DevState &S, const DevMixed &X, double *out,
                        cudaStream_t st) {

@@ -86,8 +86,9 @@ enum swgpu_boundary_type {
     SWGPU_BC_INFLOW_HYDROGRAPH = 5 /* triangular hydrograph of unit discharge
                                     q(t) (p0 peak in m^2/s, p1 rise, p2 fall,
                                     p3 start time) entering along the inward
-                                    normal at critical depth (q^2/g)^(1/3)
-                                    above the edge bed; no reference
+                                    normal; stage the inside edge's, or
+                                    critical depth (q^2/g)^(1/3) above the
+                                    edge bed where higher; no reference
                                     counterpart                            */
 };
 
@@ -173,6 +174,36 @@ typedef struct {
  * (gpu_domain_advanced.py:582-903) and equip_kernel_functions (:186-507). */
 int swgpu_create(const swgpu_mesh *mesh, const swgpu_params *params,
                  int precision, void **handle_out);
+
+/* Batched ensemble: nscen independent scenarios in one handle, advanced
+ * together by one device-resident loop (one graph of fused steps over all
+ * of them), each with its own time, timestep, yield/final times and stop
+ * state.  mesh is the scenarios' meshes concatenated: scenario s owns
+ * triangles [scenario_offsets[s], scenario_offsets[s+1]) (offsets[0] = 0,
+ * offsets[nscen] = number_of_elements, every offset a multiple of 256 --
+ * pad a scenario with isolated triangles), its neighbour, surrogate and
+ * boundary indices are global, and no triangle has a neighbour in another
+ * scenario.  Boundary tags and quantities are set with the single-domain
+ * calls on the concatenated arrays.  Per-method calls that reduce a single
+ * timestep (compute_fluxes, update_conserved_quantities) are refused.  No
+ * counterpart in the reference (which runs one domain per process). */
+int swgpu_create_ensemble(const swgpu_mesh *mesh, const int64_t *scenario_offsets, int nscen,
+                          const swgpu_params *params, int precision, void **handle_out);
+
+/* Number of scenarios of a handle (1 for swgpu_create handles). */
+int swgpu_ensemble_size(void *handle, int *nscen);
+
+/* Evolve state of one scenario (swgpu_get_state reads scenario 0). */
+int swgpu_ensemble_get_state(void *handle, int scenario, swgpu_state *state);
+
+/* Per-scenario finaltime (<= 0: none) after swgpu_evolve_start, which gives
+ * every scenario the same one.  swgpu_evolve_run then returns when every
+ * scenario has stopped (final time, yield, step budget or error). */
+int swgpu_ensemble_set_finaltimes(void *handle, const double *finaltimes);
+
+/* Water volume of each scenario, each equal to swgpu_mass of that scenario
+ * run alone. */
+int swgpu_ensemble_mass(void *handle, double *masses);
 
 /* Frees everything the handle owns.  No counterpart in the reference (its
  * PyCUDA allocations are released by the garbage collector). */

@@ -919,11 +919,12 @@ void swcpu_update_boundary(swcpu_domain *D)
             D->ymom_boundary_values[m] = 0.0;
         } else if (T->type == SWCPU_BC_INFLOW_HYDROGRAPH) {
             /* triangular hydrograph of unit discharge q(t) entering through
-             * the edge at critical depth (q^2/g)^(1/3) above the edge bed */
+             * the edge: stage the inside edge's, or critical depth
+             * (q^2/g)^(1/3) above the edge bed where that is higher */
             const double q = swcpu_hydrograph(T->p, D->time);
             const double h = cbrt(q * q / D->params->g);
             const double n1 = D->normals[2 * ki], n2 = D->normals[2 * ki + 1];
-            D->stage_boundary_values[m] = D->bed_edge_values[ki] + h;
+            D->stage_boundary_values[m] = omax(D->stage_edge_values[ki], D->bed_edge_values[ki] + h);
             D->xmom_boundary_values[m] = -q * n1;
             D->ymom_boundary_values[m] = -q * n2;
         } else {

@@ -378,14 +378,25 @@ def inflow_harbour(target_triangles=45000, seed=4, peak=200.0, rise=900.0, frict
                     "wall": Reflective_boundary()}, finaltime=3600.0)
 
 
-def ensemble_harbours(count=256, seed=4, nmin=5000, nmax=200000):
+def _inflow_harbour_args(args):
+    i, seed, n, p, r, f = args
+    return inflow_harbour(int(n), seed=int(seed * 100003 + i), peak=p, rise=r, friction=f)
+
+
+def ensemble_harbours(count=256, seed=4, nmin=5000, nmax=200000, processes=1):
     """Ensemble scenarios: ``count`` inflow harbours with triangle counts
     log-uniform in [nmin, nmax], hydrograph peak U[50, 500] m^3/s, rise
-    U[300, 1800] s and Manning n U[0.01, 0.05], all drawn from ``seed``."""
+    U[300, 1800] s and Manning n U[0.01, 0.05], all drawn from ``seed``.
+    ``processes`` > 1 builds the meshes in a pool of spawned processes."""
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), count))
     peaks = rng.uniform(50.0, 500.0, count)
     rises = rng.uniform(300.0, 1800.0, count)
     frics = rng.uniform(0.01, 0.05, count)
-    return [inflow_harbour(int(n), seed=int(seed * 100003 + i), peak=p, rise=r, friction=f)
-            for i, (n, p, r, f) in enumerate(zip(sizes, peaks, rises, frics))]
+    args = [(i, seed, n, p, r, f) for i, (n, p, r, f) in
+            enumerate(zip(sizes, peaks, rises, frics))]
+    if processes and processes > 1 and count > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(processes, count)) as pool:
+            return pool.map(_inflow_harbour_args, args, chunksize=1)
+    return [_inflow_harbour_args(a) for a in args]

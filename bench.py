@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--cells", type=int, default=1000, help="rectangular_cross cells per side")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--ensemble", type=int, default=32,
+                    help="scenarios of the batched-ensemble measurement (0: skip)")
+    ap.add_argument("--ensemble-finaltime", type=float, default=3600.0)
     return ap.parse_args()
 
 
@@ -251,6 +254,36 @@ def run_ours(args, rank, world, local, sc):
     return out
 
 
+def run_ensemble(count, finaltime):
+    """Batched ensemble of inflow harbours (N log-uniform in [5k, 200k],
+    hydrograph peak U[50, 500] m^3/s, rise U[300, 1800] s, Manning n
+    U[0.01, 0.05]; seed 4), mixed precision, every scenario from rest to
+    ``finaltime``; device time of the whole run (CUDA events around the
+    graph launches)."""
+    import numpy as np
+    from anuga_cuda import DEFAULT, scenarios
+    from anuga_cuda.ensemble import Ensemble
+    t0 = time.perf_counter()
+    scs = scenarios.ensemble_harbours(count, seed=4, processes=os.cpu_count() or 1)
+    gen_s = time.perf_counter() - t0
+    ens = Ensemble(scs, DEFAULT, "mixed")
+    ms = ens.run_timed(finaltime)
+    st = ens.states()
+    steps = np.array([s.total_steps for s in st], dtype=np.float64)
+    n = np.array([sc.N for sc in scs], dtype=np.float64)
+    done = sum(1 for s in st if s.status == 0 and abs(s.time - finaltime) <= 1e-9 * finaltime)
+    return {"metric": "ensemble runs/s", "value": done / (ms / 1000.0), "unit": "runs/s",
+            "higher_is_better": True, "scenarios": count, "completed": done,
+            "finaltime_s": finaltime, "wall_s": ms / 1000.0, "precision": "mixed",
+            "triangles_total": int(n.sum()), "steps_min": int(steps.min()),
+            "steps_max": int(steps.max()),
+            "triangle_steps_per_s": float((n * steps).sum() / (ms / 1000.0)),
+            "generation_s": gen_s,
+            "workload": f"{count} inflow harbours (2 km x 1 km, Delaunay of jittered lattice, "
+                        "GRF bed), N log-uniform [5k, 200k], triangular hydrograph "
+                        "peak U[50,500] m3/s rise U[300,1800] s, n U[0.01,0.05], seed 4"}
+
+
 def cpu_oracle_rate(sc, seconds=12.0, warm_steps=1):
     """Serial CPU oracle on the same workload for a bounded time."""
     from anuga_cuda import DEFAULT
@@ -375,6 +408,8 @@ def main():
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": f"{steps} Euler steps of the full {N}-triangle mesh "
                                           f"({wall:.1f} s) on one core"}
+    if args.ensemble > 0:
+        line["ensemble"] = run_ensemble(args.ensemble, args.ensemble_finaltime)
     print(json.dumps(line))
 
 

@@ -14,7 +14,8 @@ import numpy as np
 from ._build import library_path
 
 __all__ = [
-    "lib", "SwgpuError", "Mesh_t", "Params_t", "State_t", "BoundaryTag_t", "check",
+    "lib", "SwgpuError", "Mesh_t", "Params_t", "State_t", "BoundaryTag_t", "LaunchConfig_t",
+    "check",
     "STAGE", "XMOMENTUM", "YMOMENTUM", "ELEVATION", "FRICTION", "HEIGHT", "XVELOCITY",
     "YVELOCITY", "FP64", "MIXED", "BC_REFLECTIVE", "BC_DIRICHLET", "BC_TIME_STAGE_SINE",
     "BC_TRANSMISSIVE", "BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM", "BC_INFLOW_HYDROGRAPH",
@@ -71,7 +72,7 @@ PARAM_FIELDS = [
     ("optimise_dry_cells", C.c_int64), ("extrapolate_velocity_second_order", C.c_int64),
     ("use_sloped_mannings", C.c_int64), ("max_smallsteps", C.c_int64),
     ("default_order", C.c_int64), ("optimised_gradient_limiter", C.c_int64),
-    ("use_edge_limiter", C.c_int64),
+    ("use_edge_limiter", C.c_int64), ("flow_algorithm", C.c_int64),
 ]
 
 
@@ -89,6 +90,11 @@ class State_t(C.Structure):
     ]
 
 
+class LaunchConfig_t(C.Structure):
+    _fields_ = [("flux_block", C.c_int32), ("update_block", C.c_int32),
+                ("distribute_block", C.c_int32), ("steps_per_graph", C.c_int32)]
+
+
 class BoundaryTag_t(C.Structure):
     _fields_ = [("type", C.c_int64), ("p", C.c_double * 4)]
 
@@ -100,6 +106,8 @@ _SIGNATURES = [
     ("swgpu_create_ensemble", C.c_int, [C.POINTER(Mesh_t), _i64p, C.c_int,
                                         C.POINTER(Params_t), C.c_int, C.POINTER(_VP)]),
     ("swgpu_ensemble_size", C.c_int, [_VP, C.POINTER(C.c_int)]),
+    ("swgpu_get_launch_config", C.c_int, [_VP, C.POINTER(LaunchConfig_t)]),
+    ("swgpu_set_launch_config", C.c_int, [_VP, C.POINTER(LaunchConfig_t)]),
     ("swgpu_ensemble_get_state", C.c_int, [_VP, C.c_int, C.POINTER(State_t)]),
     ("swgpu_ensemble_set_finaltimes", C.c_int, [_VP, _f64p]),
     ("swgpu_ensemble_mass", C.c_int, [_VP, _f64p]),
@@ -111,6 +119,7 @@ _SIGNATURES = [
     ("swgpu_get_boundary_values", C.c_int, [_VP, C.c_int, _f64p]),
     ("swgpu_get_explicit_update", C.c_int, [_VP, C.c_int, _f64p]),
     ("swgpu_get_semi_implicit_update", C.c_int, [_VP, C.c_int, _f64p]),
+    ("swgpu_get_max_speed", C.c_int, [_VP, _f64p]),
     ("swgpu_set_boundary_tags", C.c_int, [_VP, C.POINTER(BoundaryTag_t), C.c_int]),
     ("swgpu_protect", C.c_int, [_VP]),
     ("swgpu_distribute_to_vertices_and_edges", C.c_int, [_VP]),

@@ -37,6 +37,7 @@ class Parameters:
     default_order: int = 2
     optimised_gradient_limiter: int = 1
     use_edge_limiter: int = 0
+    flow_algorithm: int = 0            # 1: ANUGA's 'tsunami' distribute
 
     def replace(self, **kw) -> "Parameters":
         return dataclasses.replace(self, **kw)

@@ -157,6 +157,7 @@ class GPU_domain:
         self.yieldstep = None
         self.finaltime = None
         self._timestepping_method = "euler"
+        self.protect_against_isolated_degenerate_timesteps = False
         self.name = "domain"
         self.datadir = "."
         self.store = False
@@ -433,9 +434,43 @@ class GPU_domain:
 
     manning_friction_implicit = compute_forcing_terms
 
+    @property
+    def max_speed(self):
+        """Per-triangle max_speed of the last compute_fluxes (FP64)."""
+        out = np.empty(self.number_of_elements)
+        check(lib().swgpu_get_max_speed(self._h, f64p(out)), self._h)
+        return self._to_user(out)
+
+    def apply_protection_against_isolated_degenerate_timesteps(self):
+        """gpu_domain_advanced.py:914-951: when the fastest triangle exceeds
+        10 m/s and stands alone at the top of a 10-bin histogram of max_speed
+        (bins 4..8 empty), zero the momentum of the triangles above the last
+        bin edge.  Bins and counts as ANUGA's numerical_tools.create_bins /
+        histogram: edges arange(min, max, (max-min)/10), counts between
+        consecutive edges of the sorted speeds, the last bin open-ended."""
+        if not self.protect_against_isolated_degenerate_timesteps:
+            return
+        ms = self.max_speed
+        if ms.max() < 10.0:
+            return
+        mx, mn = float(ms.max()), float(ms.min())
+        bins = np.array([mn]) if mx == mn else np.arange(mn, mx, (mx - mn) / 10.0)
+        n = np.searchsorted(np.sort(ms), bins)
+        hist = np.diff(np.concatenate([n, [len(ms)]]))
+        if len(hist) > 1 and hist[-1] > 0 and (hist[4:9] == 0).all():
+            sel = ms > bins[-1]
+            for name in ("xmomentum", "ymomentum"):
+                q = self.quantities[name]
+                c, v, e = q.centroid_values, q.vertex_values, q.edge_values
+                c[sel] = 0.0
+                self._upload(name, self._to_internal(c), self._to_internal(v),
+                             self._to_internal(e))
+
     def update_timestep(self, yieldstep, finaltime):
         """Generic_Domain.update_timestep (restated in
-        src/anuga_HMPP/evolve.c:115-160) on the device-held time state."""
+        src/anuga_HMPP/evolve.c:115-160) on the device-held time state,
+        after the degenerate-timestep protection when it is switched on."""
+        self.apply_protection_against_isolated_degenerate_timesteps()
         p = self.parameters
         s = self._state()
         dt = min(p.CFL * self.flux_timestep, p.evolve_max_timestep)
@@ -545,6 +580,10 @@ class GPU_domain:
         ``max_steps`` (added) stops after that many steps in total."""
         if finaltime is not None and duration is not None:
             raise ValueError("give finaltime or duration, not both")
+        if self.protect_against_isolated_degenerate_timesteps:
+            raise NotImplementedError(
+                "the degenerate-timestep protection runs on the host between per-method "
+                "steps (evolve_one_euler_step); the device-resident evolve does not call it")
         start = self.starttime
         if duration is not None:
             finaltime = start + float(duration)

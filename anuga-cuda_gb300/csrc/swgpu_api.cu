@@ -8,6 +8,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -205,7 +206,7 @@ static int build_graph(Handle *h) {
     if (h->graph) return SWGPU_OK;
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < kStepsPerGraph; s++) issue_step(h);
+    for (int s = 0; s < h->steps_per_graph; s++) issue_step(h);
     CK(cudaStreamEndCapture(h->stream, &g));
     cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
@@ -256,6 +257,20 @@ int swgpu_device_info(char *buf, int buflen) {
         snprintf(buf, buflen, "%s sm_%d%d, %d SMs, %.1f GB (libswgpu %d)", p.name, p.major,
                  p.minor, p.multiProcessorCount, p.totalGlobalMem / 1e9, SWGPU_ABI_VERSION);
     return SWGPU_OK;
+}
+
+// Blocks of each scenario in one launch of each fused-step kernel (the
+// last-block-done counts) for the handle's launch shape.
+static void set_block_counts(Handle *h) {
+    for (int i = 0; i < h->nscen; i++) {
+        const int64_t n =
+            h->nscen > 1 ? h->scen_offsets[i + 1] - h->scen_offsets[i] : (int64_t)h->M.N;
+        Ctrl *c = &h->h_ctrl[i];
+        c->blocks_flux = (unsigned)((n + h->M.shape.flux - 1) / h->M.shape.flux);
+        c->blocks_update = (unsigned)((n + h->M.shape.update - 1) / h->M.shape.update);
+        c->blocks_distribute =
+            (unsigned)((n + h->M.shape.distribute - 1) / h->M.shape.distribute);
+    }
 }
 
 // Shared by swgpu_create (offsets == nullptr, one scenario) and
@@ -554,6 +569,7 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     P.use_sloped_mannings = (int)params->use_sloped_mannings;
     P.max_smallsteps = (int)params->max_smallsteps;
     P.default_order = (int)params->default_order;
+    P.flow_algorithm = params->flow_algorithm ? 1 : 0;
     P.limiter = params->use_edge_limiter ? kLimiterEdge
                 : params->optimised_gradient_limiter ? kLimiterOptimised
                                                      : kLimiterVertex;
@@ -574,6 +590,12 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     P.f_beta_vh_dry = (float)P.beta_vh_dry;
     if (!(P.evolve_max_timestep > 0) || (P.default_order != 1 && P.default_order != 2)) {
         fail(h, SWGPU_EINVAL, "evolve_max_timestep must be > 0 and default_order 1 or 2");
+        g_create_error = h->err;
+        swgpu_destroy(h);
+        return SWGPU_EINVAL;
+    }
+    if (P.flow_algorithm != 0 && precision != SWGPU_FP64) {
+        fail(h, SWGPU_EINVAL, "the 'tsunami' flow algorithm runs in FP64 precision only");
         g_create_error = h->err;
         swgpu_destroy(h);
         return SWGPU_EINVAL;
@@ -615,10 +637,9 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     }
     std::memset(h->h_ctrl, 0, sizeof(Ctrl) * h->nscen);
     std::memset(h->h_summary, 0, sizeof(RunSummary));
-    const int flux_tile = precision == SWGPU_MIXED ? 128 : kBlock;
+    M.shape = LaunchShape{precision == SWGPU_MIXED ? 128 : kBlock, kBlock, kBlock};
     for (int i = 0; i < h->nscen; i++) {
         Ctrl *c = &h->h_ctrl[i];
-        const int64_t n = offsets ? offsets[i + 1] - offsets[i] : N;
         c->order = P.default_order;
         c->finaltime = -1.0;
         c->yieldtime = 1.0e300;
@@ -627,11 +648,10 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         c->rec_max = P.evolve_min_timestep;
         c->rec_min = P.evolve_max_timestep;
         c->budget = -1;
-        c->blocks_flux = (unsigned)((n + flux_tile - 1) / flux_tile);
-        c->blocks_256 = (unsigned)((n + kBlock - 1) / kBlock);
         c->summary = h->d_summary;
         reset_ftmin(c, P);
     }
+    set_block_counts(h);
     TRY(push_ctrl(h));
     TRY(upload(h, h->d_summary, h->h_summary, 1));
     if (precision == SWGPU_MIXED) TRY(build_mixed_geometry(h) ? fail(h, SWGPU_ECUDA, "mixed geometry upload") : SWGPU_OK);
@@ -743,7 +763,9 @@ int swgpu_get_quantity(void *handle, int q, double *centroid, double *vertex, do
         launch_vertices_from_mixed(h->M, h->S, h->X, h->stream);
         if ((rc = check_launch(h, "mixed vertex values"))) return rc;
     }
-    if ((vertex || edge) && q <= SWGPU_YMOMENTUM) {
+    // the 'tsunami' distribute stores its extrapolated edge values, which are
+    // not the interpolation of the vertex values
+    if ((vertex || edge) && q <= SWGPU_YMOMENTUM && !h->P.flow_algorithm) {
         launch_interpolate_fp64(h->M, h->S, h->stream);
         if ((rc = check_launch(h, "interpolate"))) return rc;
     }
@@ -824,6 +846,14 @@ int swgpu_get_explicit_update(void *handle, int q, double *out) {
                                                  : q == SWGPU_YMOMENTUM ? h->S.evh : nullptr;
     if (!src || !out) return fail(h, SWGPU_EINVAL, "bad quantity or null output");
     return download(h, out, src, (size_t)h->M.N);
+}
+
+int swgpu_get_max_speed(void *handle, double *out) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "max_speed");
+    if (rc) return rc;
+    if (!out) return fail(h, SWGPU_EINVAL, "null output");
+    return download(h, out, h->S.max_speed, (size_t)h->M.N);
 }
 
 int swgpu_get_semi_implicit_update(void *handle, int q, double *out) {
@@ -1037,6 +1067,46 @@ int swgpu_ensemble_mass(void *handle, double *masses) {
     return SWGPU_OK;
 }
 
+int swgpu_get_launch_config(void *handle, swgpu_launch_config *cfg) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !cfg) return fail(h, SWGPU_EINVAL, "null argument");
+    cfg->flux_block = h->M.shape.flux;
+    cfg->update_block = h->M.shape.update;
+    cfg->distribute_block = h->M.shape.distribute;
+    cfg->steps_per_graph = h->steps_per_graph;
+    return SWGPU_OK;
+}
+
+int swgpu_set_launch_config(void *handle, const swgpu_launch_config *cfg) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h || !cfg) return fail(h, SWGPU_EINVAL, "null argument");
+    auto one_of = [](int v, std::initializer_list<int> ok) {
+        for (int x : ok)
+            if (v == x) return true;
+        return false;
+    };
+    // an ensemble scenario starts on a 256-triangle boundary: no block may
+    // straddle two scenarios
+    const int top = h->nscen > 1 ? 256 : 512;
+    if (!one_of(cfg->flux_block, {64, 128, 256}) ||
+        !one_of(cfg->update_block, {128, 256, 512}) ||
+        !one_of(cfg->distribute_block, {128, 256, 512}) || cfg->update_block > top ||
+        cfg->distribute_block > top || cfg->steps_per_graph < 1 || cfg->steps_per_graph > 64)
+        return fail(h, SWGPU_EINVAL,
+                    "launch config: flux 64/128/256, update and distribute 128/256/512 "
+                    "(at most 256 for an ensemble), 1..64 steps per graph");
+    int rc = sync_ctrl(h);
+    if (rc) return rc;
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;  // recaptured with the new shape on the next run
+    }
+    h->M.shape = LaunchShape{cfg->flux_block, cfg->update_block, cfg->distribute_block};
+    h->steps_per_graph = cfg->steps_per_graph;
+    set_block_counts(h);
+    return push_ctrl(h);
+}
+
 int swgpu_ensemble_size(void *handle, int *nscen) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h || !nscen) return fail(h, SWGPU_EINVAL, "null argument");
@@ -1220,7 +1290,7 @@ static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *
     // with a step budget the device stops itself after max_steps steps, so
     // exactly ceil(max_steps / steps-per-graph) graphs are launched
     const int64_t max_graphs =
-        max_steps > 0 ? (max_steps + kStepsPerGraph - 1) / kStepsPerGraph : INT64_MAX;
+        max_steps > 0 ? (max_steps + h->steps_per_graph - 1) / h->steps_per_graph : INT64_MAX;
     cudaError_t e = cudaSuccess;
     int inflight = 0, slot = 0;
     bool halted = false;

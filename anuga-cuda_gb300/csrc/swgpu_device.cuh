@@ -178,8 +178,9 @@ __device__ __forceinline__ void publish_step_clock(Ctrl *c, const DevParams &P) 
 // pattern (positive IEEE doubles order like their bits) only when it lowers
 // the running minimum.  In the fused loop the last block then publishes the
 // step's clock.
+template <int BLOCK = kBlock>
 __device__ __forceinline__ void block_min_timestep(double t, Ctrl *ctrl) {
-    __shared__ double wmin[kBlock / 32];
+    __shared__ double wmin[BLOCK / 32];
     for (int o = 16; o > 0; o >>= 1) t = omin(t, __shfl_xor_sync(0xffffffffu, t, o));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) wmin[warp] = t;

@@ -129,10 +129,16 @@ __device__ __forceinline__ EdgeFlux edge_flux(const DevMesh &M, const DevState &
     if (pk >= 0) {
         n = pk >> 2;
         const int m = pk & 3;
-        const int a = (m == 0) ? 1 : 0, b = (m == 2) ? 1 : 2;  // the other two vertices of n
-        wr = 0.5 * (S.wv[a * N + n] + S.wv[b * N + n]);
-        uhr = 0.5 * (S.uhv[a * N + n] + S.uhv[b * N + n]);
-        vhr = 0.5 * (S.vhv[a * N + n] + S.vhv[b * N + n]);
+        if (P.flow_algorithm) {
+            wr = S.we[m * N + n];
+            uhr = S.uhe[m * N + n];
+            vhr = S.vhe[m * N + n];
+        } else {
+            const int a = (m == 0) ? 1 : 0, b = (m == 2) ? 1 : 2;  // the other two vertices
+            wr = 0.5 * (S.wv[a * N + n] + S.wv[b * N + n]);
+            uhr = 0.5 * (S.uhv[a * N + n] + S.uhv[b * N + n]);
+            vhr = 0.5 * (S.vhv[a * N + n] + S.vhv[b * N + n]);
+        }
         zr = S.ze[m * N + n];
     } else {
         const int mb = -pk - 1;
@@ -185,7 +191,8 @@ __device__ __forceinline__ void pick(int i, const EdgeFlux &a, const EdgeFlux &b
 // neighbour index, then its remaining edges by edge index.  The central
 // flux is exactly antisymmetric in IEEE arithmetic, so -flux(k,i) equals
 // the +flux(n,m) that ANUGA's edge loop adds, and the sums agree bitwise.
-__global__ void __launch_bounds__(kBlock) flux_fp64(DevMesh M, DevState S, DevParams P,
+template <int BS>
+__global__ void __launch_bounds__(BS) flux_fp64(DevMesh M, DevState S, DevParams P,
                                                     Ctrl *ctrl, int flags) {
     ctrl = block_ctrl(ctrl, M);
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
@@ -204,16 +211,26 @@ __global__ void __launch_bounds__(kBlock) flux_fp64(DevMesh M, DevState S, DevPa
             vv[i] = S.vhv[i * N + k];
             ez[i] = S.ze[i * N + k];
         }
-        // quantity.c:687-706 (_interpolate_from_vertices_to_edges)
-        ew[0] = 0.5 * (vw[1] + vw[2]);
-        ew[1] = 0.5 * (vw[0] + vw[2]);
-        ew[2] = 0.5 * (vw[0] + vw[1]);
-        euh[0] = 0.5 * (vu[1] + vu[2]);
-        euh[1] = 0.5 * (vu[0] + vu[2]);
-        euh[2] = 0.5 * (vu[0] + vu[1]);
-        evh[0] = 0.5 * (vv[1] + vv[2]);
-        evh[1] = 0.5 * (vv[0] + vv[2]);
-        evh[2] = 0.5 * (vv[0] + vv[1]);
+        if (P.flow_algorithm) {
+            // 'tsunami': the extrapolated edge values themselves
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                ew[i] = S.we[i * N + k];
+                euh[i] = S.uhe[i * N + k];
+                evh[i] = S.vhe[i * N + k];
+            }
+        } else {
+            // quantity.c:687-706 (_interpolate_from_vertices_to_edges)
+            ew[0] = 0.5 * (vw[1] + vw[2]);
+            ew[1] = 0.5 * (vw[0] + vw[2]);
+            ew[2] = 0.5 * (vw[0] + vw[1]);
+            euh[0] = 0.5 * (vu[1] + vu[2]);
+            euh[1] = 0.5 * (vu[0] + vu[2]);
+            euh[2] = 0.5 * (vu[0] + vu[1]);
+            evh[0] = 0.5 * (vv[1] + vv[2]);
+            evh[1] = 0.5 * (vv[0] + vv[2]);
+            evh[2] = 0.5 * (vv[0] + vv[1]);
+        }
 
         double ms_own = 0.0;
         const EdgeFlux F0 = edge_flux<0>(M, S, P, k, ew, euh, evh, ez, h0, lim, t, ms_own, bad);
@@ -271,7 +288,7 @@ __global__ void __launch_bounds__(kBlock) flux_fp64(DevMesh M, DevState S, DevPa
     }
     if (bad) set_status(ctrl, SWGPU_EBED);
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
-    block_min_timestep(t, ctrl);
+    block_min_timestep<BS>(t, ctrl);
     if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
         publish_step_clock(ctrl, P);
 }
@@ -328,6 +345,31 @@ __global__ void __launch_bounds__(kBlock) forcing_fp64(DevMesh M, DevState S, De
 }
 
 // src/anuga_HMPP/shallow_water_ext.c:1638-1705 (_protect) on one triangle.
+// The 'tsunami' protection (src/anuga_cuda/protect/protect.cu:64-131) of
+// triangle k: below max(0.1 (max bed edge - bed centroid), mah) momentum is
+// zeroed; a non-positive depth lifts stage to the lowest bed vertex minus
+// mah.  Returns the lifted stage floor bmin (or -inf) for the vertex clamp.
+__device__ __forceinline__ double protect_swb2_one(const DevParams &P, double zc,
+                                                   const double (&zv)[3], double &w, double &uh,
+                                                   double &vh) {
+    const double mah = P.minimum_allowed_height;
+    const double hc = w - zc;
+    const double bmax = 0.5 * fmax(zv[0] + zv[1], fmax(zv[1] + zv[2], zv[2] + zv[0]));
+    double floor_w = -pos_inf();
+    if (hc < fmax(0.1 * (bmax - zc), mah)) {
+        uh = 0.0;
+        vh = 0.0;
+        if (hc <= 0.0) {
+            const double bmin = fmin(zv[0], fmin(zv[1], zv[2])) - mah;
+            if (w < bmin) {
+                w = fmax(w, bmin);
+                floor_w = bmin;
+            }
+        }
+    }
+    return floor_w;
+}
+
 __device__ __forceinline__ void protect_one(const DevParams &P, double zc, double &w, double &uh,
                                             double &vh) {
     const double hc = w - zc;
@@ -367,7 +409,8 @@ __device__ __forceinline__ bool semi_update(double &c, double e, double semi, do
 // the centroids in between) and the centroid velocities the next
 // extrapolation reads.  API: dt given, semi-implicit terms from
 // compute_forcing_terms, no protect.
-__global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, DevParams P,
+template <int BS>
+__global__ void __launch_bounds__(BS) update_fp64(DevMesh M, DevState S, DevParams P,
                                                       Ctrl *ctrl, double dt_api, int flags,
                                                       Stage stg) {
     const bool fused = flags & kFused;
@@ -419,7 +462,14 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
         }
         if (fused) {
             const double zc = S.zc[k];
-            protect_one(P, zc, w, uh, vh);
+            if (P.flow_algorithm) {
+                // the stage vertex clamp of protect_swb2 is overwritten by the
+                // extrapolation that follows in the same step
+                const double zv[3] = {S.zv[k], S.zv[M.N + k], S.zv[2 * M.N + k]};
+                protect_swb2_one(P, zc, zv, w, uh, vh);
+            } else {
+                protect_one(P, zc, w, uh, vh);
+            }
             if (P.extrapolate_velocity_second_order == 1) {
                 const double dk = omax(w - zc, P.minimum_allowed_height);
                 S.uvel[k] = uh / dk;
@@ -437,7 +487,7 @@ __global__ void __launch_bounds__(kBlock) update_fp64(DevMesh M, DevState S, Dev
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (fused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_256))
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_update))
             commit_stage(ctrl, clk, P, stg);
     }
 }
@@ -462,10 +512,20 @@ __global__ void __launch_bounds__(kBlock) saxpy_fp64(int N, double a, double b, 
 // extrapolate_velocity_second_order_true, extrapolate_second_order_sw.cu:77-104).
 __global__ void __launch_bounds__(kBlock) prepare_fp64(DevMesh M, DevState S, DevParams P) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= M.N) return;
+    const int N = M.N;
+    if (k >= N) return;
     double w = S.w[k], uh = S.uh[k], vh = S.vh[k];
     const double zc = S.zc[k];
-    protect_one(P, zc, w, uh, vh);
+    if (P.flow_algorithm) {
+        const double zv[3] = {S.zv[k], S.zv[N + k], S.zv[2 * N + k]};
+        const double floor_w = protect_swb2_one(P, zc, zv, w, uh, vh);
+        if (floor_w > -pos_inf()) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) S.wv[i * N + k] = fmax(S.wv[i * N + k], floor_w);
+        }
+    } else {
+        protect_one(P, zc, w, uh, vh);
+    }
     S.w[k] = w;
     S.uh[k] = uh;
     S.vh[k] = vh;
@@ -562,6 +622,181 @@ __device__ __forceinline__ void one_nbr_jumps(double qk, double q1, double dx2, 
     for (int i = 0; i < 3; i++) out[i] = qk + d[i];
 }
 
+// The 'tsunami' distribute (gpu_domain_advanced.py:1755-1812): the edge
+// extrapolation of src/anuga_HMPP/shallow_water_ext.c:3328-3964
+// (_extrapolate_second_order_edge_sw) after protect_swb2 (applied by the
+// update kernel or prepare_fp64): limited auxiliary-triangle gradients
+// evaluated at the edge midpoints, dry surrogate neighbours replaced by the
+// triangle itself, beta fully wet or dry, vertex values from the edge values
+// (v_i = e_j + e_k - e_i), momenta back from velocities with the edge and
+// vertex depths; cells skipped as dry keep their previous edge values.  Edge
+// values are always stored (the flux reads them), then the boundary values.
+template <int BS>
+__global__ void __launch_bounds__(BS) distribute_de_fp64(DevMesh M, DevState S, DevParams P,
+                                                         const BcTag *tags, Ctrl *ctrl,
+                                                         int flags) {
+    const bool fused = flags & kFused;
+    ctrl = block_ctrl(ctrl, M);
+    if (fused && ctrl_halted(ctrl)) return;
+    const int N = M.N;
+    const double time = ctrl->time;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int bad_bc = 0, no_nbr = 0;
+    if (k < N) {
+        const bool vel = P.extrapolate_velocity_second_order == 1;
+        const double *U = vel ? S.uvel : S.uh;  // extrapolated centroid values
+        const double *V = vel ? S.vvel : S.vh;
+        const double wk = S.w[k], uk = U[k], vk = V[k];
+        const int nbk = M.nb[k];
+        double ew[3], eu[3], ev[3];
+        bool flat = false, keep = false;
+        if (nbk == 3) {
+            flat = true;
+        } else {
+            const double x = M.cxy[k], y = M.cxy[N + k];
+            double vx[3], vy[3], dxv[3], dyv[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                vx[i] = M.vxy[(2 * i) * N + k];
+                vy[i] = M.vxy[(2 * i + 1) * N + k];
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const int a = (i + 1) % 3, b = (i + 2) % 3;
+                dxv[i] = 0.5 * (vx[a] + vx[b]) - x;  // edge midpoint offsets
+                dyv[i] = 0.5 * (vy[a] + vy[b]) - y;
+            }
+            if (nbk <= 1) {
+                int k0 = M.surr[k], k1 = M.surr[N + k], k2 = M.surr[2 * N + k];
+                if (S.w[k2] <= S.zc[k2]) k2 = k;
+                if (S.w[k0] <= S.zc[k0]) k0 = k;
+                if (S.w[k1] <= S.zc[k1]) k1 = k;
+                const double x0 = M.cxy[k0], y0 = M.cxy[N + k0];
+                const double dx1 = M.cxy[k1] - x0, dx2 = M.cxy[k2] - x0;
+                const double dy1 = M.cxy[N + k1] - y0, dy2 = M.cxy[N + k2] - y0;
+                const double area2 = dy2 * dx1 - dy1 * dx2;
+                if (area2 <= 0) {
+                    flat = true;
+                } else {
+                    const double hc = wk - S.zc[k];
+                    const double h0 = S.w[k0] - S.zc[k0];
+                    const double h1 = S.w[k1] - S.zc[k1];
+                    const double h2 = S.w[k2] - S.zc[k2];
+                    const double hmin = omin(omin(h0, omin(h1, h2)), hc);
+                    const double hfactor = hmin > 0.0 ? 1.0 : 0.0;
+                    if (P.optimise_dry_cells && omax(h0, omax(h1, h2)) < P.epsilon) {
+                        keep = true;
+                    } else {
+                        const double inv_area2 = 1.0 / area2;
+                        aux_jumps(wk, S.w[k0], S.w[k1], S.w[k2], dx1, dy1, dx2, dy2, inv_area2,
+                                  dxv, dyv, P.beta_w_dry + (P.beta_w - P.beta_w_dry) * hfactor,
+                                  ew);
+                        aux_jumps(uk, U[k0], U[k1], U[k2], dx1, dy1, dx2, dy2, inv_area2, dxv,
+                                  dyv, P.beta_uh_dry + (P.beta_uh - P.beta_uh_dry) * hfactor,
+                                  eu);
+                        aux_jumps(vk, V[k0], V[k1], V[k2], dx1, dy1, dx2, dy2, inv_area2, dxv,
+                                  dyv, P.beta_vh_dry + (P.beta_vh - P.beta_vh_dry) * hfactor,
+                                  ev);
+                    }
+                }
+            } else {
+                int k1 = -1;
+#pragma unroll
+                for (int i = 2; i >= 0; i--) {
+                    const int sn = M.surr[i * N + k];
+                    if (sn != k) k1 = sn;
+                }
+                if (k1 < 0) {
+                    no_nbr = 1;
+                    flat = true;
+                } else {
+                    const double dx1 = M.cxy[k1] - x, dy1 = M.cxy[N + k1] - y;
+                    const double area2 = dx1 * dx1 + dy1 * dy1;
+                    double dx2 = 1.0 / area2;
+                    const double dy2 = dx2 * dy1;
+                    dx2 *= dx1;
+                    one_nbr_jumps(wk, S.w[k1], dx2, dy2, dxv, dyv, P.beta_w, ew);
+                    one_nbr_jumps(uk, U[k1], dx2, dy2, dxv, dyv, P.beta_w, eu);
+                    one_nbr_jumps(vk, V[k1], dx2, dy2, dxv, dyv, P.beta_w, ev);
+                }
+            }
+        }
+        if (flat) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                ew[i] = wk;
+                eu[i] = uk;
+                ev[i] = vk;
+            }
+        } else if (keep) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                ew[i] = S.we[i * N + k];
+                eu[i] = S.uhe[i * N + k];
+                ev[i] = S.vhe[i * N + k];
+            }
+        }
+        double ow[3], ou[3], ov[3];
+        ow[0] = ew[1] + ew[2] - ew[0];
+        ow[1] = ew[0] + ew[2] - ew[1];
+        ow[2] = ew[0] + ew[1] - ew[2];
+        ou[0] = eu[1] + eu[2] - eu[0];
+        ou[1] = eu[0] + eu[2] - eu[1];
+        ou[2] = eu[0] + eu[1] - eu[2];
+        ov[0] = ev[1] + ev[2] - ev[0];
+        ov[1] = ev[0] + ev[2] - ev[1];
+        ov[2] = ev[0] + ev[1] - ev[2];
+        if (vel) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const double de = omax(ew[i] - S.ze[i * N + k], 0.0);
+                eu[i] = eu[i] * de;
+                ev[i] = ev[i] * de;
+                const double dv = omax(ow[i] - S.zv[i * N + k], 0.0);
+                ou[i] = ou[i] * dv;
+                ov[i] = ov[i] * dv;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            S.we[i * N + k] = ew[i];
+            S.uhe[i * N + k] = eu[i];
+            S.vhe[i * N + k] = ev[i];
+            S.wv[i * N + k] = ow[i];
+            S.uhv[i * N + k] = ou[i];
+            S.vhv[i * N + k] = ov[i];
+        }
+        if ((flags & kWriteBoundary) && nbk > 0) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const int pk = M.nbr[i * N + k];
+                if (pk < 0) {
+                    const int mb = -pk - 1;
+                    const double ze = S.ze[i * N + k];
+                    double wb, uhb, vhb;
+                    if (!eval_boundary(tags[M.btag[mb]], time, ew[i], eu[i], ev[i],
+                                       M.normals[(2 * i) * N + k],
+                                       M.normals[(2 * i + 1) * N + k], ze, P.g, wb, uhb, vhb)) {
+                        bad_bc = 1;
+                        wb = uhb = vhb = 0.0;
+                    }
+                    S.wb[mb] = wb;
+                    S.uhb[mb] = uhb;
+                    S.vhb[mb] = vhb;
+                    S.zb[mb] = ze;
+                }
+            }
+        }
+    }
+    if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
+    if (no_nbr) set_status(ctrl, SWGPU_EMESH);
+    if (fused) {
+        __syncthreads();
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_distribute))
+            apply_pending_halt(ctrl);
+    }
+}
+
 // distribute_to_vertices_and_edges for triangle k: extrapolation of the
 // current order (src/anuga_HMPP/shallow_water_ext.c:2717-3324 or
 // extrapolate_first_order.cu:3-30), balance_deep_and_shallow
@@ -651,7 +886,8 @@ __device__ __forceinline__ bool limit_by_neighbours(const DevMesh &M, const doub
     return ok;
 }
 
-__global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S, DevParams P,
+template <int BS>
+__global__ void __launch_bounds__(BS) distribute_fp64(DevMesh M, DevState S, DevParams P,
                                                           const BcTag *tags, Ctrl *ctrl,
                                                           int flags) {
     const bool fused = flags & kFused;
@@ -880,13 +1116,13 @@ __global__ void __launch_bounds__(kBlock) distribute_fp64(DevMesh M, DevState S,
     if (no_nbr) set_status(ctrl, SWGPU_EMESH);
     if (fused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_256)) apply_pending_halt(ctrl);
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_distribute)) apply_pending_halt(ctrl);
     }
 }
 
 // update_boundary as a stand-alone pass over boundary slots, from the
 // stored vertex values (gpu_domain_advanced.py:2006-2108).
-__global__ void __launch_bounds__(kBlock) boundary_fp64(DevMesh M, DevState S, double g,
+__global__ void __launch_bounds__(kBlock) boundary_fp64(DevMesh M, DevState S, DevParams P,
                                                         const BcTag *tags, Ctrl *ctrl) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M.Nb) return;
@@ -894,12 +1130,17 @@ __global__ void __launch_bounds__(kBlock) boundary_fp64(DevMesh M, DevState S, d
     const int k = M.bcell[m], i = M.bedge[m];
     if (M.blk_scen) ctrl += M.blk_scen[k >> 8];  // the owning scenario's time
     const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-    const double we = 0.5 * (S.wv[a * N + k] + S.wv[b * N + k]);
-    const double uhe = 0.5 * (S.uhv[a * N + k] + S.uhv[b * N + k]);
-    const double vhe = 0.5 * (S.vhv[a * N + k] + S.vhv[b * N + k]);
+    // the 'tsunami' distribute stores its edge values; otherwise they are the
+    // interpolation of the vertex values
+    const double we = P.flow_algorithm ? S.we[i * N + k]
+                                       : 0.5 * (S.wv[a * N + k] + S.wv[b * N + k]);
+    const double uhe = P.flow_algorithm ? S.uhe[i * N + k]
+                                        : 0.5 * (S.uhv[a * N + k] + S.uhv[b * N + k]);
+    const double vhe = P.flow_algorithm ? S.vhe[i * N + k]
+                                        : 0.5 * (S.vhv[a * N + k] + S.vhv[b * N + k]);
     double wb, uhb, vhb;
     if (!eval_boundary(tags[M.btag[m]], ctrl->time, we, uhe, vhe, M.normals[(2 * i) * N + k],
-                       M.normals[(2 * i + 1) * N + k], S.ze[i * N + k], g, wb, uhb, vhb)) {
+                       M.normals[(2 * i + 1) * N + k], S.ze[i * N + k], P.g, wb, uhb, vhb)) {
         set_status(ctrl, SWGPU_EBOUNDARY);
         wb = uhb = vhb = 0.0;
     }
@@ -982,18 +1223,38 @@ void launch_prepare_fp64(const DevMesh &M, const DevState &S, const DevParams &P
                          cudaStream_t st) {
     prepare_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P);
 }
+// Block sizes of the fused-step kernels come from M.shape.
 void launch_distribute_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                             const BcTag *tags, Ctrl *ctrl, int flags, cudaStream_t st) {
-    distribute_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P, tags, ctrl, flags);
+    const int bs = M.shape.distribute, g = (M.N + bs - 1) / bs;
+    if (P.flow_algorithm) {
+        if (bs == 128)
+            distribute_de_fp64<128><<<g, 128, 0, st>>>(M, S, P, tags, ctrl, flags);
+        else if (bs == 512)
+            distribute_de_fp64<512><<<g, 512, 0, st>>>(M, S, P, tags, ctrl, flags);
+        else
+            distribute_de_fp64<256><<<g, 256, 0, st>>>(M, S, P, tags, ctrl, flags);
+    } else if (bs == 128)
+        distribute_fp64<128><<<g, 128, 0, st>>>(M, S, P, tags, ctrl, flags);
+    else if (bs == 512)
+        distribute_fp64<512><<<g, 512, 0, st>>>(M, S, P, tags, ctrl, flags);
+    else
+        distribute_fp64<256><<<g, 256, 0, st>>>(M, S, P, tags, ctrl, flags);
 }
 void launch_boundary_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                           const BcTag *tags, Ctrl *ctrl,
                           cudaStream_t st) {
-    if (M.Nb > 0) boundary_fp64<<<grid_for(M.Nb), kBlock, 0, st>>>(M, S, P.g, tags, ctrl);
+    if (M.Nb > 0) boundary_fp64<<<grid_for(M.Nb), kBlock, 0, st>>>(M, S, P, tags, ctrl);
 }
 void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P, Ctrl *ctrl,
                       int flags, cudaStream_t st) {
-    flux_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P, ctrl, flags);
+    const int bs = M.shape.flux, g = (M.N + bs - 1) / bs;
+    if (bs == 64)
+        flux_fp64<64><<<g, 64, 0, st>>>(M, S, P, ctrl, flags);
+    else if (bs == 128)
+        flux_fp64<128><<<g, 128, 0, st>>>(M, S, P, ctrl, flags);
+    else
+        flux_fp64<256><<<g, 256, 0, st>>>(M, S, P, ctrl, flags);
 }
 void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                          cudaStream_t st) {
@@ -1001,7 +1262,13 @@ void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P
 }
 void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P, Ctrl *ctrl,
                         double dt, int flags, const Stage &stage, cudaStream_t st) {
-    update_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P, ctrl, dt, flags, stage);
+    const int bs = M.shape.update, g = (M.N + bs - 1) / bs;
+    if (bs == 128)
+        update_fp64<128><<<g, 128, 0, st>>>(M, S, P, ctrl, dt, flags, stage);
+    else if (bs == 512)
+        update_fp64<512><<<g, 512, 0, st>>>(M, S, P, ctrl, dt, flags, stage);
+    else
+        update_fp64<256><<<g, 256, 0, st>>>(M, S, P, ctrl, dt, flags, stage);
 }
 void launch_saxpy_fp64(const DevMesh &M, const DevState &S, double a, double b,
                        cudaStream_t st) {

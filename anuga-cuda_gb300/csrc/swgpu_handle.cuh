@@ -10,7 +10,7 @@
 
 namespace swgpu {
 
-constexpr int kStepsPerGraph = 16;
+constexpr int kStepsPerGraph = 16;  // default steps captured in one graph
 
 struct Handle {
     int device = 0;
@@ -23,6 +23,7 @@ struct Handle {
     DevParams P{};
     BcTag *d_tags = nullptr;
     int ntags = 0;
+    int steps_per_graph = kStepsPerGraph;
     int nscen = 1;               // scenarios (Ctrl blocks); > 1 for an ensemble
     std::vector<int64_t> scen_offsets;  // ensemble: first triangle of each scenario, + N
     int *d_blk_scen = nullptr;   // ensemble: scenario of each 256-triangle block

@@ -23,8 +23,16 @@ constexpr int kBlock = 256;
 // boundary edge -> -(slot + 1), as in ANUGA's neighbours array.
 __host__ __device__ inline int pack_neighbour(int n, int m) { return (n << 2) | m; }
 
+// Threads per block of the fused-step kernels (the autotuner's knobs;
+// results do not depend on them).  flux: FP64 block size, or the mixed
+// flux's TMA tile (64, 128, 256); update, distribute: 128, 256 or 512.
+struct LaunchShape {
+    int flux, update, distribute;
+};
+
 struct DevMesh {
     int N, Nb;
+    LaunchShape shape;
     const int *nbr;            // [3][N] packed neighbour / boundary slot
     const int *surr;           // [3][N] surrogate neighbours
     const uint8_t *nb;         // [N] number_of_boundaries
@@ -98,6 +106,7 @@ struct DevParams {
     int extrapolate_velocity_second_order, use_sloped_mannings;
     int max_smallsteps, default_order;
     int limiter;  // kLimiterOptimised, kLimiterVertex or kLimiterEdge
+    int flow_algorithm;  // 0 default, 1 'tsunami' (protect_swb2 + edge extrapolation)
     // FP32 copies for the mixed kernels (set on the host; FP64 arithmetic
     // on GB300 runs at 1/64 of the FP32 rate, so none is done per thread)
     float f_g, f_eps, f_H0, f_h0, f_lim, f_mah, f_mas, f_max_dt, f_alpha;
@@ -135,7 +144,8 @@ struct __align__(16) Ctrl {
     long long clk_order, clk_smallsteps;  // by the update kernel
     double step_t0;                 // time at the start of a Runge-Kutta step
     unsigned int blocks_flux;       // blocks of this scenario in one flux launch
-    unsigned int blocks_256;        // ... in one update / distribute launch
+    unsigned int blocks_update;     // ... in one update launch
+    unsigned int blocks_distribute; // ... in one distribute launch
     RunSummary *summary;            // shared by all scenarios of a handle
 };
 

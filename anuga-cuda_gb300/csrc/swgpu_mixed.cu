@@ -213,31 +213,32 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, Ctrl 
     return false;
 }
 
-constexpr int kFluxTile = 128;  // triangles per flux block (= threads)
-
-// The flux kernel's own data for one tile, filled by 26 bulk copies.
+// The flux kernel's own data for one tile of TILE triangles (= threads per
+// block: 64, 128 or 256), filled by 26 bulk copies.
+template <int TILE>
 struct __align__(128) FluxTile {
-    float wf[kFluxTile], wlo[kFluxTile], hf[kFluxTile], radius[kFluxTile], inv_area[kFluxTile];
-    float he[3][kFluxTile], dwe[3][kFluxTile], uhe[3][kFluxTile], vhe[3][kFluxTile];
-    float nx[3][kFluxTile], ny[3][kFluxTile], len[3][kFluxTile];
+    float wf[TILE], wlo[TILE], hf[TILE], radius[TILE], inv_area[TILE];
+    float he[3][TILE], dwe[3][TILE], uhe[3][TILE], vhe[3][TILE];
+    float nx[3][TILE], ny[3][TILE], len[3][TILE];
 };
 
 // Fluxes + gravity_wb, FP32, triangle centric (no atomics).  Each block
-// stages its tile of 128 triangles with one-dimensional TMA bulk copies into
+// stages its tile of TILE triangles with one-dimensional TMA bulk copies into
 // shared memory; neighbours inside the tile (most of them, in Morton order)
 // are read from shared memory, the others from global memory.
-__global__ void __launch_bounds__(kFluxTile) flux_mixed(DevMesh M, DevMixed X, DevParams P,
+template <int TILE>
+__global__ void __launch_bounds__(TILE) flux_mixed(DevMesh M, DevMixed X, DevParams P,
                                                         Ctrl *ctrl, int flags) {
     ctrl = block_ctrl(ctrl, M);
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
-    __shared__ FluxTile T;
+    __shared__ FluxTile<TILE> T;
     __shared__ __align__(8) unsigned long long bar;
     const int N = M.N, SP = X.S;
     const int tid = threadIdx.x;
-    const int k0 = blockIdx.x * kFluxTile;
-    const int cnt = min(kFluxTile, N - k0);
+    const int k0 = blockIdx.x * TILE;
+    const int cnt = min(TILE, N - k0);
     // tile length in the padded planes (a multiple of 64 elements)
-    const int span = min(kFluxTile, SP - k0);
+    const int span = min(TILE, SP - k0);
     if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
     if (tid == 0) {
@@ -330,7 +331,7 @@ __global__ void __launch_bounds__(kFluxTile) flux_mixed(DevMesh M, DevMixed X, D
         X.evh[k] = (a2 - ghc * gy) * inv_area;
     }
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
-    block_min_timestep_f<kFluxTile>(t, ctrl);
+    block_min_timestep_f<TILE>(t, ctrl);
     if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
         publish_step_clock(ctrl, P);
 }
@@ -375,7 +376,8 @@ __device__ __forceinline__ void finish_state(const DevParams &P, double &h, doub
 
 // Update: h += dt*E_h;  q += q*(r - 1) + dt*E_q*r  with r = 1/(1 - dt*S) the
 // semi-implicit Manning factor.  Increments in FP32, additions in FP64.
-__global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S, DevMixed X,
+template <int BS>
+__global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevState S, DevMixed X,
                                                        DevParams P, Ctrl *ctrl, int flags,
                                                        Stage stg) {
     ctrl = block_ctrl(ctrl, M);
@@ -434,7 +436,7 @@ __global__ void __launch_bounds__(kBlock, 8) update_mixed(DevMesh M, DevState S,
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
     if (flags & kFused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_256))
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_update))
             commit_stage(ctrl, clk, P, stg);
     }
 }
@@ -500,7 +502,8 @@ __device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], floa
 }
 
 // Extrapolation + balance + boundary conditions, FP32, in stage jumps.
-__global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevState S, DevMixed X,
+template <int BS>
+__global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, DevState S, DevMixed X,
                                                            DevParams P, const BcTag *tags,
                                                            Ctrl *ctrl, int flags) {
     const bool fused = flags & kFused;
@@ -710,7 +713,7 @@ __global__ void __launch_bounds__(kBlock, 6) distribute_mixed(DevMesh M, DevStat
     if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
     if (fused) {
         __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_256)) apply_pending_halt(ctrl);
+        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_distribute)) apply_pending_halt(ctrl);
     }
 }
 
@@ -787,19 +790,39 @@ __global__ void mass_final_mixed(const double *partials, int n, double *out) {
 
 // ------------------------------------------------------------ launches ---
 
+// Block sizes come from M.shape (the autotuner's choice; results do not
+// depend on it).
 void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                              const DevParams &P, const BcTag *tags, Ctrl *ctrl, int flags,
                              cudaStream_t st) {
-    distribute_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, S, X, P, tags, ctrl, flags);
+    const int bs = M.shape.distribute, g = (M.N + bs - 1) / bs;
+    if (bs == 128)
+        distribute_mixed<128><<<g, 128, 0, st>>>(M, S, X, P, tags, ctrl, flags);
+    else if (bs == 512)
+        distribute_mixed<512><<<g, 512, 0, st>>>(M, S, X, P, tags, ctrl, flags);
+    else
+        distribute_mixed<256><<<g, 256, 0, st>>>(M, S, X, P, tags, ctrl, flags);
 }
 void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, const DevParams &P,
                        Ctrl *ctrl, int flags, cudaStream_t st) {
-    flux_mixed<<<(M.N + kFluxTile - 1) / kFluxTile, kFluxTile, 0, st>>>(M, X, P, ctrl, flags);
+    const int t = M.shape.flux, g = (M.N + t - 1) / t;
+    if (t == 64)
+        flux_mixed<64><<<g, 64, 0, st>>>(M, X, P, ctrl, flags);
+    else if (t == 256)
+        flux_mixed<256><<<g, 256, 0, st>>>(M, X, P, ctrl, flags);
+    else
+        flux_mixed<128><<<g, 128, 0, st>>>(M, X, P, ctrl, flags);
 }
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,
                          cudaStream_t st) {
-    update_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, S, X, P, ctrl, flags, stage);
+    const int bs = M.shape.update, g = (M.N + bs - 1) / bs;
+    if (bs == 128)
+        update_mixed<128><<<g, 128, 0, st>>>(M, S, X, P, ctrl, flags, stage);
+    else if (bs == 512)
+        update_mixed<512><<<g, 512, 0, st>>>(M, S, X, P, ctrl, flags, stage);
+    else
+        update_mixed<256><<<g, 256, 0, st>>>(M, S, X, P, ctrl, flags, stage);
 }
 void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                           const DevParams &P, int from_stage, cudaStream_t st) {

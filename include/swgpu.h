@@ -146,6 +146,10 @@ typedef struct {
     int64_t use_edge_limiter;            /* nonzero: per-quantity limit by edge
                                             (FP64 only; gpu_domain_advanced.py:
                                             1815-1860) */
+    int64_t flow_algorithm;              /* 0: the default distribute; 1: the
+                                            'tsunami' one (protect_swb2 + edge
+                                            extrapolation, no balance; :1755-1812;
+                                            FP64 only) */
 } swgpu_params;
 
 /* Evolve state kept on the device (Domain time bookkeeping,
@@ -205,6 +209,24 @@ int swgpu_ensemble_set_finaltimes(void *handle, const double *finaltimes);
  * run alone. */
 int swgpu_ensemble_mass(void *handle, double *masses);
 
+/* Launch shape of the fused evolve step: the autotuner's knobs.  Results do
+ * not depend on it (every per-triangle operation and every reduction order
+ * is the same for every shape).  flux_block: threads per block of the FP64
+ * flux, or triangles per TMA tile of the mixed flux (64, 128, 256);
+ * update_block, distribute_block: 128, 256 or 512 (at most 256 for an
+ * ensemble); steps_per_graph: 1..64 steps captured per CUDA graph.  No
+ * counterpart in the reference (its block sizes are fixed per kernel,
+ * gpu_domain_advanced.py:186-507). */
+typedef struct {
+    int32_t flux_block;
+    int32_t update_block;
+    int32_t distribute_block;
+    int32_t steps_per_graph;
+} swgpu_launch_config;
+
+int swgpu_get_launch_config(void *handle, swgpu_launch_config *config);
+int swgpu_set_launch_config(void *handle, const swgpu_launch_config *config);
+
 /* Frees everything the handle owns.  No counterpart in the reference (its
  * PyCUDA allocations are released by the garbage collector). */
 int swgpu_destroy(void *handle);
@@ -236,6 +258,11 @@ int swgpu_get_boundary_values(void *handle, int quantity, double *out);
 
 /* explicit_update (stage/xmom/ymom) or semi_implicit_update (xmom/ymom). */
 int swgpu_get_explicit_update(void *handle, int quantity, double *out);
+
+/* max_speed per triangle from the last swgpu_compute_fluxes (FP64 handles;
+ * the copy_back of gpu_domain_advanced.py:923 for the degenerate-timestep
+ * protection). */
+int swgpu_get_max_speed(void *handle, double *out);
 int swgpu_get_semi_implicit_update(void *handle, int quantity, double *out);
 
 /* Installs the boundary tag table (Domain.set_boundary).  Every tag index

@@ -28,6 +28,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SWCPU_SO = os.path.join(HERE, "_build", "libswcpu.so")
 REF_SW_SO = os.path.join(HERE, "_ref", "libref_sw.so")
 REF_Q_SO = os.path.join(HERE, "_ref", "libref_quantity.so")
+REF_SWB2_SO = os.path.join(HERE, "_ref", "libref_swb2.so")
 REFERENCE_SRC = "/root/reference/src/anuga_HMPP"
 
 BC_REFLECTIVE, BC_DIRICHLET, BC_TIME_STAGE_SINE = 0, 1, 2
@@ -48,7 +49,7 @@ def build(ref: bool | None = None, quiet: bool = True) -> None:
 
 
 def reference_available() -> bool:
-    return os.path.exists(REF_SW_SO) and os.path.exists(REF_Q_SO)
+    return all(os.path.exists(p) for p in (REF_SW_SO, REF_Q_SO, REF_SWB2_SO))
 
 
 # --------------------------------------------------------------- swcpu.h
@@ -64,7 +65,7 @@ class OrcParams(C.Structure):
         ("optimise_dry_cells", C.c_long), ("extrapolate_velocity_second_order", C.c_long),
         ("use_sloped_mannings", C.c_long), ("max_smallsteps", C.c_long),
         ("default_order", C.c_long), ("optimised_gradient_limiter", C.c_long),
-        ("use_edge_limiter", C.c_long),
+        ("use_edge_limiter", C.c_long), ("flow_algorithm", C.c_long),
     ]
 
 
@@ -110,6 +111,7 @@ class OrcDomain(C.Structure):
         + [(n, C.c_long) for n in ["order", "smallsteps", "number_of_steps", "status"]]
         + [("timestepping_method", C.c_long)]
         + [(n, _d) for n in _BACKUPS]
+        + [("edge_coordinates", _d)]
     )
 
 
@@ -140,6 +142,10 @@ def swcpu():
         for name in ["swcpu_evolve_one_rk2_step", "swcpu_evolve_one_rk3_step"]:
             getattr(L, name).argtypes = [P, C.c_double]
             getattr(L, name).restype = C.c_int
+        L.swcpu_protect_swb2.argtypes = [P]
+        L.swcpu_protect_swb2.restype = None
+        L.swcpu_extrapolate_second_order_edge_sw.argtypes = [P]
+        L.swcpu_extrapolate_second_order_edge_sw.restype = C.c_int
         L.swcpu_extrapolate_and_limit_by_neighbours.argtypes = [P, C.c_int]
         L.swcpu_extrapolate_and_limit_by_neighbours.restype = C.c_int
         L.swcpu_backup_conserved_quantities.argtypes = [P]
@@ -162,6 +168,13 @@ def _params_struct(p) -> OrcParams:
     import dataclasses
     vals = {f.name: getattr(p, f.name) for f in dataclasses.fields(p)}
     return OrcParams(**vals)
+
+
+def edge_midpoints(V):
+    """(N, 3, 2) midpoints of the edges of triangles with vertex coordinates
+    V (N, 3, 2); edge i is opposite vertex i: 0.5 * (v_j + v_k)."""
+    return np.stack([0.5 * (V[:, 1] + V[:, 2]), 0.5 * (V[:, 2] + V[:, 0]),
+                     0.5 * (V[:, 0] + V[:, 1])], axis=1)
 
 
 class OracleDomain:
@@ -193,6 +206,8 @@ class OracleDomain:
         self.arrays["work_b"] = np.zeros(N)
         for n in _BACKUPS:
             self.arrays[n] = np.zeros(N)
+        V = np.asarray(mesh.vertex_coordinates, dtype=np.float64).reshape(N, 3, 2)
+        self.arrays["edge_coordinates"] = edge_midpoints(V).reshape(-1)
         ntag = max(int(mesh.boundary_tag.max()) + 1 if Nb else 1, len(tags or []), 1)
         self._tags = (OrcTag * ntag)()
         for i, (t, p) in enumerate(tags or []):
@@ -274,6 +289,12 @@ class OracleDomain:
 
     def extrapolate_first_order(self):
         self.L.swcpu_extrapolate_first_order(self._ref())
+
+    def protect_swb2(self):
+        self.L.swcpu_protect_swb2(self._ref())
+
+    def extrapolate_second_order_edge_sw(self):
+        return self.L.swcpu_extrapolate_second_order_edge_sw(self._ref())
 
     def extrapolate_and_limit_by_neighbours(self, by_edge):
         return self.L.swcpu_extrapolate_and_limit_by_neighbours(self._ref(), int(by_edge))
@@ -427,6 +448,11 @@ class ReferenceKernels:
         # gravity_wb exists in the reference only as a Python-C entry point
         # taking a domain object; the module's numpy C API is set up by its
         # init function.
+        self.sw._extrapolate_second_order_edge_sw.argtypes = [C.POINTER(RefDomain)]
+        self.sw._extrapolate_second_order_edge_sw.restype = C.c_int
+        self.swb2 = C.CDLL(REF_SWB2_SO, mode=os.RTLD_LAZY)
+        self.swb2.protect_swb2.argtypes = [C.c_long, C.c_long] + [C.c_double] * 3 + [_d] * 7
+        self.swb2.protect_swb2.restype = None
         self.sw.initshallow_water_ext.argtypes = []
         self.sw.initshallow_water_ext.restype = None
         self.sw.initshallow_water_ext()
@@ -457,7 +483,8 @@ class ReferenceKernels:
         R.beta_vh, R.beta_vh_dry = p.beta_vh, p.beta_vh_dry
         for n in ["neighbours", "neighbour_edges", "surrogate_neighbours", "normals",
                   "edgelengths", "radii", "areas", "tri_full_flag", "vertex_coordinates",
-                  "centroid_coordinates", "number_of_boundaries", "max_speed"]:
+                  "centroid_coordinates", "number_of_boundaries", "max_speed",
+                  "edge_coordinates"]:
             setattr(R, n, self._ptr(A[n]))
         flags = np.zeros(3 * N, np.int64)
         keep.append(flags)
@@ -541,6 +568,20 @@ class ReferenceKernels:
             *(self._ptr(A[n]) for n in ["xmom_centroid_values", "ymom_centroid_values",
                                         "xmom_vertex_values", "ymom_vertex_values"]),
             p.H0, int(p.tight_slope_limiters), int(p.use_centroid_velocities), p.alpha_balance)
+
+    def protect_swb2(self, od: OracleDomain) -> None:
+        """protect_swb2 of src/anuga_HMPP/swb2_domain_ext.c:7 on od's arrays."""
+        p, A = od.params, od.arrays
+        self.swb2.protect_swb2(od.N, 3 * od.N, p.minimum_allowed_height,
+                               p.maximum_allowed_speed, p.epsilon,
+                               *(self._ptr(A[n]) for n in [
+                                   "stage_centroid_values", "stage_vertex_values",
+                                   "bed_centroid_values", "bed_vertex_values",
+                                   "xmom_centroid_values", "ymom_centroid_values", "areas"]))
+
+    def extrapolate_second_order_edge_sw(self, od: OracleDomain) -> int:
+        R = self._struct(od)
+        return self.sw._extrapolate_second_order_edge_sw(C.byref(R))
 
     def protect(self, od: OracleDomain) -> int:
         p, A = od.params, od.arrays

@@ -834,6 +834,241 @@ int swcpu_extrapolate_and_limit_by_neighbours(swcpu_domain *D, int by_edge)
     return err;
 }
 
+/* The 'tsunami' protection, src/anuga_cuda/protect/protect.cu:64-131
+ * (_protect_swb2; HMPP restatement src/anuga_HMPP/swb2_domain_ext.c:7-79):
+ * below max(0.1 (max bed edge - bed centroid), minimum_allowed_height)
+ * momentum is zeroed; a non-positive depth lifts stage (and the stage
+ * vertex values) to the lowest bed vertex minus minimum_allowed_height. */
+void swcpu_protect_swb2(swcpu_domain *D)
+{
+    const double mah = D->params->minimum_allowed_height;
+    const double minimum_relative_height = 0.1;
+    double *wc = D->stage_centroid_values, *wv = D->stage_vertex_values;
+    const double *zc = D->bed_centroid_values, *zv = D->bed_vertex_values;
+    long k;
+    for (k = 0; k < D->number_of_elements; k++) {
+        const double hc = wc[k] - zc[k];
+        const double bmax = 0.5 * fmax(zv[3 * k] + zv[3 * k + 1],
+                                       fmax(zv[3 * k + 1] + zv[3 * k + 2],
+                                            zv[3 * k + 2] + zv[3 * k]));
+        if (hc < fmax(minimum_relative_height * (bmax - zc[k]), mah)) {
+            D->xmom_centroid_values[k] = 0.0;
+            D->ymom_centroid_values[k] = 0.0;
+            if (hc <= 0.0) {
+                const double bmin = fmin(zv[3 * k], fmin(zv[3 * k + 1], zv[3 * k + 2])) - mah;
+                if (wc[k] < bmin) {
+                    wc[k] = fmax(wc[k], bmin);
+                    wv[3 * k] = fmax(wv[3 * k], bmin);
+                    wv[3 * k + 1] = fmax(wv[3 * k + 1], bmin);
+                    wv[3 * k + 2] = fmax(wv[3 * k + 2], bmin);
+                }
+            }
+        }
+    }
+}
+
+/* The limiter of the edge extrapolation: src/anuga_HMPP/
+ * shallow_water_ext.c:151-180 (limit_gradient) applied to edge jumps. */
+static void limit_gradient_jumps(double dqv[3], double qmin, double qmax, double beta)
+{
+    const double tiny = 1.0e-100;
+    double r = 1000.0, r0 = 1.0, phi;
+    int i;
+    for (i = 0; i < 3; i++) {
+        if (dqv[i] < -tiny)
+            r0 = qmin / dqv[i];
+        if (dqv[i] > tiny)
+            r0 = qmax / dqv[i];
+        r = omin(r0, r);
+    }
+    phi = omin(r * beta, 1.0);
+    dqv[0] = dqv[0] * phi;
+    dqv[1] = dqv[1] * phi;
+    dqv[2] = dqv[2] * phi;
+}
+
+/* src/anuga_HMPP/shallow_water_ext.c:3328-3964 (_extrapolate_second_order_edge_sw),
+ * the extrapolation of the 'tsunami' algorithm: limited gradients as in
+ * extrapolate_second_order_sw but evaluated at the edge midpoints, dry
+ * surrogate neighbours replaced by the triangle itself, beta switched fully
+ * wet/dry (hfactor 0 or 1), vertex values from the edge values
+ * (v_i = e_j + e_k - e_i), velocities converted back to momenta with the
+ * edge and vertex depths.  Cells skipped as dry keep their previous edge
+ * values (and, as in the reference, rescale them by depth). */
+int swcpu_extrapolate_second_order_edge_sw(swcpu_domain *D)
+{
+    const swcpu_params *P = D->params;
+    const long N = D->number_of_elements;
+    const double *C = D->centroid_coordinates, *E = D->edge_coordinates;
+    const double *w = D->stage_centroid_values, *z = D->bed_centroid_values;
+    double *we = D->stage_edge_values, *ue = D->xmom_edge_values, *ve = D->ymom_edge_values;
+    double *u = D->work_a, *v = D->work_b;  /* momentum or velocity at centroids */
+    const int vel = P->extrapolate_velocity_second_order == 1;
+    long k;
+    int i, err = 0;
+    for (k = 0; k < N; k++) {
+        if (vel) {
+            const double dk = omax(w[k] - z[k], P->minimum_allowed_height);
+            u[k] = D->xmom_centroid_values[k] / dk;
+            v[k] = D->ymom_centroid_values[k] / dk;
+        } else {
+            u[k] = D->xmom_centroid_values[k];
+            v[k] = D->ymom_centroid_values[k];
+        }
+    }
+    for (k = 0; k < N; k++) {
+        const long k3 = 3 * k, k6 = 6 * k;
+        const long nb = D->number_of_boundaries[k];
+        double dxv[3], dyv[3], dqv[3], qmin, qmax;
+        const double x = C[2 * k], y = C[2 * k + 1];
+        if (nb == 3) {
+            for (i = 0; i < 3; i++) {
+                we[k3 + i] = w[k];
+                ue[k3 + i] = u[k];
+                ve[k3 + i] = v[k];
+            }
+            continue;
+        }
+        for (i = 0; i < 3; i++) {
+            dxv[i] = E[k6 + 2 * i] - x;
+            dyv[i] = E[k6 + 2 * i + 1] - y;
+        }
+        if (nb <= 1) {
+            long k0 = D->surrogate_neighbours[k3], k1 = D->surrogate_neighbours[k3 + 1];
+            long k2 = D->surrogate_neighbours[k3 + 2];
+            double x0, y0, dx1, dx2, dy1, dy2, area2, inv_area2, hc, h0, h1, h2, hmin, hfactor;
+            const double *q[3];
+            double *qe[3];
+            double beta[3];
+            int j;
+            if (w[k2] <= z[k2])
+                k2 = k;
+            if (w[k0] <= z[k0])
+                k0 = k;
+            if (w[k1] <= z[k1])
+                k1 = k;
+            x0 = C[2 * k0];
+            y0 = C[2 * k0 + 1];
+            dx1 = C[2 * k1] - x0;
+            dx2 = C[2 * k2] - x0;
+            dy1 = C[2 * k1 + 1] - y0;
+            dy2 = C[2 * k2 + 1] - y0;
+            area2 = dy2 * dx1 - dy1 * dx2;
+            if (area2 <= 0) {
+                for (i = 0; i < 3; i++) {
+                    we[k3 + i] = w[k];
+                    ue[k3 + i] = u[k];
+                    ve[k3 + i] = v[k];
+                }
+                continue;
+            }
+            hc = w[k] - z[k];
+            h0 = w[k0] - z[k0];
+            h1 = w[k1] - z[k1];
+            h2 = w[k2] - z[k2];
+            hmin = omin(omin(h0, omin(h1, h2)), hc);
+            hfactor = hmin > 0.0 ? 1.0 : 0.0;
+            if (P->optimise_dry_cells && omax(h0, omax(h1, h2)) < P->epsilon)
+                continue;
+            inv_area2 = 1.0 / area2;
+            q[0] = w;
+            q[1] = u;
+            q[2] = v;
+            qe[0] = we;
+            qe[1] = ue;
+            qe[2] = ve;
+            beta[0] = P->beta_w_dry + (P->beta_w - P->beta_w_dry) * hfactor;
+            beta[1] = P->beta_uh_dry + (P->beta_uh - P->beta_uh_dry) * hfactor;
+            beta[2] = P->beta_vh_dry + (P->beta_vh - P->beta_vh_dry) * hfactor;
+            for (j = 0; j < 3; j++) {
+                const double dq0 = q[j][k0] - q[j][k];
+                const double dq1 = q[j][k1] - q[j][k0];
+                const double dq2 = q[j][k2] - q[j][k0];
+                double a = dy2 * dq1 - dy1 * dq2, b = dx1 * dq2 - dx2 * dq1;
+                a *= inv_area2;
+                b *= inv_area2;
+                for (i = 0; i < 3; i++)
+                    dqv[i] = a * dxv[i] + b * dyv[i];
+                qmin_qmax(dq0, dq1, dq2, &qmin, &qmax);
+                limit_gradient_jumps(dqv, qmin, qmax, beta[j]);
+                for (i = 0; i < 3; i++)
+                    qe[j][k3 + i] = q[j][k] + dqv[i];
+            }
+        } else {
+            /* one interior neighbour: the first surrogate that is not k */
+            long k1 = -1;
+            double dx1, dy1, area2, dx2, dy2;
+            const double *q[3];
+            double *qe[3];
+            int j;
+            for (i = 0; i < 3; i++)
+                if (D->surrogate_neighbours[k3 + i] != k) {
+                    k1 = D->surrogate_neighbours[k3 + i];
+                    break;
+                }
+            if (k1 < 0) {
+                err = 1;
+                continue;
+            }
+            dx1 = C[2 * k1] - x;
+            dy1 = C[2 * k1 + 1] - y;
+            area2 = dx1 * dx1 + dy1 * dy1;
+            dx2 = 1.0 / area2;
+            dy2 = dx2 * dy1;
+            dx2 *= dx1;
+            q[0] = w;
+            q[1] = u;
+            q[2] = v;
+            qe[0] = we;
+            qe[1] = ue;
+            qe[2] = ve;
+            for (j = 0; j < 3; j++) {
+                const double dq1 = q[j][k1] - q[j][k];
+                const double a = dq1 * dx2, b = dq1 * dy2;
+                for (i = 0; i < 3; i++)
+                    dqv[i] = a * dxv[i] + b * dyv[i];
+                if (dq1 >= 0.0) {
+                    qmin = 0.0;
+                    qmax = dq1;
+                } else {
+                    qmin = dq1;
+                    qmax = 0.0;
+                }
+                limit_gradient_jumps(dqv, qmin, qmax, P->beta_w);
+                for (i = 0; i < 3; i++)
+                    qe[j][k3 + i] = q[j][k] + dqv[i];
+            }
+        }
+    }
+    for (k = 0; k < N; k++) {
+        const long k3 = 3 * k;
+        double *qv[3] = {D->stage_vertex_values, D->xmom_vertex_values, D->ymom_vertex_values};
+        double *qe[3] = {we, ue, ve};
+        int j;
+        for (j = 0; j < 3; j++) {
+            qv[j][k3] = qe[j][k3 + 1] + qe[j][k3 + 2] - qe[j][k3];
+            qv[j][k3 + 1] = qe[j][k3] + qe[j][k3 + 2] - qe[j][k3 + 1];
+            qv[j][k3 + 2] = qe[j][k3] + qe[j][k3 + 1] - qe[j][k3 + 2];
+        }
+        if (vel) {
+            for (i = 0; i < 3; i++) {
+                const double de = omax(we[k3 + i] - D->bed_edge_values[k3 + i], 0.0);
+                ue[k3 + i] = ue[k3 + i] * de;
+                ve[k3 + i] = ve[k3 + i] * de;
+            }
+            for (i = 0; i < 3; i++) {
+                const double dv = omax(D->stage_vertex_values[k3 + i] -
+                                           D->bed_vertex_values[k3 + i], 0.0);
+                D->xmom_vertex_values[k3 + i] = D->xmom_vertex_values[k3 + i] * dv;
+                D->ymom_vertex_values[k3 + i] = D->ymom_vertex_values[k3 + i] * dv;
+            }
+        }
+    }
+    if (err)
+        D->status |= SWCPU_ERR_NO_INTERIOR_NEIGHBOUR;
+    return err;
+}
+
 /* src/anuga_cuda/gpu_domain_advanced.py:1744-2001: protect, then first
  * order, the per-quantity edge limiter (use_edge_limiter), the optimised
  * shallow-water extrapolation (optimised_gradient_limiter) or the
@@ -841,6 +1076,13 @@ int swcpu_extrapolate_and_limit_by_neighbours(swcpu_domain *D, int by_edge)
 void swcpu_distribute_to_vertices_and_edges(swcpu_domain *D)
 {
     const swcpu_params *P = D->params;
+    if (P->flow_algorithm == 1) {
+        /* the 'tsunami' branch (:1755-1812): protect_swb2 and the edge
+         * extrapolation, at every order, no balance */
+        swcpu_protect_swb2(D);
+        swcpu_extrapolate_second_order_edge_sw(D);
+        return;
+    }
     swcpu_protect(D);
     if (D->order == 1)
         swcpu_extrapolate_first_order(D);

@@ -52,6 +52,8 @@ typedef struct {
     long default_order;
     long optimised_gradient_limiter; /* 1: extrapolate_second_order_sw */
     long use_edge_limiter;           /* 1: per-quantity limit by edge */
+    long flow_algorithm;             /* 0 default, 1 'tsunami' (protect_swb2 +
+                                        edge extrapolation, no balance) */
 } swcpu_params;
 
 typedef struct {
@@ -102,6 +104,9 @@ typedef struct {
      * written when timestepping_method > 1 or by the backup call) */
     long timestepping_method;
     double *stage_centroid_backup, *xmom_centroid_backup, *ymom_centroid_backup;
+
+    /* edge midpoints [6N] (x, y per edge), for the edge extrapolation */
+    const double *edge_coordinates;
 } swcpu_domain;
 
 double swcpu_compute_fluxes(swcpu_domain *D);
@@ -112,6 +117,8 @@ void swcpu_protect(swcpu_domain *D);
 void swcpu_extrapolate_second_order_sw(swcpu_domain *D);
 void swcpu_extrapolate_first_order(swcpu_domain *D);
 int swcpu_extrapolate_and_limit_by_neighbours(swcpu_domain *D, int by_edge);
+void swcpu_protect_swb2(swcpu_domain *D);
+int swcpu_extrapolate_second_order_edge_sw(swcpu_domain *D);
 void swcpu_balance_deep_and_shallow(swcpu_domain *D);
 void swcpu_interpolate_to_edges(swcpu_domain *D);
 void swcpu_distribute_to_vertices_and_edges(swcpu_domain *D);

@@ -98,6 +98,8 @@ def cases():
         use_edge_limiter=1, beta_w=0.8, beta_uh=1.1, beta_vh=1.3)
     yield "channel_vertex_limiter", scenarios.channel_inflow(14, 5, seed=1), DEFAULT.replace(
         optimised_gradient_limiter=0)
+    yield "basin_tsunami", scenarios.small_basin(11, 8, seed=9), DEFAULT.replace(
+        flow_algorithm=1, beta_w_dry=0.4, beta_uh_dry=0.3, beta_vh_dry=0.2)
 
 
 def ref_step(R, od, finaltime=-1.0):
@@ -118,6 +120,12 @@ def ref_distribute(R, od):
     """distribute_to_vertices_and_edges (gpu_domain_advanced.py:1744-2001)
     with the reference's kernels, then the boundary values."""
     p = od.params
+    if p.flow_algorithm == 1:
+        # the 'tsunami' branch: protect_swb2 and the edge extrapolation
+        R.protect_swb2(od)
+        assert R.extrapolate_second_order_edge_sw(od) == 0
+        od.update_boundary()
+        return
     R.protect(od)
     if od.D.order == 1:
         od.extrapolate_first_order()
@@ -211,6 +219,18 @@ def make(name, sc, params):
     assert R.update(od, dt) == 0
     for q in ("stage", "xmom", "ymom"):
         out[f"k/update/{q}"] = od.arrays[q + "_centroid_values"].copy()
+
+    if params.flow_algorithm == 1:
+        # the 'tsunami' distribute kernels once, from the initial state
+        od = O.OracleDomain(sc.mesh, params, sc.oracle_tags())
+        sc.apply_to_oracle(od)
+        R.protect_swb2(od)
+        for q in ("stage", "xmom", "ymom"):
+            out[f"k/protect_swb2/{q}"] = od.arrays[q + "_centroid_values"].copy()
+        assert R.extrapolate_second_order_edge_sw(od) == 0
+        for q in ("stage", "xmom", "ymom"):
+            out[f"k/edge_extrapolate/{q}_edge"] = od.arrays[q + "_edge_values"].copy()
+            out[f"k/edge_extrapolate/{q}_vertex"] = od.arrays[q + "_vertex_values"].copy()
 
     # a fresh run of STEPS Euler steps from the initial state
     od = O.OracleDomain(sc.mesh, params, sc.oracle_tags())

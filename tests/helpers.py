@@ -7,7 +7,7 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 GOLDEN_CASES = ["four_triangles", "single_triangle", "basin_wetdry", "basin_momentum_limiter",
-                "harbour_small", "basin_edge_limiter", "channel_vertex_limiter"]
+                "harbour_small", "basin_edge_limiter", "channel_vertex_limiter", "basin_tsunami"]
 MESH_KEYS = ["neighbours", "neighbour_edges", "surrogate_neighbours", "number_of_boundaries",
              "tri_full_flag", "normals", "edgelengths", "radii", "areas", "vertex_coordinates",
              "centroid_coordinates", "boundary_cells", "boundary_edges", "boundary_tag"]

@@ -29,9 +29,9 @@ def test_library_exports_every_declared_symbol(swgpu_built):
 
 def test_struct_layouts_match_header():
     from anuga_cuda import _lib
-    # swgpu_mesh: 2 int64 + 14 pointers; swgpu_params: 15 doubles + 9 int64
+    # swgpu_mesh: 2 int64 + 14 pointers; swgpu_params: 15 doubles + 10 int64
     assert ctypes.sizeof(_lib.Mesh_t) == 8 * (2 + 14)
-    assert ctypes.sizeof(_lib.Params_t) == 8 * (15 + 9)
+    assert ctypes.sizeof(_lib.Params_t) == 8 * (15 + 10)
     assert ctypes.sizeof(_lib.State_t) == 8 * (7 + 6)
     assert ctypes.sizeof(_lib.BoundaryTag_t) == 8 * 5
     from anuga_cuda.config import Parameters

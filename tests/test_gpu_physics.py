@@ -159,8 +159,33 @@ def test_limiter_variants_need_fp64(swgpu_built):
     from anuga_cuda import DEFAULT, scenarios
     from anuga_cuda._lib import SwgpuError
     sc = scenarios.small_basin(8, 6, seed=1)
-    for kw in ({"use_edge_limiter": 1}, {"optimised_gradient_limiter": 0}):
+    for kw in ({"use_edge_limiter": 1}, {"optimised_gradient_limiter": 0},
+               {"flow_algorithm": 1}):
         with pytest.raises(SwgpuError):
             gpu_from_scenario(sc, DEFAULT.replace(**kw), "mixed")
         d = gpu_from_scenario(sc, DEFAULT.replace(**kw), "fp64")
         assert d.evolve_steps(20).status == 0
+
+
+def test_degenerate_timestep_protection(swgpu_built):
+    """gpu_domain_advanced.py:914-951: an isolated triangle far faster than
+    all others loses its momentum before the timestep is chosen."""
+    from anuga_cuda import DEFAULT, scenarios
+    sc = scenarios.small_basin(10, 8, seed=0, wet_dry_front=False)
+    zc = sc.elevation_vertex.mean(axis=1)
+    h = sc.stage_centroid - zc
+    k = 0        # every edge of triangle 0 is processed by it (all neighbours are higher)
+    assert h[k] > 0.1
+    sc.xmom_centroid = np.zeros(sc.N)
+    sc.ymom_centroid = np.zeros(sc.N)
+    sc.xmom_centroid[k] = 40.0 * h[k]          # 40 m/s in one wet triangle
+    d = gpu_from_scenario(sc, DEFAULT)
+    d.evolve_steps(0)
+    d.protect_against_isolated_degenerate_timesteps = True
+    d.compute_fluxes()
+    assert d.max_speed.max() > 10.0
+    d.update_timestep(1.0e300, None)
+    u = d.quantities["xmomentum"].centroid_values
+    assert u[k] == 0.0
+    with pytest.raises(NotImplementedError):
+        next(iter(d.evolve(yieldstep=1.0, finaltime=1.0)))

@@ -4,7 +4,7 @@ over 40 Euler steps and over 12 RK2 and RK3 steps.  Runs everywhere (no referenc
 import numpy as np
 import pytest
 
-from helpers import GOLDEN_CASES, bits_equal, golden_oracle, load_golden
+from helpers import GOLDEN_CASES, bits_equal, golden_oracle, golden_params, load_golden
 
 STEPS = 40
 
@@ -92,6 +92,19 @@ def test_runge_kutta_differs_from_euler():
         not bits_equal(g["rk2/0/stage"], g["run/0/stage"])
 
 
+def test_tsunami_kernels_match_reference_bitwise(oracle_mod):
+    g = load_golden("basin_tsunami")
+    od = golden_oracle(g, oracle_mod)
+    A = od.arrays
+    od.protect_swb2()
+    for q in ("stage", "xmom", "ymom"):
+        assert bits_equal(A[q + "_centroid_values"], g[f"k/protect_swb2/{q}"]), q
+    assert od.extrapolate_second_order_edge_sw() == 0
+    for q in ("stage", "xmom", "ymom"):
+        assert bits_equal(A[q + "_edge_values"], g[f"k/edge_extrapolate/{q}_edge"]), q
+        assert bits_equal(A[q + "_vertex_values"], g[f"k/edge_extrapolate/{q}_vertex"]), q
+
+
 def test_golden_cases_cover_wet_dry_and_boundaries():
     g = load_golden("basin_wetdry")
     h = g["init/stage_centroid_values"] - g["init/bed_centroid_values"]
@@ -101,8 +114,9 @@ def test_golden_cases_cover_wet_dry_and_boundaries():
     assert 2 in hs["tags/type"].tolist(), "time-dependent stage boundary"
     ch = load_golden("channel_vertex_limiter")
     assert set(ch["tags/type"].tolist()) >= {3, 4, 5}, "transmissive and inflow boundaries"
-    assert ch["params"][-2] == 0, "per-quantity vertex limiter"
-    assert load_golden("basin_edge_limiter")["params"][-1] == 1, "edge limiter"
+    assert golden_params(ch).optimised_gradient_limiter == 0, "per-quantity vertex limiter"
+    assert golden_params(load_golden("basin_edge_limiter")).use_edge_limiter == 1, "edge limiter"
+    assert golden_params(load_golden("basin_tsunami")).flow_algorithm == 1, "tsunami"
     nb = np.concatenate([load_golden(c)["mesh/number_of_boundaries"] for c in GOLDEN_CASES])
     assert set(nb.tolist()) == {0, 1, 2, 3}, "every number_of_boundaries branch"
     assert np.isfinite(g["run/final/mass"]).all()

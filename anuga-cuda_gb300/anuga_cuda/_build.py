@@ -1,6 +1,6 @@
 """In-tree build of libswgpu.so for sm_103a (GB300) with nvcc.
 
-Four translation units are compiled in parallel and linked into
+Five translation units are compiled in parallel and linked into
 ``anuga_cuda/libswgpu.so`` next to this file:
 
 * ``csrc/swgpu_fp64.cu``  -- the FP64 parity kernels, ``--fmad=false`` so that
@@ -9,7 +9,8 @@ Four translation units are compiled in parallel and linked into
 * ``csrc/swgpu_mixed.cu`` -- the mixed-precision kernels (FMA allowed, FP32
   division and square root approximate, denormals flushed);
 * ``csrc/swgpu_api.cu``   -- the C ABI, allocation and the evolve loop;
-* ``csrc/swgpu_noalloc.cu`` -- the allocation-free water-volume entry point.
+* ``csrc/swgpu_noalloc.cu`` -- the allocation-free water-volume entry point;
+* ``csrc/swgpu_mlp.cu``   -- the BF16 tensor-core MLP surrogate.
 """
 from __future__ import annotations
 
@@ -30,6 +31,7 @@ UNITS = {
     "swgpu_mixed.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "swgpu_api.cu": [],
     "swgpu_noalloc.cu": ["--fmad=false"],
+    "swgpu_mlp.cu": [],
 }
 
 

@@ -38,6 +38,7 @@ STATUS_NAMES = {
 
 _i64p = C.POINTER(C.c_int64)
 _f64p = C.POINTER(C.c_double)
+_f32p = C.POINTER(C.c_float)
 
 
 class Mesh_t(C.Structure):
@@ -106,12 +107,25 @@ _SIGNATURES = [
     ("swgpu_create_ensemble", C.c_int, [C.POINTER(Mesh_t), _i64p, C.c_int,
                                         C.POINTER(Params_t), C.c_int, C.POINTER(_VP)]),
     ("swgpu_ensemble_size", C.c_int, [_VP, C.POINTER(C.c_int)]),
+    ("swgpu_set_tracking", C.c_int, [_VP, C.c_int, C.c_double]),
+    ("swgpu_get_tracking", C.c_int, [_VP, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("swgpu_get_launch_config", C.c_int, [_VP, C.POINTER(LaunchConfig_t)]),
     ("swgpu_set_launch_config", C.c_int, [_VP, C.POINTER(LaunchConfig_t)]),
     ("swgpu_ensemble_get_state", C.c_int, [_VP, C.c_int, C.POINTER(State_t)]),
     ("swgpu_ensemble_set_finaltimes", C.c_int, [_VP, _f64p]),
     ("swgpu_ensemble_mass", C.c_int, [_VP, _f64p]),
     ("swgpu_destroy", C.c_int, [_VP]),
+    ("swgpu_mlp_num_params", C.c_int, []),
+    ("swgpu_mlp_create", C.c_int, [_f32p, _f32p, _f32p, C.POINTER(_VP)]),
+    ("swgpu_mlp_destroy", C.c_int, [_VP]),
+    ("swgpu_mlp_last_error", C.c_char_p, [_VP]),
+    ("swgpu_mlp_set_data", C.c_int, [_VP, _f32p, C.c_int64, _f32p, C.c_int64, _f32p]),
+    ("swgpu_mlp_predict", C.c_int, [_VP, C.c_int64, C.c_int64, _VP, _f32p]),
+    ("swgpu_mlp_gradients", C.c_int, [_VP, _i64p, C.c_int64, C.c_float, C.c_float, _f32p,
+                                      _f32p, _f32p]),
+    ("swgpu_mlp_train", C.c_int, [_VP, C.c_int, C.c_int64, C.c_uint64, C.c_float, C.c_float,
+                                  C.c_float, _f32p, _f32p]),
+    ("swgpu_mlp_get_params", C.c_int, [_VP, _f32p]),
     ("swgpu_last_error", C.c_char_p, [_VP]),
     ("swgpu_device_info", C.c_int, [C.c_char_p, C.c_int]),
     ("swgpu_set_quantity", C.c_int, [_VP, C.c_int, _f64p, _f64p, _f64p]),

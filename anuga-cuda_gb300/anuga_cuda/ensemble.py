@@ -217,6 +217,18 @@ class Ensemble:
             out.append(st)
         return out
 
+    def set_tracking(self, threshold=0.01, on=True):
+        """Maximum depth and arrival time tracking for every scenario."""
+        check(lib().swgpu_set_tracking(self._h, int(bool(on)), float(threshold)), self._h)
+
+    def get_tracking(self):
+        """Per scenario, (max_depth, arrival_time) arrays of its triangles."""
+        hm = np.empty(self.N, dtype=np.float32)
+        ta = np.empty(self.N, dtype=np.float32)
+        check(lib().swgpu_get_tracking(self._h, hm.ctypes.data_as(C.POINTER(C.c_float)),
+                                       ta.ctypes.data_as(C.POINTER(C.c_float))), self._h)
+        return [(hm[a:b].copy(), ta[a:b].copy()) for a, b in self.ranges]
+
     def masses(self):
         m = np.empty(len(self))
         check(lib().swgpu_ensemble_mass(self._h, f64p(m)), self._h)

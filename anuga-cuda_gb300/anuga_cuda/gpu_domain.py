@@ -563,6 +563,21 @@ class GPU_domain:
     def apply_fractional_steps(self):
         pass
 
+    def set_tracking(self, threshold=0.01, on=True):
+        """Track, per triangle over the following evolve steps, the maximum
+        depth and the first time the depth exceeds ``threshold``."""
+        check(lib().swgpu_set_tracking(self._h, int(bool(on)), float(threshold)), self._h)
+
+    def get_tracking(self):
+        """(max_depth, arrival_time) per triangle in the caller's order
+        (arrival -1 where the depth never exceeded the threshold)."""
+        n = self.number_of_elements
+        hm = np.empty(n, dtype=np.float32)
+        ta = np.empty(n, dtype=np.float32)
+        check(lib().swgpu_get_tracking(self._h, hm.ctypes.data_as(C.POINTER(C.c_float)),
+                                       ta.ctypes.data_as(C.POINTER(C.c_float))), self._h)
+        return self._to_user(hm), self._to_user(ta)
+
     def get_water_volume(self):
         m = C.c_double()
         check(lib().swgpu_mass(self._h, C.byref(m)), self._h)

@@ -167,7 +167,7 @@ static void reset_ftmin(Ctrl *c, const DevParams &P) {
 static void issue_stage(Handle *h, const Stage &stg) {
     const int flux_flags = kFused | (stg.kind == kStageMid || stg.kind == kStageLast
                                          ? kNoTimestep : 0);
-    const int update_flags = kFused | kFrictionInline;
+    const int update_flags = kFused | kFrictionInline | (h->S.hmax ? kTrack : 0);
     const int dist_flags = kFused | kWriteBoundary;
     if (h->precision == SWGPU_FP64) {
         launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, flux_flags, h->stream);
@@ -1105,6 +1105,43 @@ int swgpu_set_launch_config(void *handle, const swgpu_launch_config *cfg) {
     h->steps_per_graph = cfg->steps_per_graph;
     set_block_counts(h);
     return push_ctrl(h);
+}
+
+int swgpu_set_tracking(void *handle, int on, double threshold) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (on && !(threshold >= 0.0)) return fail(h, SWGPU_EINVAL, "threshold must be >= 0");
+    if (on) {
+        if (!h->trk_hmax) {
+            int rc = dalloc(h, &h->trk_hmax, (size_t)h->M.N);
+            if (!rc) rc = dalloc(h, &h->trk_tarr, (size_t)h->M.N);
+            if (rc) return rc;
+        }
+        h->S.hmax = h->trk_hmax;
+        h->S.tarr = h->trk_tarr;
+        h->P.track_threshold = threshold;
+        launch_track_reset(h->M, h->S, h->stream);
+        int rc = check_launch(h, "tracking reset");
+        if (rc) return rc;
+    } else {
+        h->S.hmax = h->S.tarr = nullptr;  // the buffers stay for a later call
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;  // recaptured with the new tracking state and threshold
+    }
+    return SWGPU_OK;
+}
+
+int swgpu_get_tracking(void *handle, float *max_depth, float *arrival_time) {
+    Handle *h = static_cast<Handle *>(handle);
+    if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (!h->trk_hmax) return fail(h, SWGPU_EINVAL, "tracking was never switched on");
+    int rc;
+    if (max_depth && (rc = download(h, max_depth, h->trk_hmax, (size_t)h->M.N))) return rc;
+    if (arrival_time && (rc = download(h, arrival_time, h->trk_tarr, (size_t)h->M.N))) return rc;
+    return SWGPU_OK;
 }
 
 int swgpu_ensemble_size(void *handle, int *nscen) {

@@ -279,6 +279,23 @@ __device__ __forceinline__ void commit_stage(Ctrl *c, const StepClock &s, const 
     }
 }
 
+// Maximum depth and arrival time of triangle k after a whole step that
+// ends at time t_end (stages before the last of a Runge-Kutta step do not
+// count).
+__device__ __forceinline__ void track_depth(const DevState &S, int k, double h, double t_end,
+                                            double threshold) {
+    const float hf = (float)h;
+    if (hf > S.hmax[k]) S.hmax[k] = hf;
+    if (h > threshold && S.tarr[k] < 0.0f) S.tarr[k] = (float)t_end;
+}
+
+// Model time at the end of the step a stage belongs to, read by every
+// block before the update's last block commits it.
+__device__ __forceinline__ double step_end_time(const Ctrl *c, const StepClock &s,
+                                                const Stage &stg) {
+    return (stg.kind == kStageLast ? c->step_t0 : c->time) + s.dt;
+}
+
 // Last block of the distribute kernel: a pending stop takes effect.
 __device__ __forceinline__ void apply_pending_halt(Ctrl *c) {
     if (c->halt_pending) {

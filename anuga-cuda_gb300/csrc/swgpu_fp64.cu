@@ -482,6 +482,8 @@ __global__ void __launch_bounds__(BS) update_fp64(DevMesh M, DevState S, DevPara
         S.w[k] = w;
         S.uh[k] = uh;
         S.vh[k] = vh;
+        if ((flags & kTrack) && (stg.kind == kStageEuler || stg.kind == kStageLast))
+            track_depth(S, k, w - S.zc[k], step_end_time(ctrl, clk, stg), P.track_threshold);
     }
     if (bad) set_status(ctrl, SWGPU_EDENOMINATOR);
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
@@ -490,6 +492,16 @@ __global__ void __launch_bounds__(BS) update_fp64(DevMesh M, DevState S, DevPara
         if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_update))
             commit_stage(ctrl, clk, P, stg);
     }
+}
+
+__global__ void __launch_bounds__(kBlock) track_reset(int N, float *hmax, float *tarr) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    hmax[k] = 0.0f;
+    tarr[k] = -1.0f;
+}
+void launch_track_reset(const DevMesh &M, const DevState &S, cudaStream_t st) {
+    track_reset<<<grid_for(M.N), kBlock, 0, st>>>(M.N, S.hmax, S.tarr);
 }
 
 // saxpy_conserved_quantities (src/anuga_cuda/saxpy_centroid_values/

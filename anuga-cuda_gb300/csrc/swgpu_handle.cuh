@@ -24,6 +24,7 @@ struct Handle {
     BcTag *d_tags = nullptr;
     int ntags = 0;
     int steps_per_graph = kStepsPerGraph;
+    float *trk_hmax = nullptr, *trk_tarr = nullptr;  // tracking buffers (S.hmax/S.tarr when on)
     int nscen = 1;               // scenarios (Ctrl blocks); > 1 for an ensemble
     std::vector<int64_t> scen_offsets;  // ensemble: first triangle of each scenario, + N
     int *d_blk_scen = nullptr;   // ensemble: scenario of each 256-triangle block

@@ -63,6 +63,9 @@ struct DevState {
     double *hc, *uc, *vc;                     // [N] derived centroid quantities
     double *hb, *ub, *vb;                     // [Nb] derived boundary quantities
     double *partials;                         // [grid] reduction scratch
+    float *hmax, *tarr;                       // [N] tracking: maximum depth since reset,
+                                              // first time depth exceeded the threshold
+                                              // (negative: not yet); null when off
     double *bw, *buh, *bvh;                   // [N] backups of the conserved state for
                                               // Runge-Kutta steps (bw: stage in FP64,
                                               // depth in the mixed precision)
@@ -107,6 +110,7 @@ struct DevParams {
     int max_smallsteps, default_order;
     int limiter;  // kLimiterOptimised, kLimiterVertex or kLimiterEdge
     int flow_algorithm;  // 0 default, 1 'tsunami' (protect_swb2 + edge extrapolation)
+    double track_threshold;  // depth that counts as arrival
     // FP32 copies for the mixed kernels (set on the host; FP64 arithmetic
     // on GB300 runs at 1/64 of the FP32 rate, so none is done per thread)
     float f_g, f_eps, f_H0, f_h0, f_lim, f_mah, f_mas, f_max_dt, f_alpha;
@@ -159,6 +163,7 @@ enum : int {
     kFrictionInline = 8,  // update computes Manning friction itself
     kWriteMaxSpeed = 16,  // flux writes max_speed
     kNoTimestep = 32,     // flux skips the timestep reduction (later Runge-Kutta stages)
+    kTrack = 64,          // update records maximum depth and arrival time (whole steps)
 };
 
 // One stage of a fused step.  An Euler step is one stage; ANUGA's RK2 and
@@ -203,6 +208,8 @@ void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P
 void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                         Ctrl *ctrl, double dt, int flags, const Stage &stage,
                         cudaStream_t st);
+// tracking arrays to (0, -1)
+void launch_track_reset(const DevMesh &M, const DevState &S, cudaStream_t st);
 // saxpy_conserved_quantities: Q = a*Q + b*backup for stage and momenta
 void launch_saxpy_fp64(const DevMesh &M, const DevState &S, double a, double b,
                        cudaStream_t st);

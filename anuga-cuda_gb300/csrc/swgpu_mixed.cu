@@ -431,6 +431,8 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
         X.wlo[k] = wl;
         X.uvel[k] = uv;
         X.vvel[k] = vv;
+        if ((flags & kTrack) && (stg.kind == kStageEuler || stg.kind == kStageLast))
+            track_depth(S, k, h, step_end_time(ctrl, clk, stg), P.track_threshold);
     }
     if (bad) set_status(ctrl, SWGPU_EDENOMINATOR);
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);

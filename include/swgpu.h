@@ -227,6 +227,47 @@ typedef struct {
 int swgpu_get_launch_config(void *handle, swgpu_launch_config *config);
 int swgpu_set_launch_config(void *handle, const swgpu_launch_config *config);
 
+/* Per-triangle tracking over the device-resident loop: the maximum depth
+ * since the call and the first model time (end of a whole step) at which
+ * the depth exceeded threshold (-1: not yet).  on = 0 stops tracking.  The
+ * targets of the surrogate model; no counterpart in the reference. */
+int swgpu_set_tracking(void *handle, int on, double threshold);
+int swgpu_get_tracking(void *handle, float *max_depth, float *arrival_time);
+
+/* ---- BF16 MLP surrogate (swgpu_mlp_*) ---------------------------------
+ * A 16 -> 128 -> 128 -> 2 ReLU network predicting per (scenario, triangle)
+ * row the normalised maximum depth and arrival time from 9 scenario
+ * parameters and the triangle's bed, centroid and distance to the source;
+ * BF16 weights and activations on mma.sync tensor cores with FP32
+ * accumulation, FP32 master weights trained by Adam.  params is the flat
+ * FP32 vector W1 [16][128], b1 [128], W2 [128][128], b2 [128], W3 [128][2],
+ * b3 [2] (swgpu_mlp_num_params() floats, in-major weights); the feature
+ * map is (raw - mean) * inv_std over 16 features (the last 3 are zero).
+ * Handles use the current device and their own stream.  No counterpart in
+ * the reference. */
+int swgpu_mlp_num_params(void);
+int swgpu_mlp_create(const float *params, const float *feature_mean,
+                     const float *feature_inv_std, void **mlp_out);
+int swgpu_mlp_destroy(void *mlp);
+const char *swgpu_mlp_last_error(void *mlp);
+/* tri_xyz [ntri][3]: centroid x, y and bed; scen [nscen][9]; targets
+ * [nscen][ntri][2] (may be NULL for prediction only). */
+int swgpu_mlp_set_data(void *mlp, const float *tri_xyz, int64_t ntri, const float *scen,
+                       int64_t nscen, const float *targets);
+/* rows row0 .. row0+nrows-1 (row = scenario * ntri + triangle) into a
+ * DEVICE buffer out [nrows][2]; *elapsed_ms (may be NULL) = kernel time. */
+int swgpu_mlp_predict(void *mlp, int64_t row0, int64_t nrows, float *out_device,
+                      float *elapsed_ms);
+/* Outputs [nrows][2], gradient of the loss (flat like params) and loss of
+ * the given rows, without updating: mean over rows of
+ * w_depth (y0 - t0)^2 + w_arrival (y1 - t1)^2. */
+int swgpu_mlp_gradients(void *mlp, const int64_t *rows, int64_t nrows, float w_depth,
+                        float w_arrival, float *outputs, float *grad, float *loss);
+/* steps Adam steps on random batches of batch rows (seeded). */
+int swgpu_mlp_train(void *mlp, int steps, int64_t batch, uint64_t seed, float lr,
+                    float w_depth, float w_arrival, float *last_loss, float *elapsed_ms);
+int swgpu_mlp_get_params(void *mlp, float *params);
+
 /* Frees everything the handle owns.  No counterpart in the reference (its
  * PyCUDA allocations are released by the garbage collector). */
 int swgpu_destroy(void *handle);

@@ -189,3 +189,33 @@ def test_degenerate_timestep_protection(swgpu_built):
     assert u[k] == 0.0
     with pytest.raises(NotImplementedError):
         next(iter(d.evolve(yieldstep=1.0, finaltime=1.0)))
+
+
+def test_tracking_matches_stepwise(swgpu_built):
+    """Maximum depth and arrival time kept on the device equal those taken
+    from the state after every step (FP64, Euler and RK2)."""
+    import ctypes as C
+    from anuga_cuda import DEFAULT, scenarios
+    from anuga_cuda._lib import State_t, check, lib
+    sc = scenarios.channel_inflow(14, 5, seed=2)
+    zc = sc.elevation_arrays()[0]
+    for method in ("euler", "rk2"):
+        a = gpu_from_scenario(sc, DEFAULT)
+        b = gpu_from_scenario(sc, DEFAULT)
+        for d in (a, b):
+            d.set_timestepping_method(method)
+            d.evolve_steps(0)
+        a.set_tracking(0.02)
+        st = State_t()
+        check(lib().swgpu_evolve_run(a._h, 60, C.byref(st)), a._h)
+        hmax = np.zeros(sc.N, dtype=np.float32)
+        tarr = np.full(sc.N, -1.0, dtype=np.float32)
+        for _ in range(60):
+            b.step()
+            h = b.quantities["stage"].centroid_values - zc
+            hmax = np.maximum(hmax, h.astype(np.float32))
+            new = (h > 0.02) & (tarr < 0)
+            tarr[new] = np.float32(b.get_time())
+        hm, ta = a.get_tracking()
+        assert np.array_equal(hm, hmax) and np.array_equal(ta, tarr), method
+        assert (ta > 0).any() and (ta < 0).any()

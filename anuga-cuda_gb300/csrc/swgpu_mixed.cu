@@ -387,20 +387,27 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int bad = 0, nonfinite = 0;
     if (k < M.N) {
-        double h = X.hd[k], uh = S.uh[k], vh = S.vh[k];
-        if (stg.kind == kStageFirst) {  // backup_conserved_quantities (depth, momenta)
-            S.bw[k] = h;
-            S.buh[k] = uh;
-            S.bvh[k] = vh;
+        // every load first (this thread is the only writer of element k)
+        const double h0 = ro(X.hd + k), uh0 = ro(S.uh + k), vh0 = ro(S.vh + k);
+        double h = h0, uh = uh0, vh = vh0;
+        const bool combine = stg.kind == kStageMid || stg.kind == kStageLast;
+        double bh = 0.0, bu = 0.0, bv = 0.0;
+        if (combine) {
+            bh = ro(S.bw + k);
+            bu = ro(S.buh + k);
+            bv = ro(S.bvh + k);
         }
         const float mah = P.f_mah;
         const float hf0 = ro(X.hf + k);  // FP32 copies of the pre-update state
         const float uf = ro(X.uvel + k) * omaxf(hf0, mah);
         const float vf = ro(X.vvel + k) * omaxf(hf0, mah);
+        const float ew = ro(X.ew + k), euh = ro(X.euh + k), evh = ro(X.evh + k);
+        const float zmoff = ro(X.zmoff + k);
+        const double zc = ro(S.zc + k);
         float rm1 = 0.0f, r = 1.0f;  // r - 1 and r
         const float eta = ro(X.fric + k);
         if (eta > mah) {
-            const float hm = hf0 - ro(X.zmoff + k);
+            const float hm = hf0 - zmoff;
             if (hm >= mah) {
                 const float Sf = -P.f_g * eta * eta * sqrtf(uf * uf + vf * vf) *
                                  exp2f(-(7.0f / 3.0f) * __log2f(hm));
@@ -411,18 +418,23 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
                 rm1 = dS * r;  // r - 1 without cancellation
             }
         }
-        h += widen(dtf * ro(X.ew + k));
-        uh += widen(uf * rm1 + dtf * ro(X.euh + k) * r);
-        vh += widen(vf * rm1 + dtf * ro(X.evh + k) * r);
-        if (stg.kind == kStageMid || stg.kind == kStageLast) {
+        h += widen(dtf * ew);
+        uh += widen(uf * rm1 + dtf * euh * r);
+        vh += widen(vf * rm1 + dtf * evh * r);
+        if (combine) {
             // saxpy_conserved_quantities in FP64 on depth: with a + b = 1 it
             // is the stage saxpy minus the (unchanged) bed
-            h = stg.a * h + stg.b * S.bw[k];
-            uh = stg.a * uh + stg.b * S.buh[k];
-            vh = stg.a * vh + stg.b * S.bvh[k];
+            h = stg.a * h + stg.b * bh;
+            uh = stg.a * uh + stg.b * bu;
+            vh = stg.a * vh + stg.b * bv;
         }
         float hf, wf, wl, uv, vv;
-        finish_state(P, h, uh, vh, ro(S.zc + k), hf, wf, wl, uv, vv, nonfinite);
+        finish_state(P, h, uh, vh, zc, hf, wf, wl, uv, vv, nonfinite);
+        if (stg.kind == kStageFirst) {  // backup_conserved_quantities (depth, momenta)
+            S.bw[k] = h0;
+            S.buh[k] = uh0;
+            S.bvh[k] = vh0;
+        }
         X.hd[k] = h;
         S.uh[k] = uh;
         S.vh[k] = vh;
@@ -503,7 +515,27 @@ __device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], floa
     limit_f(d, qmin, qmax, beta);
 }
 
-// Extrapolation + balance + boundary conditions, FP32, in stage jumps.
+// The distribute kernel's own data for one tile of BS triangles, filled by
+// 17 bulk copies.
+template <int BS>
+struct __align__(128) DistTile {
+    float wf[BS], wlo[BS], hf[BS], uvel[BS], vvel[BS];
+    float gc[6][BS];
+    float dzv[3][BS];
+    float dze[3][BS];
+};
+
+// Centroid value of neighbour n: from the tile when n is one of the block's
+// triangles (most, in Morton order), else from global memory.
+__device__ __forceinline__ float tile_or_global(const float *tile, const float *plane, int n,
+                                                int kb, int cnt) {
+    const int ln = n - kb;
+    return (unsigned)ln < (unsigned)cnt ? tile[ln] : ro(plane + n);
+}
+
+// Extrapolation + balance + boundary conditions, FP32, in stage jumps.  Each
+// block stages its tile's own planes with one-dimensional TMA bulk copies
+// into shared memory and reads in-tile neighbours from there.
 template <int BS>
 __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, DevState S, DevMixed X,
                                                            DevParams P, const BcTag *tags,
@@ -511,35 +543,67 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
     const bool fused = flags & kFused;
     ctrl = block_ctrl(ctrl, M);
     if (fused && ctrl_halted(ctrl)) return;
+    __shared__ DistTile<BS> T;
+    __shared__ __align__(8) unsigned long long bar;
     const int N = M.N, SP = X.S;
     const int order = (int)ctrl->order;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tid = threadIdx.x;
+    const int kb = blockIdx.x * BS;
+    const int cnt = min(BS, N - kb);
+    const int span = min(BS, SP - kb);  // a multiple of 64 elements
+    const int k = kb + tid;
+    if (tid == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned bytes = (unsigned)span * 4u;
+        mbar_arrive_expect_tx(&bar, 17u * bytes);
+        bulk_load(T.wf, X.wf + kb, bytes, &bar);
+        bulk_load(T.wlo, X.wlo + kb, bytes, &bar);
+        bulk_load(T.hf, X.hf + kb, bytes, &bar);
+        bulk_load(T.uvel, X.uvel + kb, bytes, &bar);
+        bulk_load(T.vvel, X.vvel + kb, bytes, &bar);
+#pragma unroll
+        for (int j = 0; j < 6; j++) bulk_load(T.gc[j], X.gc + j * SP + kb, bytes, &bar);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            bulk_load(T.dzv[i], X.dzv + i * SP + kb, bytes, &bar);
+            bulk_load(T.dze[i], X.dze + i * SP + kb, bytes, &bar);
+        }
+    }
+    // index planes are not padded: ordinary loads while the copies fly
+    int sur[3] = {0, 0, 0}, kind = 2;
+    if (tid < cnt) {
+        kind = ro(X.kind + k);
+#pragma unroll
+        for (int i = 0; i < 3; i++) sur[i] = ro(M.surr + i * N + k);
+    }
+    const bool arrived = mbar_wait_bounded(&bar, ctrl);
     int bad_bc = 0;
-    if (k < N) {
+    if (arrived && tid < cnt) {
         const float mah = P.f_mah;
-        const float wk = ro(X.wf + k), lk = ro(X.wlo + k), hc = ro(X.hf + k);
-        const float qu = ro(X.uvel + k), qv = ro(X.vvel + k);
+        const float wk = T.wf[tid], lk = T.wlo[tid], hc = T.hf[tid];
+        const float qu = T.uvel[tid], qv = T.vvel[tid];
         const bool vel = P.extrapolate_velocity_second_order == 1;
         const float hk = omaxf(hc, mah);
         const float uk = qu * hk, vk = qv * hk;  // centroid momentum
         float dzv[3];
 #pragma unroll
-        for (int i = 0; i < 3; i++) dzv[i] = ro(X.dzv + i * SP + k);
+        for (int i = 0; i < 3; i++) dzv[i] = T.dzv[i][tid];
         float dw[3] = {0.f, 0.f, 0.f};  // vertex stage jumps
         float ou[3], ov[3];             // vertex momentum (or velocity)
         if (order != 1) {
-            const int kind = ro(X.kind + k);
             const float cu = vel ? qu : uk, cv = vel ? qv : vk;
             float du[3] = {0.f, 0.f, 0.f}, dv[3] = {0.f, 0.f, 0.f};
             bool keep = false;  // dry neighbourhood: previous vertex values stay
             if ((kind & 3) != 2) {
                 float c[6];
 #pragma unroll
-                for (int j = 0; j < 6; j++) c[j] = ro(X.gc + j * SP + k);
+                for (int j = 0; j < 6; j++) c[j] = T.gc[j][tid];
                 if ((kind & 3) == 0) {
-                    const int k0 = ro(M.surr + k), k1 = ro(M.surr + N + k),
-                              k2 = ro(M.surr + 2 * N + k);
-                    const float h0 = ro(X.hf + k0), h1 = ro(X.hf + k1), h2 = ro(X.hf + k2);
+                    const int k0 = sur[0], k1 = sur[1], k2 = sur[2];
+                    const float h0 = tile_or_global(T.hf, X.hf, k0, kb, cnt);
+                    const float h1 = tile_or_global(T.hf, X.hf, k1, kb, cnt);
+                    const float h2 = tile_or_global(T.hf, X.hf, k2, kb, cnt);
                     const float hmin = ominf(ominf(h0, ominf(h1, h2)), hc);
                     const float hmax = omaxf(h0, omaxf(h1, h2));
                     if (P.optimise_dry_cells && hmax < P.f_eps) {
@@ -547,12 +611,20 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
                     } else {
                         float hfactor = 0.0f;
                         if (hmin > 0.001f) hfactor = (hmin - 0.001f) / (hmin + 0.004f);
-                        const float w0 = ro(X.wf + k0), w1 = ro(X.wf + k1), w2 = ro(X.wf + k2);
-                        const float l0 = ro(X.wlo + k0), l1 = ro(X.wlo + k1), l2 = ro(X.wlo + k2);
+                        const float w0 = tile_or_global(T.wf, X.wf, k0, kb, cnt);
+                        const float w1 = tile_or_global(T.wf, X.wf, k1, kb, cnt);
+                        const float w2 = tile_or_global(T.wf, X.wf, k2, kb, cnt);
+                        const float l0 = tile_or_global(T.wlo, X.wlo, k0, kb, cnt);
+                        const float l1 = tile_or_global(T.wlo, X.wlo, k1, kb, cnt);
+                        const float l2 = tile_or_global(T.wlo, X.wlo, k2, kb, cnt);
                         aux_jumps_f((w0 - wk) + (l0 - lk), (w1 - w0) + (l1 - l0), (w2 - w0) + (l2 - l0), c,
                                     P.f_beta_w_dry + (P.f_beta_w - P.f_beta_w_dry) * hfactor, dw);
-                        float u0 = ro(X.uvel + k0), u1 = ro(X.uvel + k1), u2 = ro(X.uvel + k2);
-                        float v0 = ro(X.vvel + k0), v1 = ro(X.vvel + k1), v2 = ro(X.vvel + k2);
+                        float u0 = tile_or_global(T.uvel, X.uvel, k0, kb, cnt);
+                        float u1 = tile_or_global(T.uvel, X.uvel, k1, kb, cnt);
+                        float u2 = tile_or_global(T.uvel, X.uvel, k2, kb, cnt);
+                        float v0 = tile_or_global(T.vvel, X.vvel, k0, kb, cnt);
+                        float v1 = tile_or_global(T.vvel, X.vvel, k1, kb, cnt);
+                        float v2 = tile_or_global(T.vvel, X.vvel, k2, kb, cnt);
                         if (!vel) {
                             u0 *= omaxf(h0, mah);
                             v0 *= omaxf(h0, mah);
@@ -568,11 +640,14 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
                     }
                 } else {
                     const int slot = (kind >> 2) & 3;
-                    const int k1 = ro(M.surr + slot * N + k);
-                    const float h1 = ro(X.hf + k1);
+                    const int k1 = sur[slot];
+                    const float h1 = tile_or_global(T.hf, X.hf, k1, kb, cnt);
                     const float beta = P.f_beta_w;
-                    one_jumps_f((ro(X.wf + k1) - wk) + (ro(X.wlo + k1) - lk), c, beta, dw);
-                    float u1 = ro(X.uvel + k1), v1 = ro(X.vvel + k1);
+                    one_jumps_f((tile_or_global(T.wf, X.wf, k1, kb, cnt) - wk) +
+                                    (tile_or_global(T.wlo, X.wlo, k1, kb, cnt) - lk),
+                                c, beta, dw);
+                    float u1 = tile_or_global(T.uvel, X.uvel, k1, kb, cnt);
+                    float v1 = tile_or_global(T.vvel, X.vvel, k1, kb, cnt);
                     if (!vel) {
                         u1 *= omaxf(h1, mah);
                         v1 *= omaxf(h1, mah);
@@ -666,7 +741,7 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-            hle_[i] = edge_depth(hc, dw[a], dw[b], ro(X.dze + i * SP + k));
+            hle_[i] = edge_depth(hc, dw[a], dw[b], T.dze[i][tid]);
             X.he[i * SP + k] = hle_[i];
             X.dwe[i * SP + k] = 0.5f * (dw[a] + dw[b]);
             X.uhe[i * SP + k] = 0.5f * (ou[a] + ou[b]);

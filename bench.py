@@ -71,6 +71,13 @@ def parse():
     ap.add_argument("--ensemble", type=int, default=32,
                     help="scenarios of the batched-ensemble measurement (0: skip)")
     ap.add_argument("--ensemble-finaltime", type=float, default=3600.0)
+    ap.add_argument("--surrogate", action="store_true",
+                    help="also measure the BF16 MLP surrogate (trains on solver runs)")
+    ap.add_argument("--surrogate-cells", type=int, default=224)
+    ap.add_argument("--surrogate-train", type=int, default=2048)
+    ap.add_argument("--surrogate-test", type=int, default=512)
+    ap.add_argument("--surrogate-finaltime", type=float, default=300.0)
+    ap.add_argument("--surrogate-steps", type=int, default=4000)
     return ap.parse_args()
 
 
@@ -284,6 +291,37 @@ def run_ensemble(count, finaltime):
                         "peak U[50,500] m3/s rise U[300,1800] s, n U[0.01,0.05], seed 4"}
 
 
+def run_surrogate(args):
+    """The surrogate workflow on one mesh of the wet/dry family: solver runs
+    (batched ensembles, mixed precision, tracking) for the training and the
+    held-out parameter sets (seeds 5000 and 9000), BF16 MLP training,
+    inference on the held-out set, and the 5 cm block fallback report."""
+    import numpy as np
+    from anuga_cuda import surrogate as SG
+    t0 = time.perf_counter()
+    fm = SG.FamilyMesh(cells=args.surrogate_cells)
+    T = args.surrogate_finaltime
+    th_train = SG.sample_params(args.surrogate_train, seed=5000)
+    th_test = SG.sample_params(args.surrogate_test, seed=9000)
+    hm, ta, ms_train = SG.solve(fm, th_train, finaltime=T, batch=32)
+    hmt, tat, ms_test = SG.solve(fm, th_test, finaltime=T, batch=32)
+    solve_wall = time.perf_counter() - t0
+    sg = SG.Surrogate(fm, seed=1)
+    fit = sg.fit(th_train, SG.targets_from(fm, th_train, hm, ta, T),
+                 steps=args.surrogate_steps, batch=65536, lr=2e-3)
+    depth, arr, infer_ms = sg.predict(th_test)
+    rep = SG.fallback_report(depth, hmt, ms_test / len(th_test), infer_ms)
+    return {"mesh_triangles": fm.N, "train_scenarios": len(th_train),
+            "test_scenarios": len(th_test), "finaltime_s": T,
+            "solver_ms_per_scenario": ms_test / len(th_test),
+            "train_samples_per_s": fit["samples_per_s"], "train_steps": fit["steps"],
+            "train_batch": fit["batch"], "train_loss": fit["loss"],
+            "inference_scenarios_per_s": len(th_test) / (infer_ms / 1000.0),
+            "inference_rows_per_s": len(th_test) * fm.N / (infer_ms / 1000.0),
+            "baseline_mae_m": float(np.abs(hmt - hm.mean(axis=0)[None]).mean()),
+            "solver_wall_s": solve_wall, **rep}
+
+
 def cpu_oracle_rate(sc, seconds=12.0, warm_steps=1):
     """Serial CPU oracle on the same workload for a bounded time."""
     from anuga_cuda import DEFAULT
@@ -410,6 +448,8 @@ def main():
                                           f"({wall:.1f} s) on one core"}
     if args.ensemble > 0:
         line["ensemble"] = run_ensemble(args.ensemble, args.ensemble_finaltime)
+    if args.surrogate:
+        line["surrogate"] = run_surrogate(args)
     print(json.dumps(line))
 
 

@@ -52,7 +52,13 @@ class Ensemble:
     def __init__(self, scenarios, parameters: Parameters | None = None, precision="mixed"):
         if not scenarios:
             raise ValueError("an ensemble needs at least one scenario")
-        self.scenarios = list(scenarios)
+        scenarios = list(scenarios)
+        # Internally the scenarios expected to run longest (the largest
+        # meshes: smallest triangles, smallest steps) come first, so that
+        # the launches can stop short of the finished ones at the end;
+        # every per-scenario input and output is in the caller's order.
+        self.order = sorted(range(len(scenarios)), key=lambda i: -scenarios[i].N)
+        self.scenarios = [scenarios[i] for i in self.order]
         self.parameters = parameters or DEFAULT
         self.precision = precision
         self._build_arrays()
@@ -188,7 +194,8 @@ class Ensemble:
         """Run every scenario from ``starttime`` to its finaltime (a scalar
         or one per scenario), or for at most ``max_steps`` steps; returns
         the per-scenario states."""
-        ft = np.broadcast_to(np.asarray(finaltime, dtype=np.float64), (len(self),)).copy()
+        ft = self._internal(np.broadcast_to(np.asarray(finaltime, dtype=np.float64),
+                                            (len(self),)))
         big = float(ft.max())
         check(lib().swgpu_evolve_start(self._h, float(starttime), big, big), self._h)
         check(lib().swgpu_ensemble_set_finaltimes(self._h, f64p(ft)), self._h)
@@ -200,7 +207,8 @@ class Ensemble:
     def run_timed(self, finaltime, starttime=0.0):
         """As evolve (to finaltime), returning the device time of the run in
         milliseconds (CUDA events around the graph launches)."""
-        ft = np.broadcast_to(np.asarray(finaltime, dtype=np.float64), (len(self),)).copy()
+        ft = self._internal(np.broadcast_to(np.asarray(finaltime, dtype=np.float64),
+                                            (len(self),)))
         big = float(ft.max())
         check(lib().swgpu_evolve_start(self._h, float(starttime), big, big), self._h)
         check(lib().swgpu_ensemble_set_finaltimes(self._h, f64p(ft)), self._h)
@@ -209,13 +217,25 @@ class Ensemble:
         check(lib().swgpu_evolve_run_timed(self._h, 0, C.byref(st), C.byref(ms)), self._h)
         return ms.value
 
+    def _internal(self, per_scenario):
+        """A per-scenario array in the caller's order -> internal order."""
+        a = np.asarray(per_scenario)
+        return np.ascontiguousarray(a[self.order])
+
+    def _user(self, items):
+        """A per-scenario list in internal order -> the caller's order."""
+        out = [None] * len(items)
+        for j, i in enumerate(self.order):
+            out[i] = items[j]
+        return out
+
     def states(self):
         out = []
         for s in range(len(self)):
             st = _lib.State_t()
             check(lib().swgpu_ensemble_get_state(self._h, s, C.byref(st)), self._h)
             out.append(st)
-        return out
+        return self._user(out)
 
     def set_tracking(self, threshold=0.01, on=True):
         """Maximum depth and arrival time tracking for every scenario."""
@@ -227,12 +247,12 @@ class Ensemble:
         ta = np.empty(self.N, dtype=np.float32)
         check(lib().swgpu_get_tracking(self._h, hm.ctypes.data_as(C.POINTER(C.c_float)),
                                        ta.ctypes.data_as(C.POINTER(C.c_float))), self._h)
-        return [(hm[a:b].copy(), ta[a:b].copy()) for a, b in self.ranges]
+        return self._user([(hm[a:b].copy(), ta[a:b].copy()) for a, b in self.ranges])
 
     def masses(self):
         m = np.empty(len(self))
         check(lib().swgpu_ensemble_mass(self._h, f64p(m)), self._h)
-        return m
+        return np.array(self._user(list(m)))
 
     def centroid_values(self, name):
         """Centroid values of quantity ``name`` for every scenario (a list of
@@ -242,4 +262,4 @@ class Ensemble:
                "xvelocity": _lib.XVELOCITY, "yvelocity": _lib.YVELOCITY}[name]
         c = np.empty(self.N)
         check(lib().swgpu_get_quantity(self._h, qid, f64p(c), None, None), self._h)
-        return [c[a:b].copy() for a, b in self.ranges]
+        return self._user([c[a:b].copy() for a, b in self.ranges])

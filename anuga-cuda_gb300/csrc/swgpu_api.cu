@@ -405,6 +405,7 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     const size_t n1 = N, n3 = 3 * N, n6 = 6 * N, nb1 = Nb;
     DevMesh &M = h->M;
     M.N = (int)N;
+    M.n_launch = (int)N;
     M.Nb = (int)Nb;
     int *d_nbr, *d_surr, *d_bcell, *d_bedge, *d_btag;
     uint8_t *d_nb, *d_order, *d_full;
@@ -614,6 +615,8 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     TRY(dalloc(h, &h->d_tags, (size_t)std::max(h->ntags, 1)));  // zero = reflective
     TRY(dalloc(h, &h->d_ctrl, (size_t)h->nscen));
     TRY(dalloc(h, &h->d_summary, 1));
+    const int nwords = (h->nscen + 31) / 32;
+    TRY(dalloc(h, &h->d_halt_bits, (size_t)nwords));
     TRY(dalloc(h, &h->d_scalar, 4));
     if (offsets) {
         const int64_t nblk = N / 256;
@@ -627,6 +630,8 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     {
         cudaError_t e = cudaMallocHost((void **)&h->h_ctrl, sizeof(Ctrl) * h->nscen);
         if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_summary, sizeof(RunSummary));
+        if (e == cudaSuccess)
+            e = cudaMallocHost((void **)&h->h_halt_bits, sizeof(unsigned) * ((h->nscen + 31) / 32));
         if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_scalar, 4 * sizeof(double));
         if (e != cudaSuccess) {
             fail(h, SWGPU_ENOMEM, "pinned host allocation: %s", cudaGetErrorString(e));
@@ -649,6 +654,8 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         c->rec_min = P.evolve_max_timestep;
         c->budget = -1;
         c->summary = h->d_summary;
+        c->halt_bits = h->d_halt_bits;
+        c->scen = i;
         reset_ftmin(c, P);
     }
     set_block_counts(h);
@@ -680,6 +687,7 @@ int swgpu_destroy(void *handle) {
     for (void *p : h->allocs) cudaFree(p);
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
     if (h->h_summary) cudaFreeHost(h->h_summary);
+    if (h->h_halt_bits) cudaFreeHost(h->h_halt_bits);
     if (h->h_scalar) cudaFreeHost(h->h_scalar);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -1212,6 +1220,19 @@ int swgpu_evolve_start(void *handle, double starttime, double yieldstep, double 
     return device_status(h);
 }
 
+// Triangles the fused-step kernels are launched over; a change drops the
+// captured graph (the stream must be idle).
+static int set_launch_extent(Handle *h, int n) {
+    if (h->M.n_launch == n) return SWGPU_OK;
+    if (h->graph) {
+        CK(cudaStreamSynchronize(h->stream));
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->M.n_launch = n;
+    return SWGPU_OK;
+}
+
 // Before a run: every scenario that has not reached its finaltime runs;
 // those that stopped at a yield move to the next yield point
 // (gpu_domain_advanced.py:2649-2654).
@@ -1243,12 +1264,19 @@ static int prepare_run(Handle *h, int64_t max_steps) {
     h->h_summary->halted = h->nscen - running;
     h->h_summary->status = 0;
     if ((rc = upload(h, h->d_summary, h->h_summary, 1))) return rc;
+    const int nwords = (h->nscen + 31) / 32;
+    for (int w = 0; w < nwords; w++) h->h_halt_bits[w] = 0u;
+    for (int i = 0; i < h->nscen; i++)
+        if (h->h_ctrl[i].halt) h->h_halt_bits[i >> 5] |= 1u << (i & 31);
+    if ((rc = upload(h, h->d_halt_bits, h->h_halt_bits, (size_t)nwords))) return rc;
+    if ((rc = set_launch_extent(h, h->M.N))) return rc;
     return push_ctrl(h);
 }
 
 static int finish_run(Handle *h, swgpu_state *state) {
     int rc = sync_ctrl(h);
     if (rc) return rc;
+    if ((rc = set_launch_extent(h, h->M.N))) return rc;
     for (int i = 0; i < h->nscen; i++)
         if (h->h_ctrl[i].stop_reason == kStopYield) h->resume_after_yield = true;
     if (state) fill_state(h->h_ctrl, state);
@@ -1337,6 +1365,12 @@ static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *
         e = cudaMemcpyAsync(h->h_summary, h->d_summary, sizeof(RunSummary),
                             cudaMemcpyDeviceToHost, h->stream);
         if (e != cudaSuccess) break;
+        if (h->nscen > 1) {
+            e = cudaMemcpyAsync(h->h_halt_bits, h->d_halt_bits,
+                                sizeof(unsigned) * ((h->nscen + 31) / 32),
+                                cudaMemcpyDeviceToHost, h->stream);
+            if (e != cudaSuccess) break;
+        }
         e = cudaEventRecord(ev[slot], h->stream);
         if (e != cudaSuccess) break;
         launched++;
@@ -1347,6 +1381,26 @@ static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *
             if (e != cudaSuccess) break;
             inflight--;
             if (h->h_summary->halted >= h->nscen || h->h_summary->status) halted = true;
+            if (!halted && h->nscen > 1) {
+                // ensembles: launch only up to the last scenario still running
+                // (longest-running scenarios are placed first) once that
+                // saves an eighth of the current launch
+                int last = h->nscen - 1;
+                while (last > 0 && (h->h_halt_bits[last >> 5] >> (last & 31) & 1u)) last--;
+                const int extent = (int)h->scen_offsets[(size_t)last + 1];
+                if (extent <= h->M.n_launch - h->M.n_launch / 8) {
+                    e = cudaStreamSynchronize(h->stream);
+                    if (e != cudaSuccess) break;
+                    inflight = 0;
+                    if ((rc = set_launch_extent(h, extent)) || (rc = build_graph(h))) {
+                        cudaEventDestroy(ev[0]);
+                        cudaEventDestroy(ev[1]);
+                        cudaEventDestroy(t0);
+                        cudaEventDestroy(t1);
+                        return rc;
+                    }
+                }
+            }
         }
     }
     if (e == cudaSuccess) e = cudaEventRecord(t1, h->stream);

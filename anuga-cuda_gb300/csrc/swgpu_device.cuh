@@ -303,6 +303,7 @@ __device__ __forceinline__ void apply_pending_halt(Ctrl *c) {
         c->halt = 1;
         c->halt_pending = 0;
         if (c->status) atomicCAS(&c->summary->status, 0, c->status);
+        atomicOr(&c->halt_bits[c->scen >> 5], 1u << (c->scen & 31));
         __threadfence();
         atomicAdd(&c->summary->halted, 1);
     }

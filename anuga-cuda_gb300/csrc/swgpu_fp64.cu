@@ -1238,7 +1238,7 @@ void launch_prepare_fp64(const DevMesh &M, const DevState &S, const DevParams &P
 // Block sizes of the fused-step kernels come from M.shape.
 void launch_distribute_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                             const BcTag *tags, Ctrl *ctrl, int flags, cudaStream_t st) {
-    const int bs = M.shape.distribute, g = (M.N + bs - 1) / bs;
+    const int bs = M.shape.distribute, g = (M.n_launch + bs - 1) / bs;
     if (P.flow_algorithm) {
         if (bs == 128)
             distribute_de_fp64<128><<<g, 128, 0, st>>>(M, S, P, tags, ctrl, flags);
@@ -1260,7 +1260,7 @@ void launch_boundary_fp64(const DevMesh &M, const DevState &S, const DevParams &
 }
 void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P, Ctrl *ctrl,
                       int flags, cudaStream_t st) {
-    const int bs = M.shape.flux, g = (M.N + bs - 1) / bs;
+    const int bs = M.shape.flux, g = (M.n_launch + bs - 1) / bs;
     if (bs == 64)
         flux_fp64<64><<<g, 64, 0, st>>>(M, S, P, ctrl, flags);
     else if (bs == 128)
@@ -1274,7 +1274,7 @@ void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P
 }
 void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P, Ctrl *ctrl,
                         double dt, int flags, const Stage &stage, cudaStream_t st) {
-    const int bs = M.shape.update, g = (M.N + bs - 1) / bs;
+    const int bs = M.shape.update, g = (M.n_launch + bs - 1) / bs;
     if (bs == 128)
         update_fp64<128><<<g, 128, 0, st>>>(M, S, P, ctrl, dt, flags, stage);
     else if (bs == 512)

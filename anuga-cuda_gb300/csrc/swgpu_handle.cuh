@@ -32,6 +32,8 @@ struct Handle {
     Ctrl *h_ctrl = nullptr;      // pinned mirror [nscen]
     RunSummary *d_summary = nullptr;
     RunSummary *h_summary = nullptr;  // pinned
+    unsigned int *d_halt_bits = nullptr;  // one bit per scenario
+    unsigned int *h_halt_bits = nullptr;  // pinned copy
     double *d_scalar = nullptr;  // mass / misc
     double *h_scalar = nullptr;  // pinned
     std::vector<void *> allocs;

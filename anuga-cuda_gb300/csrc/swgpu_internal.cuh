@@ -32,6 +32,8 @@ struct LaunchShape {
 
 struct DevMesh {
     int N, Nb;
+    int n_launch;  // triangles the fused-step kernels are launched over: N, or for an
+                   // ensemble the scenarios still running (they come first)
     LaunchShape shape;
     const int *nbr;            // [3][N] packed neighbour / boundary slot
     const int *surr;           // [3][N] surrogate neighbours
@@ -151,6 +153,8 @@ struct __align__(16) Ctrl {
     unsigned int blocks_update;     // ... in one update launch
     unsigned int blocks_distribute; // ... in one distribute launch
     RunSummary *summary;            // shared by all scenarios of a handle
+    unsigned int *halt_bits;        // one bit per scenario, set when it halts
+    int scen;                       // this scenario's index
 };
 
 enum StopReason { kStopNone = 0, kStopYield = 1, kStopFinal = 2, kStopBudget = 3, kStopError = 4 };

@@ -872,7 +872,7 @@ __global__ void mass_final_mixed(const double *partials, int n, double *out) {
 void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                              const DevParams &P, const BcTag *tags, Ctrl *ctrl, int flags,
                              cudaStream_t st) {
-    const int bs = M.shape.distribute, g = (M.N + bs - 1) / bs;
+    const int bs = M.shape.distribute, g = (M.n_launch + bs - 1) / bs;
     if (bs == 128)
         distribute_mixed<128><<<g, 128, 0, st>>>(M, S, X, P, tags, ctrl, flags);
     else if (bs == 512)
@@ -882,7 +882,7 @@ void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed
 }
 void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, const DevParams &P,
                        Ctrl *ctrl, int flags, cudaStream_t st) {
-    const int t = M.shape.flux, g = (M.N + t - 1) / t;
+    const int t = M.shape.flux, g = (M.n_launch + t - 1) / t;
     if (t == 64)
         flux_mixed<64><<<g, 64, 0, st>>>(M, X, P, ctrl, flags);
     else if (t == 256)
@@ -893,7 +893,7 @@ void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, co
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,
                          cudaStream_t st) {
-    const int bs = M.shape.update, g = (M.N + bs - 1) / bs;
+    const int bs = M.shape.update, g = (M.n_launch + bs - 1) / bs;
     if (bs == 128)
         update_mixed<128><<<g, 128, 0, st>>>(M, S, X, P, ctrl, flags, stage);
     else if (bs == 512)

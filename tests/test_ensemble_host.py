@@ -8,6 +8,7 @@ def _assembled(scs):
     from anuga_cuda.ensemble import Ensemble
     e = Ensemble.__new__(Ensemble)
     e.scenarios, e.parameters, e.precision = list(scs), DEFAULT, "mixed"
+    e.order = list(range(len(scs)))
     e._build_arrays()
     return e
 

@@ -36,12 +36,14 @@ def get_config(h) -> dict:
     c = _lib.LaunchConfig_t()
     check(lib().swgpu_get_launch_config(h, C.byref(c)), h)
     return {"flux_block": c.flux_block, "update_block": c.update_block,
-            "distribute_block": c.distribute_block, "steps_per_graph": c.steps_per_graph}
+            "distribute_block": c.distribute_block, "steps_per_graph": c.steps_per_graph,
+            "flux_pipelined": c.flux_pipelined}
 
 
 def set_config(h, cfg: dict) -> None:
     c = _lib.LaunchConfig_t(int(cfg["flux_block"]), int(cfg["update_block"]),
-                            int(cfg["distribute_block"]), int(cfg.get("steps_per_graph", 16)))
+                            int(cfg["distribute_block"]), int(cfg.get("steps_per_graph", 16)),
+                            int(cfg.get("flux_pipelined", 0)))
     check(lib().swgpu_set_launch_config(h, C.byref(c)), h)
 
 
@@ -67,11 +69,18 @@ def tune_handle(h, steps=24, candidates=None, ensemble=False) -> dict:
     best_ms = list(start)
     for kernel, values in cand.items():
         i = _KERNEL_INDEX[kernel]
-        for v in values:
-            if v == best[_FIELD[kernel]]:
+        trials = [{_FIELD[kernel]: v} for v in values if v != best[_FIELD[kernel]]]
+        if kernel == "flux":
+            # persistent double-buffered flux (mixed precision, tiles <= 128)
+            trials += [{"flux_block": v, "flux_pipelined": 1} for v in values if v <= 128]
+        for change in trials:
+            trial = dict(best, **change)
+            if trial == best:
                 continue
-            trial = dict(best, **{_FIELD[kernel]: v})
-            set_config(h, trial)
+            try:
+                set_config(h, trial)
+            except _lib.SwgpuError:
+                continue
             _kernel_ms(h, 2)
             t = _kernel_ms(h, steps)[i]
             if t < best_ms[i]:

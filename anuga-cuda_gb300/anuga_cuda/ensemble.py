@@ -29,7 +29,7 @@ from .boundaries import Reflective_boundary
 from .config import DEFAULT, Parameters
 from .mesh import Mesh
 
-__all__ = ["Ensemble", "ALIGN"]
+__all__ = ["Ensemble", "ALIGN", "shard"]
 
 ALIGN = 256   # scenario ranges start on multiples of this many triangles
 
@@ -37,6 +37,22 @@ _MESH_INT = ("neighbours", "neighbour_edges", "surrogate_neighbours", "number_of
              "tri_full_flag")
 _MESH_FLOAT = ("normals", "edgelengths", "radii", "areas", "vertex_coordinates",
                "centroid_coordinates")
+
+
+def shard(work, rank, world):
+    """Scenario indices of one rank when ``world`` processes (one per GPU)
+    split an ensemble: longest-processing-time-first assignment of the
+    per-scenario work estimates to the least loaded rank, deterministic, so
+    every rank computes the same partition without communicating.  The
+    ensemble path needs no exchange between ranks (weak in scenarios)."""
+    load = [0.0] * world
+    mine = []
+    for i in sorted(range(len(work)), key=lambda j: (-work[j], j)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        load[r] += float(work[i])
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
 
 
 def _pad_mesh():

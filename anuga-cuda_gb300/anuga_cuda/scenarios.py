@@ -383,18 +383,28 @@ def _inflow_harbour_args(args):
     return inflow_harbour(int(n), seed=int(seed * 100003 + i), peak=p, rise=r, friction=f)
 
 
-def ensemble_harbours(count=256, seed=4, nmin=5000, nmax=200000, processes=1):
-    """Ensemble scenarios: ``count`` inflow harbours with triangle counts
-    log-uniform in [nmin, nmax], hydrograph peak U[50, 500] m^3/s, rise
-    U[300, 1800] s and Manning n U[0.01, 0.05], all drawn from ``seed``.
-    ``processes`` > 1 builds the meshes in a pool of spawned processes."""
+def ensemble_harbour_specs(count=256, seed=4, nmin=5000, nmax=200000):
+    """The parameters of ``ensemble_harbours`` without building meshes:
+    (index, seed, triangles, peak, rise, friction) per scenario."""
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), count))
     peaks = rng.uniform(50.0, 500.0, count)
     rises = rng.uniform(300.0, 1800.0, count)
     frics = rng.uniform(0.01, 0.05, count)
-    args = [(i, seed, n, p, r, f) for i, (n, p, r, f) in
+    return [(i, seed, n, p, r, f) for i, (n, p, r, f) in
             enumerate(zip(sizes, peaks, rises, frics))]
+
+
+def ensemble_harbours(count=256, seed=4, nmin=5000, nmax=200000, processes=1, only=None):
+    """Ensemble scenarios: ``count`` inflow harbours with triangle counts
+    log-uniform in [nmin, nmax], hydrograph peak U[50, 500] m^3/s, rise
+    U[300, 1800] s and Manning n U[0.01, 0.05], all drawn from ``seed``.
+    ``only`` restricts to those scenario indices (one rank's shard);
+    ``processes`` > 1 builds the meshes in a pool of spawned processes."""
+    args = ensemble_harbour_specs(count, seed, nmin, nmax)
+    if only is not None:
+        args = [args[i] for i in only]
+    count = len(args)
     if processes and processes > 1 and count > 1:
         import multiprocessing as mp
         with mp.get_context("spawn").Pool(min(processes, count)) as pool:

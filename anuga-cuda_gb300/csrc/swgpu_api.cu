@@ -642,7 +642,12 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     }
     std::memset(h->h_ctrl, 0, sizeof(Ctrl) * h->nscen);
     std::memset(h->h_summary, 0, sizeof(RunSummary));
-    M.shape = LaunchShape{precision == SWGPU_MIXED ? 128 : kBlock, kBlock, kBlock};
+    {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+        M.shape = LaunchShape{precision == SWGPU_MIXED ? 128 : kBlock, kBlock, kBlock, 0,
+                              std::max(sms, 1)};
+    }
     for (int i = 0; i < h->nscen; i++) {
         Ctrl *c = &h->h_ctrl[i];
         c->order = P.default_order;
@@ -1082,6 +1087,7 @@ int swgpu_get_launch_config(void *handle, swgpu_launch_config *cfg) {
     cfg->update_block = h->M.shape.update;
     cfg->distribute_block = h->M.shape.distribute;
     cfg->steps_per_graph = h->steps_per_graph;
+    cfg->flux_pipelined = h->M.shape.pipelined;
     return SWGPU_OK;
 }
 
@@ -1099,17 +1105,21 @@ int swgpu_set_launch_config(void *handle, const swgpu_launch_config *cfg) {
     if (!one_of(cfg->flux_block, {64, 128, 256}) ||
         !one_of(cfg->update_block, {128, 256, 512}) ||
         !one_of(cfg->distribute_block, {128, 256, 512}) || cfg->update_block > top ||
-        cfg->distribute_block > top || cfg->steps_per_graph < 1 || cfg->steps_per_graph > 64)
+        cfg->distribute_block > top || cfg->steps_per_graph < 1 || cfg->steps_per_graph > 64 ||
+        (cfg->flux_pipelined && cfg->flux_block > 128))
         return fail(h, SWGPU_EINVAL,
-                    "launch config: flux 64/128/256, update and distribute 128/256/512 "
-                    "(at most 256 for an ensemble), 1..64 steps per graph");
+                    "launch config: flux 64/128/256 (at most 128 pipelined), update and "
+                    "distribute 128/256/512 (at most 256 for an ensemble), 1..64 steps per graph");
     int rc = sync_ctrl(h);
     if (rc) return rc;
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;  // recaptured with the new shape on the next run
     }
-    h->M.shape = LaunchShape{cfg->flux_block, cfg->update_block, cfg->distribute_block};
+    h->M.shape.flux = cfg->flux_block;
+    h->M.shape.update = cfg->update_block;
+    h->M.shape.distribute = cfg->distribute_block;
+    h->M.shape.pipelined = cfg->flux_pipelined ? 1 : 0;
     h->steps_per_graph = cfg->steps_per_graph;
     set_block_counts(h);
     return push_ctrl(h);

@@ -28,6 +28,8 @@ __host__ __device__ inline int pack_neighbour(int n, int m) { return (n << 2) | 
 // flux's TMA tile (64, 128, 256); update, distribute: 128, 256 or 512.
 struct LaunchShape {
     int flux, update, distribute;
+    int pipelined;  // mixed flux: persistent double-buffered blocks (tiles of 64 or 128)
+    int sms;        // multiprocessors of the device (persistent grid size)
 };
 
 struct DevMesh {

@@ -204,13 +204,19 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
 // more as long again so that copies still in flight land before the block
 // leaves.  Returns true when the data arrived.
 constexpr int kWaitLimit = 1 << 22;
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, Ctrl *ctrl) {
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, Ctrl *ctrl,
+                                                  unsigned parity = 0) {
     for (int it = 0; it < kWaitLimit; ++it)
-        if (mbar_try_wait(bar, 0)) return true;
+        if (mbar_try_wait(bar, parity)) return true;
     set_status(ctrl, SWGPU_ETIMEOUT);
     for (int it = 0; it < kWaitLimit; ++it)
-        if (mbar_try_wait(bar, 0)) break;
+        if (mbar_try_wait(bar, parity)) break;
     return false;
+}
+// Orders this thread's earlier generic-proxy accesses to shared memory
+// before later async-proxy (bulk copy) writes to it.
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // The flux kernel's own data for one tile of TILE triangles (= threads per
@@ -221,6 +227,103 @@ struct __align__(128) FluxTile {
     float he[3][TILE], dwe[3][TILE], uhe[3][TILE], vhe[3][TILE];
     float nx[3][TILE], ny[3][TILE], len[3][TILE];
 };
+
+// The 26 bulk copies of a flux tile starting at triangle k0 (span elements
+// of each padded plane), completing on bar.  Called by one thread.
+template <int TILE>
+__device__ __forceinline__ void flux_tile_issue(const DevMixed &X, FluxTile<TILE> &T, int k0,
+                                                int span, unsigned long long *bar) {
+    const int SP = X.S;
+    const unsigned bytes = (unsigned)span * 4u;
+    mbar_arrive_expect_tx(bar, 26u * bytes);
+    bulk_load(T.wf, X.wf + k0, bytes, bar);
+    bulk_load(T.wlo, X.wlo + k0, bytes, bar);
+    bulk_load(T.hf, X.hf + k0, bytes, bar);
+    bulk_load(T.radius, X.radius + k0, bytes, bar);
+    bulk_load(T.inv_area, X.inv_area + k0, bytes, bar);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        bulk_load(T.he[i], X.he + i * SP + k0, bytes, bar);
+        bulk_load(T.dwe[i], X.dwe + i * SP + k0, bytes, bar);
+        bulk_load(T.uhe[i], X.uhe + i * SP + k0, bytes, bar);
+        bulk_load(T.vhe[i], X.vhe + i * SP + k0, bytes, bar);
+        bulk_load(T.nx[i], X.nx + i * SP + k0, bytes, bar);
+        bulk_load(T.ny[i], X.ny + i * SP + k0, bytes, bar);
+        bulk_load(T.len[i], X.len + i * SP + k0, bytes, bar);
+    }
+}
+
+// Fluxes + gravity_wb of triangle k0 + tid of a staged tile (cnt valid
+// triangles; pk: its packed neighbours); stores the explicit updates and
+// returns the triangle's CFL timestep bound.
+template <int TILE>
+__device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const DevParams &P,
+                                                    const FluxTile<TILE> &T, int k0, int cnt,
+                                                    const int (&pk)[3]) {
+    const int SP = X.S;
+    const int tid = threadIdx.x;
+    const int k = k0 + tid;
+    float t = P.f_max_dt;
+    const float eps = P.f_eps;
+    const float wk = T.wf[tid], lk = T.wlo[tid], hc = T.hf[tid];
+    const float rk = T.radius[tid];
+    const float inv_area = T.inv_area[tid];
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // flux sums
+    float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float n1 = T.nx[i][tid], n2 = T.ny[i][tid], L = T.len[i][tid];
+        const float dwl = T.dwe[i][tid], hl = T.he[i][tid];
+        const float uhl = T.uhe[i][tid], vhl = T.vhe[i][tid];
+        float hr, uhr, vhr, jump, rn = 3.0e38f;
+        if (pk[i] >= 0) {
+            // the neighbour's stored edge state: the very numbers it uses
+            // itself, so both sides see the same two states
+            const int n = pk[i] >> 2, m = pk[i] & 3;
+            const int ln = n - k0;
+            float wn, lnn, dwn;
+            if ((unsigned)ln < (unsigned)cnt) {
+                hr = T.he[m][ln];
+                dwn = T.dwe[m][ln];
+                uhr = T.uhe[m][ln];
+                vhr = T.vhe[m][ln];
+                wn = T.wf[ln];
+                lnn = T.wlo[ln];
+                rn = T.radius[ln];
+            } else {
+                hr = ro(X.he + m * SP + n);
+                dwn = ro(X.dwe + m * SP + n);
+                uhr = ro(X.uhe + m * SP + n);
+                vhr = ro(X.vhe + m * SP + n);
+                wn = ro(X.wf + n);
+                lnn = ro(X.wlo + n);
+                rn = ro(X.radius + n);
+            }
+            jump = ((wn - wk) + (lnn - lk)) + (dwn - dwl);
+        } else {
+            const int mb = -pk[i] - 1;
+            hr = ro(X.hbf + mb);
+            jump = ro(X.wjb + mb);
+            uhr = ro(X.uhbf + mb);
+            vhr = ro(X.vhbf + mb);
+        }
+        gx += dwl * L * n1;
+        gy += dwl * L * n2;
+        if (P.optimise_dry_cells && fabsf(hl) < eps && fabsf(hr) < eps) continue;
+        float f0, f1, f2, ms;
+        edge_flux_dev(hl, uhl, vhl, hr, uhr, vhr, jump, n1, n2, P, f0, f1, f2, ms);
+        a0 -= f0 * L;
+        a1 -= f1 * L;
+        a2 -= f2 * L;
+        // min(rk/ms, rn/ms) = min(rk, rn)/ms: one division per edge
+        if (ms > eps) t = ominf(t, __fdividef(fminf(rk, rn), ms));
+    }
+    const float ghc = P.f_g * hc;
+    X.ew[k] = a0 * inv_area;
+    X.euh[k] = (a1 - ghc * gx) * inv_area;
+    X.evh[k] = (a2 - ghc * gy) * inv_area;
+    return t;
+}
 
 // Fluxes + gravity_wb, FP32, triangle centric (no atomics).  Each block
 // stages its tile of TILE triangles with one-dimensional TMA bulk copies into
@@ -233,107 +336,82 @@ __global__ void __launch_bounds__(TILE) flux_mixed(DevMesh M, DevMixed X, DevPar
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     __shared__ FluxTile<TILE> T;
     __shared__ __align__(8) unsigned long long bar;
-    const int N = M.N, SP = X.S;
+    const int N = M.N;
     const int tid = threadIdx.x;
     const int k0 = blockIdx.x * TILE;
     const int cnt = min(TILE, N - k0);
-    // tile length in the padded planes (a multiple of 64 elements)
-    const int span = min(TILE, SP - k0);
     if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
-    if (tid == 0) {
-        const unsigned bytes = (unsigned)span * 4u;
-        mbar_arrive_expect_tx(&bar, 26u * bytes);
-        bulk_load(T.wf, X.wf + k0, bytes, &bar);
-        bulk_load(T.wlo, X.wlo + k0, bytes, &bar);
-        bulk_load(T.hf, X.hf + k0, bytes, &bar);
-        bulk_load(T.radius, X.radius + k0, bytes, &bar);
-        bulk_load(T.inv_area, X.inv_area + k0, bytes, &bar);
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            bulk_load(T.he[i], X.he + i * SP + k0, bytes, &bar);
-            bulk_load(T.dwe[i], X.dwe + i * SP + k0, bytes, &bar);
-            bulk_load(T.uhe[i], X.uhe + i * SP + k0, bytes, &bar);
-            bulk_load(T.vhe[i], X.vhe + i * SP + k0, bytes, &bar);
-            bulk_load(T.nx[i], X.nx + i * SP + k0, bytes, &bar);
-            bulk_load(T.ny[i], X.ny + i * SP + k0, bytes, &bar);
-            bulk_load(T.len[i], X.len + i * SP + k0, bytes, &bar);
-        }
-    }
+    // tile length in the padded planes (a multiple of 64 elements)
+    if (tid == 0) flux_tile_issue<TILE>(X, T, k0, min(TILE, X.S - k0), &bar);
     // the neighbour indices are not padded planes: ordinary loads, issued
     // while the bulk copies are in flight
-    const int k = k0 + tid;
     int pk[3] = {0, 0, 0};
     if (tid < cnt) {
 #pragma unroll
-        for (int i = 0; i < 3; i++) pk[i] = ro(M.nbr + i * N + k);
+        for (int i = 0; i < 3; i++) pk[i] = ro(M.nbr + i * N + k0 + tid);
     }
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
     float t = P.f_max_dt;
-    if (arrived && tid < cnt) {
-        const float eps = P.f_eps;
-        const float wk = T.wf[tid], lk = T.wlo[tid], hc = T.hf[tid];
-        const float rk = T.radius[tid];
-        const float inv_area = T.inv_area[tid];
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // flux sums
-        float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            const float n1 = T.nx[i][tid], n2 = T.ny[i][tid], L = T.len[i][tid];
-            const float dwl = T.dwe[i][tid], hl = T.he[i][tid];
-            const float uhl = T.uhe[i][tid], vhl = T.vhe[i][tid];
-            float hr, uhr, vhr, jump, rn = 3.0e38f;
-            if (pk[i] >= 0) {
-                // the neighbour's stored edge state: the very numbers it uses
-                // itself, so both sides see the same two states
-                const int n = pk[i] >> 2, m = pk[i] & 3;
-                const int ln = n - k0;
-                float wn, lnn, dwn;
-                if ((unsigned)ln < (unsigned)cnt) {
-                    hr = T.he[m][ln];
-                    dwn = T.dwe[m][ln];
-                    uhr = T.uhe[m][ln];
-                    vhr = T.vhe[m][ln];
-                    wn = T.wf[ln];
-                    lnn = T.wlo[ln];
-                    rn = T.radius[ln];
-                } else {
-                    hr = ro(X.he + m * SP + n);
-                    dwn = ro(X.dwe + m * SP + n);
-                    uhr = ro(X.uhe + m * SP + n);
-                    vhr = ro(X.vhe + m * SP + n);
-                    wn = ro(X.wf + n);
-                    lnn = ro(X.wlo + n);
-                    rn = ro(X.radius + n);
-                }
-                jump = ((wn - wk) + (lnn - lk)) + (dwn - dwl);
-            } else {
-                const int mb = -pk[i] - 1;
-                hr = ro(X.hbf + mb);
-                jump = ro(X.wjb + mb);
-                uhr = ro(X.uhbf + mb);
-                vhr = ro(X.vhbf + mb);
-            }
-            gx += dwl * L * n1;
-            gy += dwl * L * n2;
-            if (P.optimise_dry_cells && fabsf(hl) < eps && fabsf(hr) < eps) continue;
-            float f0, f1, f2, ms;
-            edge_flux_dev(hl, uhl, vhl, hr, uhr, vhr, jump, n1, n2, P, f0, f1, f2, ms);
-            a0 -= f0 * L;
-            a1 -= f1 * L;
-            a2 -= f2 * L;
-            // min(rk/ms, rn/ms) = min(rk, rn)/ms: one division per edge
-            if (ms > eps) t = ominf(t, __fdividef(fminf(rk, rn), ms));
-        }
-        const float ghc = P.f_g * hc;
-        X.ew[k] = a0 * inv_area;
-        X.euh[k] = (a1 - ghc * gx) * inv_area;
-        X.evh[k] = (a2 - ghc * gy) * inv_area;
-    }
+    if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T, k0, cnt, pk);
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
     block_min_timestep_f<TILE>(t, ctrl);
     if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
         publish_step_clock(ctrl, P);
+}
+
+// The same fluxes with persistent blocks: each block walks tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... and double-buffers them, the bulk
+// copies of the next tile in flight while the current one is computed.
+template <int TILE>
+__global__ void __launch_bounds__(TILE) flux_mixed_pipelined(DevMesh M, DevMixed X, DevParams P,
+                                                             Ctrl *ctrl_base, int flags,
+                                                             int ntiles) {
+    __shared__ FluxTile<TILE> T[2];
+    __shared__ __align__(8) unsigned long long bar[2];
+    const int N = M.N;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+    }
+    __syncthreads();
+    int tile = blockIdx.x, buf = 0;
+    unsigned parity = 0u;  // bit b: phase parity of bar[b]
+    if (tid == 0 && tile < ntiles)
+        flux_tile_issue<TILE>(X, T[0], tile * TILE, min(TILE, X.S - tile * TILE), &bar[0]);
+    while (tile < ntiles) {
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < ntiles) {
+            fence_proxy_async();  // the buffer's reads (previous tile) come first
+            flux_tile_issue<TILE>(X, T[buf ^ 1], next * TILE, min(TILE, X.S - next * TILE),
+                                  &bar[buf ^ 1]);
+        }
+        const int k0 = tile * TILE;
+        const int cnt = min(TILE, N - k0);
+        Ctrl *ctrl = M.blk_scen ? ctrl_base + M.blk_scen[k0 >> 8] : ctrl_base;
+        const bool skip = (flags & kFused) && ctrl_halted(ctrl);
+        int pk[3] = {0, 0, 0};
+        if (!skip && tid < cnt) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) pk[i] = ro(M.nbr + i * N + k0 + tid);
+        }
+        const bool arrived = mbar_wait_bounded(&bar[buf], ctrl, (parity >> buf) & 1u);
+        parity ^= 1u << buf;
+        if (!skip) {
+            float t = P.f_max_dt;
+            if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T[buf], k0, cnt, pk);
+            if (!(flags & kNoTimestep)) {
+                block_min_timestep_f<TILE>(t, ctrl);
+                if ((flags & kFused) && tid == 0 &&
+                    last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
+                    publish_step_clock(ctrl, P);
+            }
+        }
+        __syncthreads();  // everyone is done with T[buf] before it is refilled
+        tile = next;
+        buf ^= 1;
+    }
 }
 
 // FP32 copies of the updated state and protect (shallow_water_ext.c:
@@ -883,6 +961,16 @@ void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed
 void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, const DevParams &P,
                        Ctrl *ctrl, int flags, cudaStream_t st) {
     const int t = M.shape.flux, g = (M.n_launch + t - 1) / t;
+    if (M.shape.pipelined && t <= 128) {
+        // resident blocks per SM: 8 of 128 threads or 16 of 64 (two tiles of
+        // shared memory each)
+        const int grid = std::min(g, (t == 64 ? 16 : 8) * std::max(M.shape.sms, 1));
+        if (t == 64)
+            flux_mixed_pipelined<64><<<grid, 64, 0, st>>>(M, X, P, ctrl, flags, g);
+        else
+            flux_mixed_pipelined<128><<<grid, 128, 0, st>>>(M, X, P, ctrl, flags, g);
+        return;
+    }
     if (t == 64)
         flux_mixed<64><<<g, 64, 0, st>>>(M, X, P, ctrl, flags);
     else if (t == 256)

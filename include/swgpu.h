@@ -222,6 +222,8 @@ typedef struct {
     int32_t update_block;
     int32_t distribute_block;
     int32_t steps_per_graph;
+    int32_t flux_pipelined;   /* mixed flux: persistent blocks, double-buffered TMA
+                                 tiles (flux_block 64 or 128) */
 } swgpu_launch_config;
 
 int swgpu_get_launch_config(void *handle, swgpu_launch_config *config);

@@ -10,7 +10,8 @@ from helpers import bits_equal, gpu_from_scenario
 pytestmark = pytest.mark.gpu
 
 QS = ("stage", "xmomentum", "ymomentum")
-ODD = {"flux_block": 64, "update_block": 512, "distribute_block": 128, "steps_per_graph": 5}
+ODD = {"flux_block": 64, "update_block": 512, "distribute_block": 128, "steps_per_graph": 5,
+       "flux_pipelined": 1}
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -39,8 +40,8 @@ def test_ensemble_shape_independent(swgpu_built):
     scs = [scenarios.small_basin(9, 7, seed=1), scenarios.channel_inflow(12, 5, seed=2)]
     e1 = Ensemble(scs, DEFAULT, "mixed")
     e2 = Ensemble(scs, DEFAULT, "mixed")
-    set_config(e2._h, {"flux_block": 256, "update_block": 128, "distribute_block": 256,
-                       "steps_per_graph": 7})
+    set_config(e2._h, {"flux_block": 128, "update_block": 128, "distribute_block": 256,
+                       "steps_per_graph": 7, "flux_pipelined": 1})
     e1.evolve([0.5, 1.0])
     e2.evolve([0.5, 1.0])
     for a, b in zip(e1.centroid_values("stage"), e2.centroid_values("stage")):
@@ -57,6 +58,8 @@ def test_bad_shapes_refused(swgpu_built):
         set_config(d._h, dict(ODD, update_block=1024))
     with pytest.raises(SwgpuError):
         set_config(d._h, dict(ODD, steps_per_graph=0))
+    with pytest.raises(SwgpuError):
+        set_config(d._h, dict(ODD, flux_block=256, flux_pipelined=1))
     e = Ensemble([scenarios.small_basin(6, 5, seed=1), scenarios.small_basin(5, 4, seed=2)],
                  DEFAULT, "fp64")
     with pytest.raises(SwgpuError):
@@ -71,7 +74,7 @@ def test_tune_domain_and_cache(tmp_path, monkeypatch, swgpu_built):
     d = gpu_from_scenario(sc, DEFAULT, "mixed")
     rec = tune_domain(d, steps=4)
     assert set(rec["config"]) == {"flux_block", "update_block", "distribute_block",
-                                  "steps_per_graph"}
+                                  "steps_per_graph", "flux_pipelined"}
     assert all(t > 0 for t in rec["tuned_ms"])
     assert json.load(open(cache_path()))
     again = tune_domain(gpu_from_scenario(sc, DEFAULT, "mixed"), steps=4)

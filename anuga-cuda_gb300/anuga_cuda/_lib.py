@@ -127,6 +127,7 @@ _SIGNATURES = [
     ("swgpu_mlp_train", C.c_int, [_VP, C.c_int, C.c_int64, C.c_uint64, C.c_float, C.c_float,
                                   C.c_float, _f32p, _f32p]),
     ("swgpu_mlp_get_params", C.c_int, [_VP, _f32p]),
+    ("swgpu_mlp_set_tensor_path", C.c_int, [_VP, C.c_int]),
     ("swgpu_last_error", C.c_char_p, [_VP]),
     ("swgpu_device_info", C.c_int, [C.c_char_p, C.c_int]),
     ("swgpu_set_quantity", C.c_int, [_VP, C.c_int, _f64p, _f64p, _f64p]),

@@ -210,6 +210,266 @@ __global__ void __launch_bounds__(32 * kWarps) mlp_predict(FeatureTables F, cons
     }
 }
 
+// ---- inference on the 5th-generation tensor cores (tcgen05, TMEM) --------
+//
+// A CTA of 4 warps takes tiles of 128 rows.  Layer 1 (K = 16) and layer 2
+// (K = 128) are each one 128 x 128 tcgen05.mma chain issued by one thread:
+// A (activations) and B (weights, N x K) in shared memory in the canonical
+// K-major layout without swizzle (8-row x 16-byte core matrices, adjacent
+// along K 128 bytes apart, along M/N (K/8)*128 bytes apart), the FP32
+// accumulators in tensor memory (256 columns: layer 1 in 0..127, layer 2 in
+// 128..255).  Completion is signalled through tcgen05.commit on an
+// mbarrier; warp w then reads TMEM lanes 32w..32w+31 (its rows) with
+// tcgen05.ld, applies bias and ReLU, and writes the next layer's A tile, or
+// for layer 2 evaluates the 128 -> 2 output layer on the CUDA cores.
+
+constexpr int kTcRows = 128;
+
+struct __align__(1024) TcSmem {
+    __nv_bfloat16 a1[kTcRows * kF];   // layer-1 A: 128 x 16
+    __nv_bfloat16 b1[kH * kF];        // W1 as N x K: 128 x 16
+    __nv_bfloat16 a2[kTcRows * kH];   // layer-2 A: 128 x 128
+    __nv_bfloat16 b2[kH * kH];        // W2 as N x K: 128 x 128
+    float w3[kH * 2], bias1[kH], bias2[kH], bias3[2];
+    unsigned long long bar;
+    unsigned tmem_base;
+};
+
+// Byte offset of element (r, k) of an R x K K-major tile in the canonical
+// no-swizzle layout.
+__host__ __device__ __forceinline__ unsigned canon_offset(int r, int k, int K) {
+    return (unsigned)((r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ unsigned long long smem_desc(const void *p, unsigned lbo,
+                                                        unsigned sbo) {
+    const unsigned addr = (unsigned)__cvta_generic_to_shared(p);
+    return (unsigned long long)((addr >> 4) & 0x3FFFu) |
+           ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both
+// K-major, N = 128, M = 128.
+constexpr unsigned kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) |
+                              ((128u >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(unsigned d_tmem, unsigned long long a,
+                                       unsigned long long b, bool accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kTcIdesc), "r"((unsigned)accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(unsigned long long *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            (unsigned)__cvta_generic_to_shared(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void proxy_fence() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// 32 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+        "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void mbar_init_tc(unsigned long long *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(bar))
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"((unsigned)__cvta_generic_to_shared(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+constexpr int kTcWaitLimit = 1 << 22;
+// bounded wait for the MMA chain; false after kTcWaitLimit polls
+__device__ __forceinline__ bool tc_wait(unsigned long long *bar, unsigned parity) {
+    for (int i = 0; i < kTcWaitLimit; i++)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+
+__global__ void __launch_bounds__(128, 1) mlp_predict_tc(FeatureTables F, const float *params,
+                                                         long long row0, long long nrows,
+                                                         float *__restrict__ out,
+                                                         int *__restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned view of the dynamic shared memory
+    TcSmem &T = *reinterpret_cast<TcSmem *>(
+        smem_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // weights into the canonical layouts (BF16) and FP32 biases
+    for (int e = tid; e < kH * kF; e += 128) {
+        const int n = e / kF, k = e % kF;  // W1 [in k][out n]
+        *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(T.b1) +
+                                           canon_offset(n, k, kF)) =
+            __float2bfloat16(params[kOffW1 + k * kH + n]);
+    }
+    for (int e = tid; e < kH * kH; e += 128) {
+        const int n = e / kH, k = e % kH;  // W2 [in k][out n]
+        *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(T.b2) +
+                                           canon_offset(n, k, kH)) =
+            __float2bfloat16(params[kOffW2 + k * kH + n]);
+    }
+    for (int e = tid; e < kH * 2; e += 128)  // W3 rounded like the other weights
+        T.w3[e] = __bfloat162float(__float2bfloat16(params[kOffW3 + e]));
+    for (int e = tid; e < kH; e += 128) {
+        T.bias1[e] = params[kOffB1 + e];
+        T.bias2[e] = params[kOffB2 + e];
+    }
+    if (tid < 2) T.bias3[tid] = params[kOffB3 + tid];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+                         (unsigned)__cvta_generic_to_shared(&T.tmem_base))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) mbar_init_tc(&T.bar);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = T.tmem_base;
+    const unsigned d1 = tmem, d2 = tmem + 128u;              // column offsets
+    const unsigned lane_base = (unsigned)(32 * warp) << 16;  // this warp's TMEM lanes
+    unsigned parity = 0u;
+    bool ok = true;
+    for (long long base = (long long)blockIdx.x * kTcRows; base < nrows && ok;
+         base += (long long)gridDim.x * kTcRows) {
+        const long long r = base + tid;  // this thread's row
+        const bool valid = r < nrows;
+        // ---- layer-1 A: the row's 16 normalised features
+        {
+            float v[kF];
+            if (valid) {
+                const long long q = row0 + r;
+                const long long sidx = q / F.N, k = q - sidx * F.N;
+                const float *th = F.scen + sidx * kParams;
+                const float x = F.tri[3 * k], y = F.tri[3 * k + 1], z = F.tri[3 * k + 2];
+#pragma unroll
+                for (int c = 0; c < kF; c++)
+                    v[c] = (raw_feature(c, th, x, y, z) - F.mu[c]) * F.isd[c];
+            } else {
+#pragma unroll
+                for (int c = 0; c < kF; c++) v[c] = 0.f;
+            }
+#pragma unroll
+            for (int c = 0; c < kF; c += 2)
+                *reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(T.a1) +
+                                              canon_offset(tid, c, kF)) = pack2(v[c], v[c + 1]);
+        }
+        proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            // K = 16: one MMA
+            tc_mma(d1, smem_desc(T.a1, 128, (kF / 8) * 128), smem_desc(T.b1, 128, (kF / 8) * 128),
+                   false);
+            tc_commit(&T.bar);
+        }
+        // every thread votes, so that the whole block leaves together on a timeout
+        if (!__syncthreads_and(tc_wait(&T.bar, parity))) {
+            ok = false;
+            if (tid == 0) atomicExch(status, SWGPU_ETIMEOUT);
+            break;
+        }
+        parity ^= 1u;
+        tc_fence_after();
+        // ---- layer-1 epilogue: bias, ReLU, BF16 into layer-2 A
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++) {
+            float v[32];
+            tc_ld32(d1 + lane_base + 32u * ch, v);
+#pragma unroll
+            for (int c = 0; c < 32; c += 2) {
+                const int col = 32 * ch + c;
+                const float a = fmaxf(v[c] + T.bias1[col], 0.f);
+                const float b = fmaxf(v[c + 1] + T.bias1[col + 1], 0.f);
+                *reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(T.a2) +
+                                              canon_offset(tid, col, kH)) = pack2(a, b);
+            }
+        }
+        proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+#pragma unroll
+            for (int kk = 0; kk < kH / 16; kk++)  // K = 128 in 8 steps of 16
+                tc_mma(d2,
+                       smem_desc(reinterpret_cast<unsigned char *>(T.a2) + kk * 256, 128,
+                                 (kH / 8) * 128),
+                       smem_desc(reinterpret_cast<unsigned char *>(T.b2) + kk * 256, 128,
+                                 (kH / 8) * 128),
+                       kk > 0);
+            tc_commit(&T.bar);
+        }
+        if (!__syncthreads_and(tc_wait(&T.bar, parity))) {
+            ok = false;
+            if (tid == 0) atomicExch(status, SWGPU_ETIMEOUT);
+            break;
+        }
+        parity ^= 1u;
+        tc_fence_after();
+        // ---- layer-2 epilogue and the output layer on the CUDA cores
+        float y0 = T.bias3[0], y1 = T.bias3[1];
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++) {
+            float v[32];
+            tc_ld32(d2 + lane_base + 32u * ch, v);
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                const int col = 32 * ch + c;
+                // the activation is rounded to BF16 like the mma.sync path's
+                const float a = __bfloat162float(__float2bfloat16(fmaxf(v[c] + T.bias2[col], 0.f)));
+                y0 += a * T.w3[2 * col];
+                y1 += a * T.w3[2 * col + 1];
+            }
+        }
+        if (valid) {
+            out[2 * r] = y0;
+            out[2 * r + 1] = y1;
+        }
+        tc_fence_before();
+        __syncthreads();  // TMEM and the A tiles are reused by the next tile
+        tc_fence_after();
+    }
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem)
+                     : "memory");
+}
+
 // ---- training ------------------------------------------------------------
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
@@ -517,6 +777,8 @@ struct Mlp {
     long long *rows = nullptr;
     long long rows_cap = 0;
     float *loss = nullptr;
+    int *status = nullptr;   // device-side failure of the tensor-core kernel
+    int tensor_path = 0;     // 0: mma.sync, 1: tcgen05 (inference)
     long long adam_t = 0;
     std::vector<void *> allocs;
     std::string err;
@@ -615,6 +877,9 @@ int swgpu_mlp_create(const float *params, const float *feature_mean,
         e = cudaFuncSetAttribute(mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sizeof(BfWeights));
     if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mlp_predict_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(TcSmem) + 1024);
+    if (e == cudaSuccess)
         e = cudaFuncSetAttribute(mlp_forward_backward,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sizeof(BfWeights));
@@ -627,7 +892,7 @@ int swgpu_mlp_create(const float *params, const float *feature_mean,
         (rc = malloc_dev(m, &m->adam_m, kNumParams)) ||
         (rc = malloc_dev(m, &m->adam_v, kNumParams)) || (rc = malloc_dev(m, &m->w, 1)) ||
         (rc = malloc_dev(m, &m->mu, kF)) || (rc = malloc_dev(m, &m->isd, kF)) ||
-        (rc = malloc_dev(m, &m->loss, 1))) {
+        (rc = malloc_dev(m, &m->loss, 1)) || (rc = malloc_dev(m, &m->status, 1))) {
         for (void *p : m->allocs) cudaFree(p);
         delete m;
         return rc;
@@ -637,6 +902,7 @@ int swgpu_mlp_create(const float *params, const float *feature_mean,
     cudaMemcpy(m->isd, feature_inv_std, sizeof(float) * kF, cudaMemcpyHostToDevice);
     cudaMemset(m->adam_m, 0, sizeof(float) * kNumParams);
     cudaMemset(m->adam_v, 0, sizeof(float) * kNumParams);
+    cudaMemset(m->status, 0, sizeof(int));
     mlp_pack_weights<<<(kH * kS2 + 255) / 256, 256, 0, m->stream>>>(m->params, m->w);
     e = cudaStreamSynchronize(m->stream);
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -697,14 +963,27 @@ int swgpu_mlp_predict(void *handle, int64_t row0, int64_t nrows, float *out_devi
     cudaEvent_t a, b;
     MCK(cudaEventCreate(&a));
     MCK(cudaEventCreate(&b));
-    const long long tiles = (nrows + kRowsPerBlock - 1) / kRowsPerBlock;
-    const int grid = (int)std::min<long long>(tiles, 4LL * sm_count());
     MCK(cudaEventRecord(a, m->stream));
-    mlp_predict<<<grid, 32 * kWarps, sizeof(BfWeights), m->stream>>>(tables(m), m->w, row0,
-                                                                      nrows, out_device);
+    if (m->tensor_path == 1) {
+        // two CTAs per SM: each holds 256 TMEM columns of the SM's 512
+        const long long tiles = (nrows + kTcRows - 1) / kTcRows;
+        const int grid = (int)std::min<long long>(tiles, 2LL * sm_count());
+        mlp_predict_tc<<<grid, 128, sizeof(TcSmem) + 1024, m->stream>>>(
+            tables(m), m->params, row0, nrows, out_device, m->status);
+    } else {
+        const long long tiles = (nrows + kRowsPerBlock - 1) / kRowsPerBlock;
+        const int grid = (int)std::min<long long>(tiles, 4LL * sm_count());
+        mlp_predict<<<grid, 32 * kWarps, sizeof(BfWeights), m->stream>>>(tables(m), m->w, row0,
+                                                                          nrows, out_device);
+    }
     MCK(cudaGetLastError());
     MCK(cudaEventRecord(b, m->stream));
     MCK(cudaEventSynchronize(b));
+    if (m->tensor_path == 1) {
+        int st = 0;
+        MCK(cudaMemcpy(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (st) return mfail(m, st, "swgpu_mlp_predict: tensor-core wait timed out");
+    }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     cudaEventDestroy(a);
@@ -780,5 +1059,13 @@ int swgpu_mlp_get_params(void *handle, float *params) {
 }
 
 int swgpu_mlp_num_params(void) { return kNumParams; }
+
+int swgpu_mlp_set_tensor_path(void *handle, int path) {
+    Mlp *m = static_cast<Mlp *>(handle);
+    if (!m || (path != 0 && path != 1))
+        return mfail(m, SWGPU_EINVAL, "swgpu_mlp_set_tensor_path: 0 (mma.sync) or 1 (tcgen05)");
+    m->tensor_path = path;
+    return SWGPU_OK;
+}
 
 }  // extern "C"

@@ -269,6 +269,10 @@ int swgpu_mlp_gradients(void *mlp, const int64_t *rows, int64_t nrows, float w_d
 int swgpu_mlp_train(void *mlp, int steps, int64_t batch, uint64_t seed, float lr,
                     float w_depth, float w_arrival, float *last_loss, float *elapsed_ms);
 int swgpu_mlp_get_params(void *mlp, float *params);
+/* Inference kernel of swgpu_mlp_predict: 0 = mma.sync (default), 1 =
+ * tcgen05 (both hidden layers as 128 x 128 tcgen05.mma chains from shared
+ * memory into tensor memory). */
+int swgpu_mlp_set_tensor_path(void *mlp, int path);
 
 /* Frees everything the handle owns.  No counterpart in the reference (its
  * PyCUDA allocations are released by the garbage collector). */

@@ -42,6 +42,7 @@ def test_predict_equals_training_forward(small_family, swgpu_built):
     from anuga_cuda.surrogate import DEPTH_SCALE, Surrogate, sample_params, still_depth
     fm = small_family
     sg = Surrogate(fm, seed=4)
+    sg.set_tensor_path("mma.sync")   # the training forward's own kernel code
     th = sample_params(3, seed=8)
     targets = np.zeros((3, fm.N, 2), np.float32)
     sg.set_data(th, targets)
@@ -86,3 +87,26 @@ def test_solver_trained_surrogate(swgpu_built):
     rep = fallback_report(depth, hmt, ms_test / len(th_test), infer_ms)
     assert rep["mean_abs_error_m"] < baseline, (rep, baseline)
     assert 0.0 <= rep["blocks_over_tol_pct"] <= 100.0
+
+
+def test_tcgen05_inference_matches(small_family, swgpu_built):
+    """The tcgen05/TMEM inference kernel against the mma.sync one and the
+    NumPy FP64 restatement (BF16 rounding points alike; accumulation order
+    differs, so within the BF16 tolerance)."""
+    from anuga_cuda.surrogate import DEPTH_SCALE, Surrogate, sample_params, still_depth
+    from oracle import mlp_oracle as MO
+    fm = small_family
+    sg = Surrogate(fm, seed=11)
+    th = sample_params(5, seed=12)
+    sg.set_tensor_path("mma.sync")
+    d_sync, a_sync, _ = sg.predict(th)
+    sg.set_tensor_path("tcgen05")
+    d_tc, a_tc, _ = sg.predict(th)
+    assert np.isfinite(d_tc).all()
+    scale = np.max(np.abs(d_sync)) + 1e-6
+    assert np.max(np.abs(d_tc - d_sync)) <= TOL * scale
+    rows = np.arange(5 * fm.N)
+    yo, _, _ = MO.forward_backward(sg.params(), th, fm.tri, rows,
+                                   np.zeros((5, fm.N, 2), np.float32), sg.mu, sg.isd)
+    ref = np.maximum(still_depth(fm, th).ravel() + yo[:, 0] * DEPTH_SCALE, 0)
+    assert np.max(np.abs(d_tc.ravel() - ref)) <= TOL * scale

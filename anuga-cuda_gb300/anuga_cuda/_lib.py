@@ -94,7 +94,7 @@ class State_t(C.Structure):
 class LaunchConfig_t(C.Structure):
     _fields_ = [("flux_block", C.c_int32), ("update_block", C.c_int32),
                 ("distribute_block", C.c_int32), ("steps_per_graph", C.c_int32),
-                ("flux_pipelined", C.c_int32)]
+                ("flux_pipelined", C.c_int32), ("dependent_launch", C.c_int32)]
 
 
 class BoundaryTag_t(C.Structure):

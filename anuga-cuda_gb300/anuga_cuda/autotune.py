@@ -37,13 +37,14 @@ def get_config(h) -> dict:
     check(lib().swgpu_get_launch_config(h, C.byref(c)), h)
     return {"flux_block": c.flux_block, "update_block": c.update_block,
             "distribute_block": c.distribute_block, "steps_per_graph": c.steps_per_graph,
-            "flux_pipelined": c.flux_pipelined}
+            "flux_pipelined": c.flux_pipelined, "dependent_launch": c.dependent_launch}
 
 
 def set_config(h, cfg: dict) -> None:
     c = _lib.LaunchConfig_t(int(cfg["flux_block"]), int(cfg["update_block"]),
                             int(cfg["distribute_block"]), int(cfg.get("steps_per_graph", 16)),
-                            int(cfg.get("flux_pipelined", 0)))
+                            int(cfg.get("flux_pipelined", 0)),
+                            int(cfg.get("dependent_launch", get_config(h)["dependent_launch"])))
     check(lib().swgpu_set_launch_config(h, C.byref(c)), h)
 
 

@@ -539,6 +539,8 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         TRY(dalloc(h, &X.dze, s3));
         TRY(dalloc(h, &X.fric, s1));
         TRY(dalloc(h, &X.zmoff, s1));
+        TRY(dalloc(h, &X.zhi, s1));
+        TRY(dalloc(h, &X.zlo, s1));
         TRY(dalloc(h, &X.kind, s1));
         // FP64 vertex planes are kept for downloads (stage = depth + bed)
         TRY(dalloc(h, &S.wv, n3));
@@ -646,7 +648,7 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
         M.shape = LaunchShape{precision == SWGPU_MIXED ? 128 : kBlock, kBlock, kBlock, 0,
-                              std::max(sms, 1)};
+                              std::max(sms, 1), 1};
     }
     for (int i = 0; i < h->nscen; i++) {
         Ctrl *c = &h->h_ctrl[i];
@@ -1088,6 +1090,7 @@ int swgpu_get_launch_config(void *handle, swgpu_launch_config *cfg) {
     cfg->distribute_block = h->M.shape.distribute;
     cfg->steps_per_graph = h->steps_per_graph;
     cfg->flux_pipelined = h->M.shape.pipelined;
+    cfg->dependent_launch = h->M.shape.pdl;
     return SWGPU_OK;
 }
 
@@ -1120,6 +1123,7 @@ int swgpu_set_launch_config(void *handle, const swgpu_launch_config *cfg) {
     h->M.shape.update = cfg->update_block;
     h->M.shape.distribute = cfg->distribute_block;
     h->M.shape.pipelined = cfg->flux_pipelined ? 1 : 0;
+    h->M.shape.pdl = cfg->dependent_launch ? 1 : 0;
     h->steps_per_graph = cfg->steps_per_graph;
     set_block_counts(h);
     return push_ctrl(h);

@@ -30,6 +30,7 @@ struct LaunchShape {
     int flux, update, distribute;
     int pipelined;  // mixed flux: persistent double-buffered blocks (tiles of 64 or 128)
     int sms;        // multiprocessors of the device (persistent grid size)
+    int pdl;        // mixed kernels launched as programmatic dependents of the previous one
 };
 
 struct DevMesh {
@@ -102,6 +103,7 @@ struct DevMixed {
     float *dze;                    // [3][N] bed edge minus bed centroid
     float *fric;                   // [N] Manning n
     float *zmoff;                  // [N] mean(bed vertex) minus bed centroid
+    float *zhi, *zlo;              // [N] bed centroid as an FP32 pair hi + lo
     uint8_t *kind;                 // [N] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat
 };
 

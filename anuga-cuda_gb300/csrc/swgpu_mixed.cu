@@ -85,6 +85,51 @@ __device__ __forceinline__ float narrow(double x) {
     return __uint_as_float(r);
 }
 
+// x as an FP32 pair on the integer pipe: hi = x rounded to nearest (as
+// narrow), lo = the exact remainder x - hi rounded to nearest.  lo is zero
+// where x lies outside FP32's normal range or the remainder falls below it.
+__device__ __forceinline__ void split_double(double x, float &hi, float &lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const unsigned ed = (unsigned)((b >> 52) & 0x7ffu);
+    const int e = (int)ed - 896;
+    if (ed == 0x7ffu || e <= 0 || e >= 255) {
+        hi = narrow(x);
+        lo = 0.0f;
+        return;
+    }
+    const unsigned long long frac = b & 0xfffffffffffffull;
+    const unsigned m = (unsigned)(frac >> 29);
+    int rest = (int)(frac & 0x1fffffffull);  // the 29 dropped bits
+    unsigned r = ((unsigned)e << 23) | m;
+    if (rest > 0x10000000 || (rest == 0x10000000 && (m & 1u))) {
+        r += 1u;  // rounded up: the remainder is negative
+        rest -= 0x20000000;
+    }
+    hi = __uint_as_float(r | sign);
+    // remainder = rest * 2^(ed - 1075): one rounding (int -> float), then an
+    // exact scaling by a power of two (flushed to zero below FP32's range)
+    const int se = (int)ed - 1075 + 127;
+    const float scale = se > 0 ? __uint_as_float((unsigned)se << 23) : 0.0f;
+    lo = __uint_as_float(__float_as_uint(__fmul_rn(__int2float_rn(rest), scale)) ^ sign);
+}
+
+// (ah + al) + (bh + bl) as an FP32 pair hi + lo (TwoSum of the high parts,
+// the low parts added to its error, TwoSum again): about 46 bits.
+__device__ __forceinline__ void add_pairs(float ah, float al, float bh, float bl, float &hi,
+                                          float &lo) {
+    const float s = __fadd_rn(ah, bh);
+    const float bs = __fsub_rn(s, ah);
+    const float es = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bs)), __fsub_rn(bh, bs));
+    const float t = __fadd_rn(es, __fadd_rn(al, bl));
+    hi = __fadd_rn(s, t);
+    const float bt = __fsub_rn(hi, s);
+    lo = __fadd_rn(__fsub_rn(s, __fsub_rn(hi, bt)), __fsub_rn(t, bt));
+}
+
+// h <= 0 for an h that is not NaN, on the integer pipe (-0 included).
+__device__ __forceinline__ bool not_positive(double h) { return __double_as_longlong(h) <= 0; }
+
 // Edge depth of edge i of a triangle from its centroid depth, the stage
 // jumps of the two vertices of the edge and the bed offset of the edge.
 // Both triangles of an edge evaluate it with the same operations.
@@ -213,6 +258,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, Ctrl 
         if (mbar_try_wait(bar, parity)) break;
     return false;
 }
+// Programmatic dependent launch: let the next kernel of the stream start
+// its blocks as this one's finish, and wait (in the next kernel) until the
+// previous kernel has completed and its writes are visible.  Both are no-ops
+// for kernels launched without the programmatic attribute.
+__device__ __forceinline__ void pdl_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Orders this thread's earlier generic-proxy accesses to shared memory
 // before later async-proxy (bulk copy) writes to it.
 __device__ __forceinline__ void fence_proxy_async() {
@@ -228,29 +282,49 @@ struct __align__(128) FluxTile {
     float nx[3][TILE], ny[3][TILE], len[3][TILE];
 };
 
-// The 26 bulk copies of a flux tile starting at triangle k0 (span elements
-// of each padded plane), completing on bar.  Called by one thread.
+// The bulk copies of a flux tile starting at triangle k0 (span elements of
+// each padded plane), completing on bar, in two halves: the static geometry
+// (issued before the previous kernel has finished) and the state.
 template <int TILE>
-__device__ __forceinline__ void flux_tile_issue(const DevMixed &X, FluxTile<TILE> &T, int k0,
-                                                int span, unsigned long long *bar) {
+__device__ __forceinline__ void flux_tile_issue_static(const DevMixed &X, FluxTile<TILE> &T,
+                                                       int k0, int span,
+                                                       unsigned long long *bar) {
     const int SP = X.S;
     const unsigned bytes = (unsigned)span * 4u;
-    mbar_arrive_expect_tx(bar, 26u * bytes);
+    mbar_arrive_expect_tx(bar, 26u * bytes);  // the whole tile: 11 static + 15 dynamic planes
+    bulk_load(T.radius, X.radius + k0, bytes, bar);
+    bulk_load(T.inv_area, X.inv_area + k0, bytes, bar);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        bulk_load(T.nx[i], X.nx + i * SP + k0, bytes, bar);
+        bulk_load(T.ny[i], X.ny + i * SP + k0, bytes, bar);
+        bulk_load(T.len[i], X.len + i * SP + k0, bytes, bar);
+    }
+}
+template <int TILE>
+__device__ __forceinline__ void flux_tile_issue_dynamic(const DevMixed &X, FluxTile<TILE> &T,
+                                                        int k0, int span,
+                                                        unsigned long long *bar) {
+    const int SP = X.S;
+    const unsigned bytes = (unsigned)span * 4u;
     bulk_load(T.wf, X.wf + k0, bytes, bar);
     bulk_load(T.wlo, X.wlo + k0, bytes, bar);
     bulk_load(T.hf, X.hf + k0, bytes, bar);
-    bulk_load(T.radius, X.radius + k0, bytes, bar);
-    bulk_load(T.inv_area, X.inv_area + k0, bytes, bar);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         bulk_load(T.he[i], X.he + i * SP + k0, bytes, bar);
         bulk_load(T.dwe[i], X.dwe + i * SP + k0, bytes, bar);
         bulk_load(T.uhe[i], X.uhe + i * SP + k0, bytes, bar);
         bulk_load(T.vhe[i], X.vhe + i * SP + k0, bytes, bar);
-        bulk_load(T.nx[i], X.nx + i * SP + k0, bytes, bar);
-        bulk_load(T.ny[i], X.ny + i * SP + k0, bytes, bar);
-        bulk_load(T.len[i], X.len + i * SP + k0, bytes, bar);
     }
+}
+// The 26 bulk copies of a flux tile starting at triangle k0 (span elements
+// of each padded plane), completing on bar.  Called by one thread.
+template <int TILE>
+__device__ __forceinline__ void flux_tile_issue(const DevMixed &X, FluxTile<TILE> &T, int k0,
+                                                int span, unsigned long long *bar) {
+    flux_tile_issue_static<TILE>(X, T, k0, span, bar);
+    flux_tile_issue_dynamic<TILE>(X, T, k0, span, bar);
 }
 
 // Fluxes + gravity_wb of triangle k0 + tid of a staged tile (cnt valid
@@ -330,28 +404,31 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
 // shared memory; neighbours inside the tile (most of them, in Morton order)
 // are read from shared memory, the others from global memory.
 template <int TILE>
-__global__ void __launch_bounds__(TILE) flux_mixed(DevMesh M, DevMixed X, DevParams P,
+__global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMixed X, DevParams P,
                                                         Ctrl *ctrl, int flags) {
+    pdl_launch_dependents();
     ctrl = block_ctrl(ctrl, M);
-    if ((flags & kFused) && ctrl_halted(ctrl)) return;
     __shared__ FluxTile<TILE> T;
     __shared__ __align__(8) unsigned long long bar;
     const int N = M.N;
     const int tid = threadIdx.x;
     const int k0 = blockIdx.x * TILE;
     const int cnt = min(TILE, N - k0);
+    const int span = min(TILE, X.S - k0);  // tile length in the padded planes (x64)
     if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
-    // tile length in the padded planes (a multiple of 64 elements)
-    if (tid == 0) flux_tile_issue<TILE>(X, T, k0, min(TILE, X.S - k0), &bar);
-    // the neighbour indices are not padded planes: ordinary loads, issued
-    // while the bulk copies are in flight
+    // geometry and neighbour indices do not change between steps: fetched
+    // while the previous kernel may still run
+    if (tid == 0) flux_tile_issue_static<TILE>(X, T, k0, span, &bar);
     int pk[3] = {0, 0, 0};
     if (tid < cnt) {
 #pragma unroll
         for (int i = 0; i < 3; i++) pk[i] = ro(M.nbr + i * N + k0 + tid);
     }
+    pdl_wait();
+    if (tid == 0) flux_tile_issue_dynamic<TILE>(X, T, k0, span, &bar);
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
+    if ((flags & kFused) && ctrl_halted(ctrl)) return;  // the copies have landed
     float t = P.f_max_dt;
     if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T, k0, cnt, pk);
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
@@ -379,9 +456,15 @@ __global__ void __launch_bounds__(TILE) flux_mixed_pipelined(DevMesh M, DevMixed
     int tile = blockIdx.x, buf = 0;
     unsigned parity = 0u;  // bit b: phase parity of bar[b]
     if (tid == 0 && tile < ntiles)
-        flux_tile_issue<TILE>(X, T[0], tile * TILE, min(TILE, X.S - tile * TILE), &bar[0]);
+        flux_tile_issue_static<TILE>(X, T[0], tile * TILE, min(TILE, X.S - tile * TILE), &bar[0]);
+    pdl_wait();
+    if (tid == 0 && tile < ntiles)
+        flux_tile_issue_dynamic<TILE>(X, T[0], tile * TILE, min(TILE, X.S - tile * TILE), &bar[0]);
+    if (tile + (int)gridDim.x >= ntiles) pdl_launch_dependents();
     while (tile < ntiles) {
         const int next = tile + gridDim.x;
+        // the next kernel's blocks may start once every block is on its last tile
+        if (next < ntiles && next + (int)gridDim.x >= ntiles) pdl_launch_dependents();
         if (tid == 0 && next < ntiles) {
             fence_proxy_async();  // the buffer's reads (previous tile) come first
             flux_tile_issue<TILE>(X, T[buf ^ 1], next * TILE, min(TILE, X.S - next * TILE),
@@ -416,22 +499,26 @@ __global__ void __launch_bounds__(TILE) flux_mixed_pipelined(DevMesh M, DevMixed
 
 // FP32 copies of the updated state and protect (shallow_water_ext.c:
 // 1638-1705) on depth; shared by the update and the stand-alone prepare.
+// No FP64 arithmetic: the stage pair comes from depth and bed as FP32 pairs
+// (zhi + zlo: the bed centroid).
 __device__ __forceinline__ void finish_state(const DevParams &P, double &h, double &uh, double &vh,
-                                             double zc, float &hf, float &wf, float &wlo,
-                                             float &uvel, float &vvel, int &nonfinite) {
-    hf = narrow(h);
+                                             float zhi, float zlo, float &hf, float &wf,
+                                             float &wlo, float &uvel, float &vvel,
+                                             int &nonfinite) {
+    float hl;
+    split_double(h, hf, hl);
     float uhf = narrow(uh), vhf = narrow(vh);
-    if (hf < P.f_mah) {
+    if (hf < P.f_mah) {  // false for NaN: h is a number below
         if (P.f_mas < P.f_eps) {
             uh = vh = 0.0;
             uhf = vhf = 0.0f;
-            if (h <= 0.0) {
+            if (not_positive(h)) {
                 h = 0.0;
-                hf = 0.0f;
+                hf = hl = 0.0f;
             }
-        } else if (h <= 0.0) {
+        } else if (not_positive(h)) {
             h = uh = vh = 0.0;
-            hf = uhf = vhf = 0.0f;
+            hf = hl = uhf = vhf = 0.0f;
         } else {
             const float u = uhf / hf, v = vhf / hf, ms = P.f_mas;
             if (fabsf(u) > ms) uhf = (u > 0 ? ms : -ms) * hf;
@@ -442,9 +529,7 @@ __device__ __forceinline__ void finish_state(const DevParams &P, double &h, doub
     }
     // stage as an unevaluated FP32 sum hi + lo (~46 bits): the limiter and
     // the flux take stage differences between neighbours from it
-    const double w = h + zc;
-    wf = narrow(w);
-    wlo = narrow(w - widen(wf));
+    add_pairs(hf, hl, zhi, zlo, wf, wlo);
     if (!(fabsf(hf) <= 3.0e38f) || !(fabsf(uhf) <= 3.0e38f) || !(fabsf(vhf) <= 3.0e38f))
         nonfinite = 1;
     const float inv = __fdividef(1.0f, omaxf(hf, P.f_mah));
@@ -458,13 +543,20 @@ template <int BS>
 __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevState S, DevMixed X,
                                                        DevParams P, Ctrl *ctrl, int flags,
                                                        Stage stg) {
+    pdl_launch_dependents();
     ctrl = block_ctrl(ctrl, M);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = k < M.N;
+    // static per-triangle data before the previous kernel has finished
+    const float eta = in ? ro(X.fric + k) : 0.0f;
+    const float zmoff = in ? ro(X.zmoff + k) : 0.0f;
+    const float zhi = in ? ro(X.zhi + k) : 0.0f, zlo = in ? ro(X.zlo + k) : 0.0f;
+    pdl_wait();
     if ((flags & kFused) && ctrl_halted(ctrl)) return;
     const StepClock clk = published_step_clock(ctrl);
     const float dtf = (float)clk.dt;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int bad = 0, nonfinite = 0;
-    if (k < M.N) {
+    if (in) {
         // every load first (this thread is the only writer of element k)
         const double h0 = ro(X.hd + k), uh0 = ro(S.uh + k), vh0 = ro(S.vh + k);
         double h = h0, uh = uh0, vh = vh0;
@@ -480,10 +572,7 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
         const float uf = ro(X.uvel + k) * omaxf(hf0, mah);
         const float vf = ro(X.vvel + k) * omaxf(hf0, mah);
         const float ew = ro(X.ew + k), euh = ro(X.euh + k), evh = ro(X.evh + k);
-        const float zmoff = ro(X.zmoff + k);
-        const double zc = ro(S.zc + k);
         float rm1 = 0.0f, r = 1.0f;  // r - 1 and r
-        const float eta = ro(X.fric + k);
         if (eta > mah) {
             const float hm = hf0 - zmoff;
             if (hm >= mah) {
@@ -507,7 +596,7 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
             vh = stg.a * vh + stg.b * bv;
         }
         float hf, wf, wl, uv, vv;
-        finish_state(P, h, uh, vh, zc, hf, wf, wl, uv, vv, nonfinite);
+        finish_state(P, h, uh, vh, zhi, zlo, hf, wf, wl, uv, vv, nonfinite);
         if (stg.kind == kStageFirst) {  // backup_conserved_quantities (depth, momenta)
             S.bw[k] = h0;
             S.buh[k] = uh0;
@@ -619,27 +708,23 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
                                                            DevParams P, const BcTag *tags,
                                                            Ctrl *ctrl, int flags) {
     const bool fused = flags & kFused;
+    pdl_launch_dependents();
     ctrl = block_ctrl(ctrl, M);
-    if (fused && ctrl_halted(ctrl)) return;
     __shared__ DistTile<BS> T;
     __shared__ __align__(8) unsigned long long bar;
     const int N = M.N, SP = X.S;
-    const int order = (int)ctrl->order;
     const int tid = threadIdx.x;
     const int kb = blockIdx.x * BS;
     const int cnt = min(BS, N - kb);
     const int span = min(BS, SP - kb);  // a multiple of 64 elements
     const int k = kb + tid;
+    const unsigned bytes = (unsigned)span * 4u;
     if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
+    // static planes (reconstruction coefficients, bed offsets) and index
+    // planes before the previous kernel has finished
     if (tid == 0) {
-        const unsigned bytes = (unsigned)span * 4u;
         mbar_arrive_expect_tx(&bar, 17u * bytes);
-        bulk_load(T.wf, X.wf + kb, bytes, &bar);
-        bulk_load(T.wlo, X.wlo + kb, bytes, &bar);
-        bulk_load(T.hf, X.hf + kb, bytes, &bar);
-        bulk_load(T.uvel, X.uvel + kb, bytes, &bar);
-        bulk_load(T.vvel, X.vvel + kb, bytes, &bar);
 #pragma unroll
         for (int j = 0; j < 6; j++) bulk_load(T.gc[j], X.gc + j * SP + kb, bytes, &bar);
 #pragma unroll
@@ -648,14 +733,23 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
             bulk_load(T.dze[i], X.dze + i * SP + kb, bytes, &bar);
         }
     }
-    // index planes are not padded: ordinary loads while the copies fly
     int sur[3] = {0, 0, 0}, kind = 2;
     if (tid < cnt) {
         kind = ro(X.kind + k);
 #pragma unroll
         for (int i = 0; i < 3; i++) sur[i] = ro(M.surr + i * N + k);
     }
+    pdl_wait();
+    if (tid == 0) {
+        bulk_load(T.wf, X.wf + kb, bytes, &bar);
+        bulk_load(T.wlo, X.wlo + kb, bytes, &bar);
+        bulk_load(T.hf, X.hf + kb, bytes, &bar);
+        bulk_load(T.uvel, X.uvel + kb, bytes, &bar);
+        bulk_load(T.vvel, X.vvel + kb, bytes, &bar);
+    }
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
+    if (fused && ctrl_halted(ctrl)) return;  // the copies have landed
+    const int order = (int)ctrl->order;
     int bad_bc = 0;
     if (arrived && tid < cnt) {
         const float mah = P.f_mah;
@@ -718,7 +812,8 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
                     }
                 } else {
                     const int slot = (kind >> 2) & 3;
-                    const int k1 = sur[slot];
+                    // selected without indexing, which would put sur in local memory
+                    const int k1 = slot == 0 ? sur[0] : (slot == 1 ? sur[1] : sur[2]);
                     const float h1 = tile_or_global(T.hf, X.hf, k1, kb, cnt);
                     const float beta = P.f_beta_w;
                     one_jumps_f((tile_or_global(T.wf, X.wf, k1, kb, cnt) - wk) +
@@ -882,7 +977,7 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
     double uh = S.uh[k], vh = S.vh[k];
     float hf, wf, wl, uv, vv;
     int nonfinite = 0;
-    finish_state(P, h, uh, vh, S.zc[k], hf, wf, wl, uv, vv, nonfinite);
+    finish_state(P, h, uh, vh, X.zhi[k], X.zlo[k], hf, wf, wl, uv, vv, nonfinite);
     X.hd[k] = h;
     S.uh[k] = uh;
     S.vh[k] = vh;
@@ -947,47 +1042,69 @@ __global__ void mass_final_mixed(const double *partials, int n, double *out) {
 
 // Block sizes come from M.shape (the autotuner's choice; results do not
 // depend on it).
+// A launch of kernel k; with pdl, as a programmatic dependent of the stream's
+// previous kernel (it may start during that kernel's last wave and waits for
+// it with griddepcontrol.wait before reading what that kernel writes).
+template <typename... KArgs, typename... Args>
+static void launch_k(void (*k)(KArgs...), int grid, int block, cudaStream_t st, bool pdl,
+                     Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                              const DevParams &P, const BcTag *tags, Ctrl *ctrl, int flags,
                              cudaStream_t st) {
     const int bs = M.shape.distribute, g = (M.n_launch + bs - 1) / bs;
+    const bool pdl = M.shape.pdl;
     if (bs == 128)
-        distribute_mixed<128><<<g, 128, 0, st>>>(M, S, X, P, tags, ctrl, flags);
+        launch_k(distribute_mixed<128>, g, 128, st, pdl, M, S, X, P, tags, ctrl, flags);
     else if (bs == 512)
-        distribute_mixed<512><<<g, 512, 0, st>>>(M, S, X, P, tags, ctrl, flags);
+        launch_k(distribute_mixed<512>, g, 512, st, pdl, M, S, X, P, tags, ctrl, flags);
     else
-        distribute_mixed<256><<<g, 256, 0, st>>>(M, S, X, P, tags, ctrl, flags);
+        launch_k(distribute_mixed<256>, g, 256, st, pdl, M, S, X, P, tags, ctrl, flags);
 }
 void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, const DevParams &P,
                        Ctrl *ctrl, int flags, cudaStream_t st) {
     const int t = M.shape.flux, g = (M.n_launch + t - 1) / t;
+    const bool pdl = M.shape.pdl;
     if (M.shape.pipelined && t <= 128) {
         // resident blocks per SM: 8 of 128 threads or 16 of 64 (two tiles of
         // shared memory each)
         const int grid = std::min(g, (t == 64 ? 16 : 8) * std::max(M.shape.sms, 1));
         if (t == 64)
-            flux_mixed_pipelined<64><<<grid, 64, 0, st>>>(M, X, P, ctrl, flags, g);
+            launch_k(flux_mixed_pipelined<64>, grid, 64, st, pdl, M, X, P, ctrl, flags, g);
         else
-            flux_mixed_pipelined<128><<<grid, 128, 0, st>>>(M, X, P, ctrl, flags, g);
+            launch_k(flux_mixed_pipelined<128>, grid, 128, st, pdl, M, X, P, ctrl, flags, g);
         return;
     }
     if (t == 64)
-        flux_mixed<64><<<g, 64, 0, st>>>(M, X, P, ctrl, flags);
+        launch_k(flux_mixed<64>, g, 64, st, pdl, M, X, P, ctrl, flags);
     else if (t == 256)
-        flux_mixed<256><<<g, 256, 0, st>>>(M, X, P, ctrl, flags);
+        launch_k(flux_mixed<256>, g, 256, st, pdl, M, X, P, ctrl, flags);
     else
-        flux_mixed<128><<<g, 128, 0, st>>>(M, X, P, ctrl, flags);
+        launch_k(flux_mixed<128>, g, 128, st, pdl, M, X, P, ctrl, flags);
 }
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,
                          cudaStream_t st) {
     const int bs = M.shape.update, g = (M.n_launch + bs - 1) / bs;
+    const bool pdl = M.shape.pdl;
     if (bs == 128)
-        update_mixed<128><<<g, 128, 0, st>>>(M, S, X, P, ctrl, flags, stage);
+        launch_k(update_mixed<128>, g, 128, st, pdl, M, S, X, P, ctrl, flags, stage);
     else if (bs == 512)
-        update_mixed<512><<<g, 512, 0, st>>>(M, S, X, P, ctrl, flags, stage);
+        launch_k(update_mixed<512>, g, 512, st, pdl, M, S, X, P, ctrl, flags, stage);
     else
-        update_mixed<256><<<g, 256, 0, st>>>(M, S, X, P, ctrl, flags, stage);
+        launch_k(update_mixed<256>, g, 256, st, pdl, M, S, X, P, ctrl, flags, stage);
 }
 void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                           const DevParams &P, int from_stage, cudaStream_t st) {
@@ -1024,7 +1141,7 @@ int build_mixed_geometry(Handle *h) {
         return SWGPU_ECUDA;
     // FP32 planes use the padded stride sp (see DevMixed::S)
     std::vector<float> nx(3 * sp), ny(3 * sp), len(3 * sp), inv_area(n1), radius(n1), gc(6 * sp),
-        dzv(3 * sp), dze(3 * sp), fric(n1), zmoff(n1);
+        dzv(3 * sp), dze(3 * sp), fric(n1), zmoff(n1), zhi(n1), zlo(n1);
     std::vector<uint8_t> kind(n1);
     const std::vector<double> &V = h->h_vxy, &C = h->h_cxy;
     for (int k = 0; k < N; k++) {
@@ -1039,6 +1156,8 @@ int build_mixed_geometry(Handle *h) {
         radius[k] = (float)h->h_radii[k];
         fric[k] = (float)fr[k];
         zmoff[k] = (float)((zv[k] + zv[n1 + k] + zv[2 * n1 + k]) / 3.0 - zc[k]);
+        zhi[k] = (float)zc[k];
+        zlo[k] = (float)(zc[k] - (double)zhi[k]);
         const double x = C[k], y = C[n1 + k];
         double dxv[3], dyv[3];
         for (int i = 0; i < 3; i++) {
@@ -1091,6 +1210,8 @@ int build_mixed_geometry(Handle *h) {
     put(X.dze, dze.data(), 3 * sp * 4);
     put(X.fric, fric.data(), n1 * 4);
     put(X.zmoff, zmoff.data(), n1 * 4);
+    put(X.zhi, zhi.data(), n1 * 4);
+    put(X.zlo, zlo.data(), n1 * 4);
     put(X.kind, kind.data(), n1);
     return e == cudaSuccess ? SWGPU_OK : SWGPU_ECUDA;
 }

@@ -224,6 +224,10 @@ typedef struct {
     int32_t steps_per_graph;
     int32_t flux_pipelined;   /* mixed flux: persistent blocks, double-buffered TMA
                                  tiles (flux_block 64 or 128) */
+    int32_t dependent_launch; /* mixed kernels: each step kernel is launched as a
+                                 programmatic dependent of the previous one, so
+                                 its blocks start (and fetch the static planes)
+                                 during that kernel's last wave */
 } swgpu_launch_config;
 
 int swgpu_get_launch_config(void *handle, swgpu_launch_config *config);

@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 QS = ("stage", "xmomentum", "ymomentum")
 ODD = {"flux_block": 64, "update_block": 512, "distribute_block": 128, "steps_per_graph": 5,
-       "flux_pipelined": 1}
+       "flux_pipelined": 1, "dependent_launch": 0}
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -74,7 +74,7 @@ def test_tune_domain_and_cache(tmp_path, monkeypatch, swgpu_built):
     d = gpu_from_scenario(sc, DEFAULT, "mixed")
     rec = tune_domain(d, steps=4)
     assert set(rec["config"]) == {"flux_block", "update_block", "distribute_block",
-                                  "steps_per_graph", "flux_pipelined"}
+                                  "steps_per_graph", "flux_pipelined", "dependent_launch"}
     assert all(t > 0 for t in rec["tuned_ms"])
     assert json.load(open(cache_path()))
     again = tune_domain(gpu_from_scenario(sc, DEFAULT, "mixed"), steps=4)

@@ -427,8 +427,10 @@ __global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMi
     }
     pdl_wait();
     if (tid == 0) flux_tile_issue_dynamic<TILE>(X, T, k0, span, &bar);
+    // read while the copies fly; acted on once they have landed
+    const bool halted = (flags & kFused) && ctrl_halted(ctrl);
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
-    if ((flags & kFused) && ctrl_halted(ctrl)) return;  // the copies have landed
+    if (halted) return;
     float t = P.f_max_dt;
     if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T, k0, cnt, pk);
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
@@ -552,26 +554,30 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
     const float zmoff = in ? ro(X.zmoff + k) : 0.0f;
     const float zhi = in ? ro(X.zhi + k) : 0.0f, zlo = in ? ro(X.zlo + k) : 0.0f;
     pdl_wait();
-    if ((flags & kFused) && ctrl_halted(ctrl)) return;
+    // every load first, the control block's with them (this thread is the
+    // only writer of element k)
+    const bool halted = (flags & kFused) && ctrl_halted(ctrl);
     const StepClock clk = published_step_clock(ctrl);
+    const int kk = in ? k : 0;
+    const double h0 = ro(X.hd + kk), uh0 = ro(S.uh + kk), vh0 = ro(S.vh + kk);
+    const bool combine = stg.kind == kStageMid || stg.kind == kStageLast;
+    double bh = 0.0, bu = 0.0, bv = 0.0;
+    if (combine) {
+        bh = ro(S.bw + kk);
+        bu = ro(S.buh + kk);
+        bv = ro(S.bvh + kk);
+    }
+    const float hf0 = ro(X.hf + kk);  // FP32 copies of the pre-update state
+    const float uv0 = ro(X.uvel + kk), vv0 = ro(X.vvel + kk);
+    const float ew = ro(X.ew + kk), euh = ro(X.euh + kk), evh = ro(X.evh + kk);
+    if (halted) return;
     const float dtf = (float)clk.dt;
     int bad = 0, nonfinite = 0;
     if (in) {
-        // every load first (this thread is the only writer of element k)
-        const double h0 = ro(X.hd + k), uh0 = ro(S.uh + k), vh0 = ro(S.vh + k);
         double h = h0, uh = uh0, vh = vh0;
-        const bool combine = stg.kind == kStageMid || stg.kind == kStageLast;
-        double bh = 0.0, bu = 0.0, bv = 0.0;
-        if (combine) {
-            bh = ro(S.bw + k);
-            bu = ro(S.buh + k);
-            bv = ro(S.bvh + k);
-        }
         const float mah = P.f_mah;
-        const float hf0 = ro(X.hf + k);  // FP32 copies of the pre-update state
-        const float uf = ro(X.uvel + k) * omaxf(hf0, mah);
-        const float vf = ro(X.vvel + k) * omaxf(hf0, mah);
-        const float ew = ro(X.ew + k), euh = ro(X.euh + k), evh = ro(X.evh + k);
+        const float uf = uv0 * omaxf(hf0, mah);
+        const float vf = vv0 * omaxf(hf0, mah);
         float rm1 = 0.0f, r = 1.0f;  // r - 1 and r
         if (eta > mah) {
             const float hm = hf0 - zmoff;
@@ -747,9 +753,11 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
         bulk_load(T.uvel, X.uvel + kb, bytes, &bar);
         bulk_load(T.vvel, X.vvel + kb, bytes, &bar);
     }
-    const bool arrived = mbar_wait_bounded(&bar, ctrl);
-    if (fused && ctrl_halted(ctrl)) return;  // the copies have landed
+    // read while the copies fly; acted on once they have landed
+    const bool halted = fused && ctrl_halted(ctrl);
     const int order = (int)ctrl->order;
+    const bool arrived = mbar_wait_bounded(&bar, ctrl);
+    if (halted) return;
     int bad_bc = 0;
     if (arrived && tid < cnt) {
         const float mah = P.f_mah;

@@ -175,7 +175,10 @@ static void issue_stage(Handle *h, const Stage &stg) {
         launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl, dist_flags, h->stream);
     } else {
         launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, flux_flags, h->stream);
+        if (!(flux_flags & kNoTimestep))
+            launch_step_clock_mixed(h->P, h->d_ctrl, h->nscen, h->M.shape.pdl, h->stream);
         launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, update_flags, stg, h->stream);
+        launch_step_commit_mixed(h->P, h->d_ctrl, h->nscen, stg, h->M.shape.pdl, h->stream);
         launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl, dist_flags,
                                 h->stream);
     }
@@ -1322,15 +1325,20 @@ int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms) {
         CK(cudaEventRecord(ev[0], h->stream));
         if (h->precision == SWGPU_FP64)
             launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, kFused, h->stream);
-        else
+        else {
             launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused, h->stream);
+            launch_step_clock_mixed(h->P, h->d_ctrl, h->nscen, h->M.shape.pdl, h->stream);
+        }
         CK(cudaEventRecord(ev[1], h->stream));
         if (h->precision == SWGPU_FP64)
             launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, kFused | kFrictionInline,
                                kEulerStage, h->stream);
-        else
+        else {
             launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused | kFrictionInline,
                                 kEulerStage, h->stream);
+            launch_step_commit_mixed(h->P, h->d_ctrl, h->nscen, kEulerStage, h->M.shape.pdl,
+                                     h->stream);
+        }
         CK(cudaEventRecord(ev[2], h->stream));
         if (h->precision == SWGPU_FP64)
             launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,

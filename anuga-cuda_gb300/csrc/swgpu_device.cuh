@@ -309,4 +309,21 @@ __device__ __forceinline__ void apply_pending_halt(Ctrl *c) {
     }
 }
 
+// Mixed path: the step-commit kernel announces a stop decided by
+// commit_step at once (stop reason, summary, halt bit), and halt = 2 means
+// "stopped after this step's distribute": the mixed distribute skips only
+// halt == 1, every other mixed kernel any nonzero halt, and the next step's
+// clock kernel turns 2 into 1.
+__device__ __forceinline__ void announce_halt(Ctrl *c) {
+    if (c->halt_pending) {
+        c->stop_reason = c->halt_pending;
+        c->halt = 2;
+        c->halt_pending = 0;
+        if (c->status) atomicCAS(&c->summary->status, 0, c->status);
+        atomicOr(&c->halt_bits[c->scen >> 5], 1u << (c->scen & 31));
+        __threadfence();
+        atomicAdd(&c->summary->halted, 1);
+    }
+}
+
 }  // namespace swgpu

@@ -233,6 +233,13 @@ void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed
                              int flags, cudaStream_t st);
 void launch_flux_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                        const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st);
+// the step's clock from the fused mixed flux's minimum, per scenario;
+// launched between that flux and the update of a stage that takes a new dt
+void launch_step_clock_mixed(const DevParams &P, Ctrl *ctrl, int nscen, bool pdl,
+                             cudaStream_t st);
+// the stage's commit after the fused mixed update, per scenario
+void launch_step_commit_mixed(const DevParams &P, Ctrl *ctrl, int nscen, const Stage &stage,
+                              bool pdl, cudaStream_t st);
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,
                          cudaStream_t st);

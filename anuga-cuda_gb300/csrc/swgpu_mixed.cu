@@ -434,9 +434,9 @@ __global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMi
     float t = P.f_max_dt;
     if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T, k0, cnt, pk);
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
+    // the step's clock is evaluated from the minimum by step_clock_mixed once
+    // this grid has completed: no block waits on a count of finished blocks
     block_min_timestep_f<TILE>(t, ctrl);
-    if ((flags & kFused) && threadIdx.x == 0 && last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
-        publish_step_clock(ctrl, P);
 }
 
 // The same fluxes with persistent blocks: each block walks tiles
@@ -486,12 +486,7 @@ __global__ void __launch_bounds__(TILE) flux_mixed_pipelined(DevMesh M, DevMixed
         if (!skip) {
             float t = P.f_max_dt;
             if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T[buf], k0, cnt, pk);
-            if (!(flags & kNoTimestep)) {
-                block_min_timestep_f<TILE>(t, ctrl);
-                if ((flags & kFused) && tid == 0 &&
-                    last_block_done(&ctrl->done_flux, ctrl->blocks_flux))
-                    publish_step_clock(ctrl, P);
-            }
+            if (!(flags & kNoTimestep)) block_min_timestep_f<TILE>(t, ctrl);
         }
         __syncthreads();  // everyone is done with T[buf] before it is refilled
         tile = next;
@@ -619,13 +614,9 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
         if ((flags & kTrack) && (stg.kind == kStageEuler || stg.kind == kStageLast))
             track_depth(S, k, h, step_end_time(ctrl, clk, stg), P.track_threshold);
     }
+    // the stage is committed by step_commit_mixed once this grid has completed
     if (bad) set_status(ctrl, SWGPU_EDENOMINATOR);
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
-    if (flags & kFused) {
-        __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_update, ctrl->blocks_update))
-            commit_stage(ctrl, clk, P, stg);
-    }
 }
 
 
@@ -753,8 +744,9 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
         bulk_load(T.uvel, X.uvel + kb, bytes, &bar);
         bulk_load(T.vvel, X.vvel + kb, bytes, &bar);
     }
-    // read while the copies fly; acted on once they have landed
-    const bool halted = fused && ctrl_halted(ctrl);
+    // read while the copies fly; acted on once they have landed (halt == 2:
+    // the scenario stops after this distribute)
+    const bool halted = fused && ctrl_halted(ctrl) == 1;
     const int order = (int)ctrl->order;
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
     if (halted) return;
@@ -969,10 +961,36 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
         }
     }
     if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
-    if (fused) {
-        __syncthreads();
-        if (threadIdx.x == 0 && last_block_done(&ctrl->done_distribute, ctrl->blocks_distribute)) apply_pending_halt(ctrl);
-    }
+}
+
+// update_timestep (the step's clock) of each running scenario, evaluated
+// once from the flux kernel's minimum after that grid has completed and
+// published for the update kernel.  One thread per scenario.
+__global__ void __launch_bounds__(128) step_clock_mixed(Ctrl *ctrl, int nscen, DevParams P) {
+    pdl_launch_dependents();
+    pdl_wait();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nscen) return;
+    Ctrl *c = ctrl + s;
+    const int halt = c->halt;
+    if (halt == 2) c->halt = 1;  // the last step's distribute has run
+    if (halt) return;
+    publish_step_clock(c, P);
+}
+
+// The stage's commit (commit_stage: time, counters, the stop decision) of
+// each running scenario, after the update grid has completed (its status
+// flags included) and before the distribute, which reads the new time.
+__global__ void __launch_bounds__(128) step_commit_mixed(Ctrl *ctrl, int nscen, DevParams P,
+                                                         Stage stg) {
+    pdl_launch_dependents();
+    pdl_wait();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nscen) return;
+    Ctrl *c = ctrl + s;
+    if (c->halt) return;
+    commit_stage(c, published_step_clock(c), P, stg);
+    announce_halt(c);
 }
 
 // Depth from the FP64 stage (after an upload) or from the mixed state, then
@@ -1101,6 +1119,14 @@ void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, co
         launch_k(flux_mixed<256>, g, 256, st, pdl, M, X, P, ctrl, flags);
     else
         launch_k(flux_mixed<128>, g, 128, st, pdl, M, X, P, ctrl, flags);
+}
+void launch_step_clock_mixed(const DevParams &P, Ctrl *ctrl, int nscen, bool pdl,
+                             cudaStream_t st) {
+    launch_k(step_clock_mixed, (nscen + 127) / 128, 128, st, pdl, ctrl, nscen, P);
+}
+void launch_step_commit_mixed(const DevParams &P, Ctrl *ctrl, int nscen, const Stage &stage,
+                              bool pdl, cudaStream_t st) {
+    launch_k(step_commit_mixed, (nscen + 127) / 128, 128, st, pdl, ctrl, nscen, P, stage);
 }
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,

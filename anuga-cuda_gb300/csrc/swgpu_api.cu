@@ -545,6 +545,12 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         TRY(dalloc(h, &X.zhi, s1));
         TRY(dalloc(h, &X.zlo, s1));
         TRY(dalloc(h, &X.kind, s1));
+        TRY(dalloc(h, &X.nbrp, s3));
+        TRY(dalloc(h, &X.surrp, s3));
+        CK(cudaMemcpy2DAsync(X.nbrp, X.S * sizeof(int), M.nbr, (size_t)N * sizeof(int),
+                             (size_t)N * sizeof(int), 3, cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpy2DAsync(X.surrp, X.S * sizeof(int), M.surr, (size_t)N * sizeof(int),
+                             (size_t)N * sizeof(int), 3, cudaMemcpyDeviceToDevice, h->stream));
         // FP64 vertex planes are kept for downloads (stage = depth + bed)
         TRY(dalloc(h, &S.wv, n3));
         TRY(dalloc(h, &S.uhv, n3));

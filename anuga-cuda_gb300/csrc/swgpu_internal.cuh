@@ -104,7 +104,10 @@ struct DevMixed {
     float *fric;                   // [N] Manning n
     float *zmoff;                  // [N] mean(bed vertex) minus bed centroid
     float *zhi, *zlo;              // [N] bed centroid as an FP32 pair hi + lo
-    uint8_t *kind;                 // [N] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat
+    int *nbrp;                     // [3][S] DevMesh::nbr in padded planes (TMA-staged)
+    int *surrp;                    // [3][S] DevMesh::surr in padded planes (TMA-staged)
+    uint8_t *kind;                 // [S] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat;
+                                   // | 16: the triangle has a boundary edge
 };
 
 struct DevParams {

@@ -274,12 +274,13 @@ __device__ __forceinline__ void fence_proxy_async() {
 }
 
 // The flux kernel's own data for one tile of TILE triangles (= threads per
-// block: 64, 128 or 256), filled by 26 bulk copies.
+// block: 64, 128 or 256), filled by 29 bulk copies.
 template <int TILE>
 struct __align__(128) FluxTile {
     float wf[TILE], wlo[TILE], hf[TILE], radius[TILE], inv_area[TILE];
     float he[3][TILE], dwe[3][TILE], uhe[3][TILE], vhe[3][TILE];
     float nx[3][TILE], ny[3][TILE], len[3][TILE];
+    int nbr[3][TILE];  // packed neighbours (read where used: no registers held)
 };
 
 // The bulk copies of a flux tile starting at triangle k0 (span elements of
@@ -291,7 +292,7 @@ __device__ __forceinline__ void flux_tile_issue_static(const DevMixed &X, FluxTi
                                                        unsigned long long *bar) {
     const int SP = X.S;
     const unsigned bytes = (unsigned)span * 4u;
-    mbar_arrive_expect_tx(bar, 26u * bytes);  // the whole tile: 11 static + 15 dynamic planes
+    mbar_arrive_expect_tx(bar, 29u * bytes);  // the whole tile: 14 static + 15 dynamic planes
     bulk_load(T.radius, X.radius + k0, bytes, bar);
     bulk_load(T.inv_area, X.inv_area + k0, bytes, bar);
 #pragma unroll
@@ -299,6 +300,7 @@ __device__ __forceinline__ void flux_tile_issue_static(const DevMixed &X, FluxTi
         bulk_load(T.nx[i], X.nx + i * SP + k0, bytes, bar);
         bulk_load(T.ny[i], X.ny + i * SP + k0, bytes, bar);
         bulk_load(T.len[i], X.len + i * SP + k0, bytes, bar);
+        bulk_load(T.nbr[i], X.nbrp + i * SP + k0, bytes, bar);
     }
 }
 template <int TILE>
@@ -318,7 +320,7 @@ __device__ __forceinline__ void flux_tile_issue_dynamic(const DevMixed &X, FluxT
         bulk_load(T.vhe[i], X.vhe + i * SP + k0, bytes, bar);
     }
 }
-// The 26 bulk copies of a flux tile starting at triangle k0 (span elements
+// The 29 bulk copies of a flux tile starting at triangle k0 (span elements
 // of each padded plane), completing on bar.  Called by one thread.
 template <int TILE>
 __device__ __forceinline__ void flux_tile_issue(const DevMixed &X, FluxTile<TILE> &T, int k0,
@@ -328,20 +330,18 @@ __device__ __forceinline__ void flux_tile_issue(const DevMixed &X, FluxTile<TILE
 }
 
 // Fluxes + gravity_wb of triangle k0 + tid of a staged tile (cnt valid
-// triangles; pk: its packed neighbours); stores the explicit updates and
-// returns the triangle's CFL timestep bound.
+// triangles); stores the explicit updates and returns the triangle's CFL
+// timestep bound.
 template <int TILE>
 __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const DevParams &P,
-                                                    const FluxTile<TILE> &T, int k0, int cnt,
-                                                    const int (&pk)[3]) {
+                                                    const FluxTile<TILE> &T, int k0, int cnt) {
     const int SP = X.S;
     const int tid = threadIdx.x;
     const int k = k0 + tid;
     float t = P.f_max_dt;
     const float eps = P.f_eps;
-    const float wk = T.wf[tid], lk = T.wlo[tid], hc = T.hf[tid];
+    const float wk = T.wf[tid], lk = T.wlo[tid];
     const float rk = T.radius[tid];
-    const float inv_area = T.inv_area[tid];
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // flux sums
     float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
 #pragma unroll
@@ -350,10 +350,11 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
         const float dwl = T.dwe[i][tid], hl = T.he[i][tid];
         const float uhl = T.uhe[i][tid], vhl = T.vhe[i][tid];
         float hr, uhr, vhr, jump, rn = 3.0e38f;
-        if (pk[i] >= 0) {
+        const int pki = T.nbr[i][tid];
+        if (pki >= 0) {
             // the neighbour's stored edge state: the very numbers it uses
             // itself, so both sides see the same two states
-            const int n = pk[i] >> 2, m = pk[i] & 3;
+            const int n = pki >> 2, m = pki & 3;
             const int ln = n - k0;
             float wn, lnn, dwn;
             if ((unsigned)ln < (unsigned)cnt) {
@@ -375,7 +376,7 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
             }
             jump = ((wn - wk) + (lnn - lk)) + (dwn - dwl);
         } else {
-            const int mb = -pk[i] - 1;
+            const int mb = -pki - 1;
             hr = ro(X.hbf + mb);
             jump = ro(X.wjb + mb);
             uhr = ro(X.uhbf + mb);
@@ -392,7 +393,8 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
         // min(rk/ms, rn/ms) = min(rk, rn)/ms: one division per edge
         if (ms > eps) t = ominf(t, __fdividef(fminf(rk, rn), ms));
     }
-    const float ghc = P.f_g * hc;
+    const float ghc = P.f_g * T.hf[tid];
+    const float inv_area = T.inv_area[tid];
     X.ew[k] = a0 * inv_area;
     X.euh[k] = (a1 - ghc * gx) * inv_area;
     X.evh[k] = (a2 - ghc * gy) * inv_area;
@@ -420,11 +422,6 @@ __global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMi
     // geometry and neighbour indices do not change between steps: fetched
     // while the previous kernel may still run
     if (tid == 0) flux_tile_issue_static<TILE>(X, T, k0, span, &bar);
-    int pk[3] = {0, 0, 0};
-    if (tid < cnt) {
-#pragma unroll
-        for (int i = 0; i < 3; i++) pk[i] = ro(M.nbr + i * N + k0 + tid);
-    }
     pdl_wait();
     if (tid == 0) flux_tile_issue_dynamic<TILE>(X, T, k0, span, &bar);
     // read while the copies fly; acted on once they have landed
@@ -432,7 +429,7 @@ __global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMi
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
     if (halted) return;
     float t = P.f_max_dt;
-    if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T, k0, cnt, pk);
+    if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T, k0, cnt);
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
     // the step's clock is evaluated from the minimum by step_clock_mixed once
     // this grid has completed: no block waits on a count of finished blocks
@@ -476,16 +473,11 @@ __global__ void __launch_bounds__(TILE) flux_mixed_pipelined(DevMesh M, DevMixed
         const int cnt = min(TILE, N - k0);
         Ctrl *ctrl = M.blk_scen ? ctrl_base + M.blk_scen[k0 >> 8] : ctrl_base;
         const bool skip = (flags & kFused) && ctrl_halted(ctrl);
-        int pk[3] = {0, 0, 0};
-        if (!skip && tid < cnt) {
-#pragma unroll
-            for (int i = 0; i < 3; i++) pk[i] = ro(M.nbr + i * N + k0 + tid);
-        }
         const bool arrived = mbar_wait_bounded(&bar[buf], ctrl, (parity >> buf) & 1u);
         parity ^= 1u << buf;
         if (!skip) {
             float t = P.f_max_dt;
-            if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T[buf], k0, cnt, pk);
+            if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T[buf], k0, cnt);
             if (!(flags & kNoTimestep)) block_min_timestep_f<TILE>(t, ctrl);
         }
         __syncthreads();  // everyone is done with T[buf] before it is refilled
@@ -679,14 +671,64 @@ __device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], floa
     limit_f(d, qmin, qmax, beta);
 }
 
+// Boundary values (evaluate_segment, per boundary type) of triangle k's
+// boundary edges from the edge values this thread has just stored.  Out of
+// line: boundary triangles are rare, and the FP64 evaluation inlined would
+// raise the register pressure of every thread of the distribute.  Returns 1
+// when an edge's boundary could not be evaluated.
+__device__ __noinline__ int boundary_edges_mixed(int k, int N, int SP, double time, double g,
+                                                 const int *nbr, const int *btag,
+                                                 const BcTag *tags, const double *ze_,
+                                                 const float *he, const float *uhe_,
+                                                 const float *vhe_, const float *nx,
+                                                 const float *ny, double *wb_, double *uhb_,
+                                                 double *vhb_, double *zb_, float *hbf,
+                                                 float *wjb, float *uhbf, float *vhbf) {
+    int bad = 0;
+    for (int i = 0; i < 3; i++) {
+        const int pk = ro(nbr + i * N + k);
+        if (pk >= 0) continue;
+        const int mb = -pk - 1;
+        const float hle = he[i * SP + k];  // this thread's own stores: plain loads
+        const double ze = ro(ze_ + i * N + k);
+        const double we = ze + widen(hle);
+        const BcTag &T = tags[ro(btag + mb)];
+        double wb, uhb, vhb;
+        if (!eval_boundary(T, time, we, widen(uhe_[i * SP + k]), widen(vhe_[i * SP + k]),
+                           widen(ro(nx + i * SP + k)), widen(ro(ny + i * SP + k)), ze, g, wb, uhb,
+                           vhb)) {
+            bad = 1;
+            wb = we;
+            uhb = vhb = 0.0;
+        }
+        wb_[mb] = wb;
+        uhb_[mb] = uhb;
+        vhb_[mb] = vhb;
+        zb_[mb] = ze;
+        if (boundary_keeps_edge_stage(T.type)) {
+            // same depth and stage as the edge: exactly no jump
+            hbf[mb] = hle;
+            wjb[mb] = 0.0f;
+        } else {
+            hbf[mb] = (float)(wb - ze);
+            wjb[mb] = (float)(wb - we);
+        }
+        uhbf[mb] = (float)uhb;
+        vhbf[mb] = (float)vhb;
+    }
+    return bad;
+}
+
 // The distribute kernel's own data for one tile of BS triangles, filled by
-// 17 bulk copies.
+// 21 bulk copies.
 template <int BS>
 struct __align__(128) DistTile {
     float wf[BS], wlo[BS], hf[BS], uvel[BS], vvel[BS];
     float gc[6][BS];
     float dzv[3][BS];
     float dze[3][BS];
+    int sur[3][BS];      // surrogate neighbours
+    uint8_t kind[BS];    // DevMixed::kind
 };
 
 // Centroid value of neighbour n: from the tile when n is one of the block's
@@ -721,20 +763,16 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
     // static planes (reconstruction coefficients, bed offsets) and index
     // planes before the previous kernel has finished
     if (tid == 0) {
-        mbar_arrive_expect_tx(&bar, 17u * bytes);
+        mbar_arrive_expect_tx(&bar, 20u * bytes + (unsigned)span);
 #pragma unroll
         for (int j = 0; j < 6; j++) bulk_load(T.gc[j], X.gc + j * SP + kb, bytes, &bar);
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             bulk_load(T.dzv[i], X.dzv + i * SP + kb, bytes, &bar);
             bulk_load(T.dze[i], X.dze + i * SP + kb, bytes, &bar);
+            bulk_load(T.sur[i], X.surrp + i * SP + kb, bytes, &bar);
         }
-    }
-    int sur[3] = {0, 0, 0}, kind = 2;
-    if (tid < cnt) {
-        kind = ro(X.kind + k);
-#pragma unroll
-        for (int i = 0; i < 3; i++) sur[i] = ro(M.surr + i * N + k);
+        bulk_load(T.kind, X.kind + kb, (unsigned)span, &bar);  // span: a multiple of 64 bytes
     }
     pdl_wait();
     if (tid == 0) {
@@ -752,6 +790,7 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
     if (halted) return;
     int bad_bc = 0;
     if (arrived && tid < cnt) {
+        const int kind = T.kind[tid];
         const float mah = P.f_mah;
         const float wk = T.wf[tid], lk = T.wlo[tid], hc = T.hf[tid];
         const float qu = T.uvel[tid], qv = T.vvel[tid];
@@ -772,7 +811,7 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
 #pragma unroll
                 for (int j = 0; j < 6; j++) c[j] = T.gc[j][tid];
                 if ((kind & 3) == 0) {
-                    const int k0 = sur[0], k1 = sur[1], k2 = sur[2];
+                    const int k0 = T.sur[0][tid], k1 = T.sur[1][tid], k2 = T.sur[2][tid];
                     const float h0 = tile_or_global(T.hf, X.hf, k0, kb, cnt);
                     const float h1 = tile_or_global(T.hf, X.hf, k1, kb, cnt);
                     const float h2 = tile_or_global(T.hf, X.hf, k2, kb, cnt);
@@ -812,8 +851,7 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
                     }
                 } else {
                     const int slot = (kind >> 2) & 3;
-                    // selected without indexing, which would put sur in local memory
-                    const int k1 = slot == 0 ? sur[0] : (slot == 1 ? sur[1] : sur[2]);
+                    const int k1 = T.sur[slot][tid];
                     const float h1 = tile_or_global(T.hf, X.hf, k1, kb, cnt);
                     const float beta = P.f_beta_w;
                     one_jumps_f((tile_or_global(T.wf, X.wf, k1, kb, cnt) - wk) +
@@ -910,55 +948,18 @@ __global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, Dev
         }
         // edge values (quantity.c:687-706 interpolation) stored for the flux:
         // depth, stage jump from the centroid, momentum
-        float hle_[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-            hle_[i] = edge_depth(hc, dw[a], dw[b], T.dze[i][tid]);
-            X.he[i * SP + k] = hle_[i];
+            X.he[i * SP + k] = edge_depth(hc, dw[a], dw[b], T.dze[i][tid]);
             X.dwe[i * SP + k] = 0.5f * (dw[a] + dw[b]);
             X.uhe[i * SP + k] = 0.5f * (ou[a] + ou[b]);
             X.vhe[i * SP + k] = 0.5f * (ov[a] + ov[b]);
         }
-        if ((flags & kWriteBoundary) && ro(M.nb + k) > 0) {
-            const double time = ctrl->time;
-#pragma unroll
-            for (int i = 0; i < 3; i++) {
-                const int pk = ro(M.nbr + i * N + k);
-                if (pk < 0) {
-                    const int mb = -pk - 1;
-                    const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-                    const float hle = hle_[i];
-                    const double ze = ro(S.ze + i * N + k);
-                    const double we = ze + widen(hle);
-                    const float uhe = 0.5f * (ou[a] + ou[b]);
-                    const float vhe = 0.5f * (ov[a] + ov[b]);
-                    const BcTag &T = tags[ro(M.btag + mb)];
-                    double wb, uhb, vhb;
-                    if (!eval_boundary(T, time, we, widen(uhe), widen(vhe),
-                                       widen(ro(X.nx + i * SP + k)), widen(ro(X.ny + i * SP + k)),
-                                       ze, P.g, wb, uhb, vhb)) {
-                        bad_bc = 1;
-                        wb = we;
-                        uhb = vhb = 0.0;
-                    }
-                    S.wb[mb] = wb;
-                    S.uhb[mb] = uhb;
-                    S.vhb[mb] = vhb;
-                    S.zb[mb] = ze;
-                    if (boundary_keeps_edge_stage(T.type)) {
-                        // same depth and stage as the edge: exactly no jump
-                        X.hbf[mb] = hle;
-                        X.wjb[mb] = 0.0f;
-                    } else {
-                        X.hbf[mb] = (float)(wb - ze);
-                        X.wjb[mb] = (float)(wb - we);
-                    }
-                    X.uhbf[mb] = (float)uhb;
-                    X.vhbf[mb] = (float)vhb;
-                }
-            }
-        }
+        if ((flags & kWriteBoundary) && (kind & 16))  // a boundary edge
+            bad_bc = boundary_edges_mixed(k, N, SP, ctrl->time, P.g, M.nbr, M.btag, tags, S.ze,
+                                          X.he, X.uhe, X.vhe, X.nx, X.ny, S.wb, S.uhb, S.vhb,
+                                          S.zb, X.hbf, X.wjb, X.uhbf, X.vhbf);
     }
     if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
 }
@@ -1226,6 +1227,7 @@ int build_mixed_geometry(Handle *h) {
                 for (int i = 0; i < 3; i++) c[2 * i] = (dx1 * dxv[i] + dy1 * dyv[i]) / area2;
             }
         }
+        if (h->h_nb[k] > 0) kd |= 16;  // has a boundary edge
         kind[k] = kd;
         for (int j = 0; j < 6; j++) gc[j * sp + k] = (float)c[j];
     }

@@ -637,15 +637,25 @@ __device__ __forceinline__ void qminmax_f(float dq0, float dq1, float dq2, float
     }
 }
 
-// limit_gradient (shallow_water_ext.c:151-181); correctly rounded divisions
-// (the limiter's branch points are where FP32 error would grow)
+// a / b from the approximate reciprocal and one Newton correction of the
+// quotient (Markstein's method: q = a r, q += r (a - b q)), within about an
+// ulp; for the |b| > 1e-30 of the limiter, under FTZ.
+__device__ __forceinline__ float div_refined(float a, float b) {
+    const float r = __fdividef(1.0f, b);
+    const float q = a * r;
+    return fmaf(fmaf(-b, q, a), r, q);
+}
+
+// limit_gradient (shallow_water_ext.c:151-181); refined divisions (the
+// limiter is where FP32 error grows most: an approximate quotient here
+// raised the 1000-step stage error by 14%, the refined one by 0.04%)
 __device__ __forceinline__ void limit_f(float (&d)[3], float qmin, float qmax, float beta) {
     const float TINY = 1.0e-30f;
     float r = 1000.0f, r0 = 1.0f;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        if (d[i] < -TINY) r0 = __fdiv_rn(qmin, d[i]);
-        if (d[i] > TINY) r0 = __fdiv_rn(qmax, d[i]);
+        if (d[i] < -TINY) r0 = div_refined(qmin, d[i]);
+        if (d[i] > TINY) r0 = div_refined(qmax, d[i]);
         r = ominf(r0, r);
     }
     const float phi = ominf(r * beta, 1.0f);
@@ -743,7 +753,7 @@ __device__ __forceinline__ float tile_or_global(const float *tile, const float *
 // block stages its tile's own planes with one-dimensional TMA bulk copies
 // into shared memory and reads in-tile neighbours from there.
 template <int BS>
-__global__ void __launch_bounds__(BS, 1536 / BS) distribute_mixed(DevMesh M, DevState S, DevMixed X,
+__global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, DevState S, DevMixed X,
                                                            DevParams P, const BcTag *tags,
                                                            Ctrl *ctrl, int flags) {
     const bool fused = flags & kFused;

@@ -460,6 +460,12 @@ __global__ void __launch_bounds__(TILE) flux_mixed_pipelined(DevMesh M, DevMixed
     if (tid == 0 && tile < ntiles)
         flux_tile_issue_dynamic<TILE>(X, T[0], tile * TILE, min(TILE, X.S - tile * TILE), &bar[0]);
     if (tile + (int)gridDim.x >= ntiles) pdl_launch_dependents();
+    // the block's timestep minimum is taken over all its tiles of one
+    // scenario and reduced once (at the end, or when the scenario changes):
+    // no per-tile barrier waits for the atomic
+    Ctrl *acc_ctrl = nullptr;
+    float tacc = P.f_max_dt;
+    const bool take_dt = !(flags & kNoTimestep);
     while (tile < ntiles) {
         const int next = tile + gridDim.x;
         // the next kernel's blocks may start once every block is on its last tile
@@ -473,17 +479,20 @@ __global__ void __launch_bounds__(TILE) flux_mixed_pipelined(DevMesh M, DevMixed
         const int cnt = min(TILE, N - k0);
         Ctrl *ctrl = M.blk_scen ? ctrl_base + M.blk_scen[k0 >> 8] : ctrl_base;
         const bool skip = (flags & kFused) && ctrl_halted(ctrl);
+        if (take_dt && acc_ctrl && ctrl != acc_ctrl) {  // uniform over the block
+            block_min_timestep_f<TILE>(tacc, acc_ctrl);
+            tacc = P.f_max_dt;
+        }
+        acc_ctrl = ctrl;
         const bool arrived = mbar_wait_bounded(&bar[buf], ctrl, (parity >> buf) & 1u);
         parity ^= 1u << buf;
-        if (!skip) {
-            float t = P.f_max_dt;
-            if (arrived && tid < cnt) t = flux_tile_triangle<TILE>(X, P, T[buf], k0, cnt);
-            if (!(flags & kNoTimestep)) block_min_timestep_f<TILE>(t, ctrl);
-        }
+        if (!skip && arrived && tid < cnt)
+            tacc = ominf(tacc, flux_tile_triangle<TILE>(X, P, T[buf], k0, cnt));
         __syncthreads();  // everyone is done with T[buf] before it is refilled
         tile = next;
         buf ^= 1;
     }
+    if (take_dt && acc_ctrl) block_min_timestep_f<TILE>(tacc, acc_ctrl);
 }
 
 // FP32 copies of the updated state and protect (shallow_water_ext.c:
@@ -1115,9 +1124,17 @@ void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, co
     const int t = M.shape.flux, g = (M.n_launch + t - 1) / t;
     const bool pdl = M.shape.pdl;
     if (M.shape.pipelined && t <= 128) {
-        // resident blocks per SM: 8 of 128 threads or 16 of 64 (two tiles of
-        // shared memory each)
-        const int grid = std::min(g, (t == 64 ? 16 : 8) * std::max(M.shape.sms, 1));
+        // one wave of persistent blocks: as many as are resident per SM
+        static int resident[2] = {0, 0};
+        int &r = resident[t == 64 ? 0 : 1];
+        if (r == 0) {
+            if (t == 64)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, flux_mixed_pipelined<64>, 64, 0);
+            else
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, flux_mixed_pipelined<128>, 128, 0);
+            r = std::max(r, 1);
+        }
+        const int grid = std::min(g, r * std::max(M.shape.sms, 1));
         if (t == 64)
             launch_k(flux_mixed_pipelined<64>, grid, 64, st, pdl, M, X, P, ctrl, flags, g);
         else

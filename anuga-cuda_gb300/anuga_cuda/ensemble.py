@@ -61,6 +61,19 @@ def _pad_mesh():
                 {(0, 0): "pad", (0, 1): "pad", (0, 2): "pad"}, reorder=False)
 
 
+def _initial_timestep(sc, g=9.8):
+    """The scenario's CFL timestep at rest, min over wet triangles of
+    radius / sqrt(g h) (over all triangles with h = 1 m when none is wet):
+    a proxy for its number of steps to a common finaltime (on the inflow
+    harbours its rank order equals that of the steps actually taken)."""
+    r = np.asarray(sc.mesh.radii, dtype=np.float64)
+    h = np.asarray(sc.stage_centroid, dtype=np.float64) - sc.elevation_arrays()[0]
+    wet = h > 0.01
+    if not wet.any():
+        return float(np.min(r) / np.sqrt(g))
+    return float(np.min(r[wet] / np.sqrt(g * h[wet])))
+
+
 class Ensemble:
     """``scenarios``: a list of Scenario objects (mesh, initial state,
     friction, boundaries).  ``precision`` "mixed" (default) or "fp64"."""
@@ -69,11 +82,12 @@ class Ensemble:
         if not scenarios:
             raise ValueError("an ensemble needs at least one scenario")
         scenarios = list(scenarios)
-        # Internally the scenarios expected to run longest (the largest
-        # meshes: smallest triangles, smallest steps) come first, so that
-        # the launches can stop short of the finished ones at the end;
-        # every per-scenario input and output is in the caller's order.
-        self.order = sorted(range(len(scenarios)), key=lambda i: -scenarios[i].N)
+        # Internally the scenarios expected to run longest (the smallest
+        # initial CFL timestep, i.e. the most steps) come first, so that the
+        # launches can stop short of the finished ones at the end; every
+        # per-scenario input and output is in the caller's order.
+        dt0 = [_initial_timestep(sc) for sc in scenarios]
+        self.order = sorted(range(len(scenarios)), key=lambda i: (dt0[i], -scenarios[i].N, i))
         self.scenarios = [scenarios[i] for i in self.order]
         self.parameters = parameters or DEFAULT
         self.precision = precision

@@ -9,7 +9,7 @@ and the first time the depth exceeded a threshold.  The surrogate
 (``libswgpu`` ``swgpu_mlp_*``: 16 -> 128 -> 128 -> 2, BF16 tensor cores)
 learns both from the scenario parameters and the triangle's bed,
 coordinates and distance to the hump centre (the depth as its excess over
-the still-water depth, which the bathymetry alone fixes), and predicts them
+the initial depth, which the parameters fix exactly), and predicts them
 for new parameters in one pass over all (scenario, triangle) rows.
 
 ``fallback_report`` compares predictions with solver fields on held-out
@@ -32,7 +32,8 @@ from .ensemble import ALIGN, Ensemble
 from .scenarios import Scenario, wet_dry
 
 __all__ = ["PARAM_NAMES", "PARAM_RANGES", "FamilyMesh", "sample_params", "family_scenario",
-           "solve", "Surrogate", "init_params", "fallback_report", "still_depth", "targets_from"]
+           "solve", "Surrogate", "init_params", "fallback_report", "still_depth", "initial_depth",
+           "targets_from"]
 
 PARAM_NAMES = ("height", "x0", "y0", "radius", "manning", "sea_level", "aspect", "u0", "v0")
 PARAM_RANGES = np.array([(0.5, 3.0), (3000.0, 7000.0), (3000.0, 7000.0), (150.0, 500.0),
@@ -108,11 +109,26 @@ def still_depth(fm: FamilyMesh, thetas):
     return np.maximum(eta - fm.zc[None, :], 0.0).astype(np.float32)
 
 
+def initial_depth(fm: FamilyMesh, thetas):
+    """Depth of each scenario's initial state, [S][N]: the hump over the sea
+    at rest (as family_scenario builds it).  The maximum depth is at least
+    this, and the part the network learns is its excess: the sharp Gaussian
+    of the hump itself is known exactly from the parameters."""
+    th = np.asarray(thetas, np.float64)
+    x, y = fm.xy[:, 0], fm.xy[:, 1]
+    out = np.empty((len(th), fm.N), np.float32)
+    for s, (A, x0, y0, rad, _n, eta, asp, _u, _v) in enumerate(th):
+        dx, dy = x - x0, y - y0
+        shape = np.exp(-(dx * dx / (2 * rad * rad) + dy * dy / (2 * (asp * rad) ** 2)))
+        out[s] = np.maximum(eta + A * shape - fm.zc, 0.0)
+    return out
+
+
 def targets_from(fm: FamilyMesh, thetas, hmax, tarr, finaltime):
     """Normalised targets [S][N][2]: the maximum depth in excess of the
-    still-water depth, and the arrival time."""
+    initial depth, and the arrival time."""
     t = np.empty(hmax.shape + (2,), np.float32)
-    t[..., 0] = (hmax - still_depth(fm, thetas)) / DEPTH_SCALE
+    t[..., 0] = (hmax - initial_depth(fm, thetas)) / DEPTH_SCALE
     t[..., 1] = np.where(tarr >= 0, tarr / finaltime, NEVER)
     return t
 
@@ -228,7 +244,7 @@ class Surrogate:
         self._check(lib().swgpu_mlp_predict(self._h, 0, S * N, C.c_void_p(out.data_ptr()),
                                             _f32p(ms)), self._h)
         y = out.cpu().numpy().reshape(S, N, 2)
-        depth = np.maximum(still_depth(self.fm, thetas) + y[..., 0] * DEPTH_SCALE, 0.0)
+        depth = np.maximum(initial_depth(self.fm, thetas) + y[..., 0] * DEPTH_SCALE, 0.0)
         arr = np.where(y[..., 1] > 0.5 * (1.0 + NEVER), -1.0, np.clip(y[..., 1], 0, 1))
         return depth, arr, float(ms[0])
 

@@ -77,7 +77,7 @@ def parse():
     ap.add_argument("--surrogate-train", type=int, default=2048)
     ap.add_argument("--surrogate-test", type=int, default=512)
     ap.add_argument("--surrogate-finaltime", type=float, default=300.0)
-    ap.add_argument("--surrogate-steps", type=int, default=4000)
+    ap.add_argument("--surrogate-steps", type=int, default=40000)
     return ap.parse_args()
 
 

@@ -39,7 +39,7 @@ def test_gradients_match_oracle(small_family, swgpu_built):
 
 
 def test_predict_equals_training_forward(small_family, swgpu_built):
-    from anuga_cuda.surrogate import DEPTH_SCALE, Surrogate, sample_params, still_depth
+    from anuga_cuda.surrogate import DEPTH_SCALE, Surrogate, initial_depth, sample_params
     fm = small_family
     sg = Surrogate(fm, seed=4)
     sg.set_tensor_path("mma.sync")   # the training forward's own kernel code
@@ -49,7 +49,7 @@ def test_predict_equals_training_forward(small_family, swgpu_built):
     rows = np.arange(3 * fm.N)
     y, _, _ = sg.gradients(rows)
     depth, _, _ = sg.predict(th)
-    exp = np.maximum(still_depth(fm, th).ravel() + y[:, 0] * DEPTH_SCALE, 0)
+    exp = np.maximum(initial_depth(fm, th).ravel() + y[:, 0] * DEPTH_SCALE, 0)
     assert np.array_equal(depth.ravel(), exp)
 
 
@@ -93,7 +93,7 @@ def test_tcgen05_inference_matches(small_family, swgpu_built):
     """The tcgen05/TMEM inference kernel against the mma.sync one and the
     NumPy FP64 restatement (BF16 rounding points alike; accumulation order
     differs, so within the BF16 tolerance)."""
-    from anuga_cuda.surrogate import DEPTH_SCALE, Surrogate, sample_params, still_depth
+    from anuga_cuda.surrogate import DEPTH_SCALE, Surrogate, initial_depth, sample_params
     from oracle import mlp_oracle as MO
     fm = small_family
     sg = Surrogate(fm, seed=11)
@@ -108,5 +108,5 @@ def test_tcgen05_inference_matches(small_family, swgpu_built):
     rows = np.arange(5 * fm.N)
     yo, _, _ = MO.forward_backward(sg.params(), th, fm.tri, rows,
                                    np.zeros((5, fm.N, 2), np.float32), sg.mu, sg.isd)
-    ref = np.maximum(still_depth(fm, th).ravel() + yo[:, 0] * DEPTH_SCALE, 0)
+    ref = np.maximum(initial_depth(fm, th).ravel() + yo[:, 0] * DEPTH_SCALE, 0)
     assert np.max(np.abs(d_tc.ravel() - ref)) <= TOL * scale

@@ -201,8 +201,12 @@ __device__ __forceinline__ void block_min_timestep(double t, Ctrl *ctrl) {
 
 // FP32 variant for the mixed flux: the reduction stays in FP32 and only the
 // block's minimum is widened for the atomic.
+// ftmin_seen: the running minimum as read earlier by the block (default:
+// read it here, after the reduction).
 template <int BLOCK = kBlock>
-__device__ __forceinline__ void block_min_timestep_f(float t, Ctrl *ctrl) {
+__device__ __forceinline__ void block_min_timestep_f(float t, Ctrl *ctrl,
+                                                     const unsigned long long *ftmin_seen =
+                                                         nullptr) {
     __shared__ float wminf[BLOCK / 32];
     for (int o = 16; o > 0; o >>= 1) t = ominf(t, __shfl_xor_sync(0xffffffffu, t, o));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -217,8 +221,9 @@ __device__ __forceinline__ void block_min_timestep_f(float t, Ctrl *ctrl) {
             } else {
                 const double td = (double)t;
                 const unsigned long long bits = (unsigned long long)__double_as_longlong(td);
-                if (bits < *(volatile unsigned long long *)&ctrl->ftmin_bits)
-                    atomicMin(&ctrl->ftmin_bits, bits);
+                const unsigned long long seen =
+                    ftmin_seen ? *ftmin_seen : *(volatile unsigned long long *)&ctrl->ftmin_bits;
+                if (bits < seen) atomicMin(&ctrl->ftmin_bits, bits);
             }
         }
     }

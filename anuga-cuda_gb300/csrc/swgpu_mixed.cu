@@ -426,6 +426,11 @@ __global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMi
     if (tid == 0) flux_tile_issue_dynamic<TILE>(X, T, k0, span, &bar);
     // read while the copies fly; acted on once they have landed
     const bool halted = (flags & kFused) && ctrl_halted(ctrl);
+    // the running timestep minimum, read (by the thread that will reduce)
+    // while the copies fly: the block's atomic is skipped when it cannot
+    // lower it, without a read at the end
+    __shared__ unsigned long long ft_seen;
+    if (tid == 0) ft_seen = *(volatile unsigned long long *)&ctrl->ftmin_bits;
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
     if (halted) return;
     float t = P.f_max_dt;
@@ -433,7 +438,7 @@ __global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMi
     if (flags & kNoTimestep) return;  // later Runge-Kutta stage: the step's dt is set
     // the step's clock is evaluated from the minimum by step_clock_mixed once
     // this grid has completed: no block waits on a count of finished blocks
-    block_min_timestep_f<TILE>(t, ctrl);
+    block_min_timestep_f<TILE>(t, ctrl, &ft_seen);
 }
 
 // The same fluxes with persistent blocks: each block walks tiles

@@ -589,9 +589,9 @@ class GPU_domain:
         """Domain.evolve as a generator (gpu_domain_advanced.py:2296-2697).
 
         The time loop runs on the device: each Euler stage is three kernels
-        (flux, update, distribute; the mixed path adds two one-thread-per-
-        scenario kernels for the step's clock and its commit; an RK2 step
-        is two stages, an RK3 step three; set_timestepping_method),
+        (flux, update, distribute; the mixed path adds a one-thread-per-
+        scenario kernel for the step's clock; an RK2 step is two stages,
+        an RK3 step three; set_timestepping_method),
         the timestep is reduced on the device, and steps are issued as CUDA
         graphs; the host synchronises only between graphs and at yields.
         ``max_steps`` (added) stops after that many steps in total."""

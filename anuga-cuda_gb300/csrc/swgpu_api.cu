@@ -178,8 +178,7 @@ static void issue_stage(Handle *h, const Stage &stg) {
         if (!(flux_flags & kNoTimestep))
             launch_step_clock_mixed(h->P, h->d_ctrl, h->nscen, h->M.shape.pdl, h->stream);
         launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, update_flags, stg, h->stream);
-        launch_step_commit_mixed(h->P, h->d_ctrl, h->nscen, stg, h->M.shape.pdl, h->stream);
-        launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl, dist_flags,
+        launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl, dist_flags, stg,
                                 h->stream);
     }
 }
@@ -231,7 +230,7 @@ static int issue_distribute(Handle *h, bool with_boundary) {
         launch_prepare_mixed(h->M, h->S, h->X, h->P, h->mixed_from_stage ? 1 : 0, h->stream);
         h->mixed_from_stage = false;
         launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl,
-                                with_boundary ? kWriteBoundary : 0, h->stream);
+                                with_boundary ? kWriteBoundary : 0, kEulerStage, h->stream);
     }
     h->vertices_stale = false;
     return check_launch(h, "distribute");
@@ -1339,19 +1338,16 @@ int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms) {
         if (h->precision == SWGPU_FP64)
             launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, kFused | kFrictionInline,
                                kEulerStage, h->stream);
-        else {
+        else
             launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused | kFrictionInline,
                                 kEulerStage, h->stream);
-            launch_step_commit_mixed(h->P, h->d_ctrl, h->nscen, kEulerStage, h->M.shape.pdl,
-                                     h->stream);
-        }
         CK(cudaEventRecord(ev[2], h->stream));
         if (h->precision == SWGPU_FP64)
             launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,
                                    kFused | kWriteBoundary, h->stream);
         else
             launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl,
-                                    kFused | kWriteBoundary, h->stream);
+                                    kFused | kWriteBoundary, kEulerStage, h->stream);
         CK(cudaEventRecord(ev[3], h->stream));
         if ((rc = check_launch(h, "profile step"))) return rc;
         CK(cudaEventSynchronize(ev[3]));

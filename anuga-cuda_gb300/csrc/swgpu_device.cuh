@@ -172,6 +172,7 @@ __device__ __forceinline__ void publish_step_clock(Ctrl *c, const DevParams &P) 
     c->clk_order = s.order;
     c->clk_smallsteps = s.smallsteps;
     c->clk_small_error = s.small_error;
+    c->clk_t0 = c->time;
 }
 
 // Block-wide minimum of a positive double, then one atomicMin on its bit
@@ -314,11 +315,11 @@ __device__ __forceinline__ void apply_pending_halt(Ctrl *c) {
     }
 }
 
-// Mixed path: the step-commit kernel announces a stop decided by
-// commit_step at once (stop reason, summary, halt bit), and halt = 2 means
-// "stopped after this step's distribute": the mixed distribute skips only
-// halt == 1, every other mixed kernel any nonzero halt, and the next step's
-// clock kernel turns 2 into 1.
+// Mixed path: the stage commit (in the distribute's first block of the
+// scenario) announces a stop decided by commit_step at once (stop reason,
+// summary, halt bit), and halt = 2 means "stopped after this step's
+// distribute": the mixed distribute skips only halt == 1, every other mixed
+// kernel any nonzero halt, and the next step's clock kernel turns 2 into 1.
 __device__ __forceinline__ void announce_halt(Ctrl *c) {
     if (c->halt_pending) {
         c->stop_reason = c->halt_pending;

@@ -138,9 +138,11 @@ struct RunSummary {
     int status;
 };
 
-// Device-resident evolve bookkeeping, one per scenario.  Written by the last block of the
-// update kernel (time, order, counters) and the last block of the
-// distribute kernel (halt); read by every kernel at entry.
+// Device-resident evolve bookkeeping, one per scenario.  FP64 path: written by the
+// last block of the update kernel (time, order, counters) and the last block of
+// the distribute kernel (halt).  Mixed path: the step clock kernel publishes the
+// clock, the first block of the scenario in the distribute commits the stage.
+// Read by every kernel at entry.
 struct __align__(16) Ctrl {
     unsigned long long ftmin_bits;  // minimum flux timestep of this step (bits of a positive double)
     double time, yieldtime, finaltime, yieldstep, timestep, flux_timestep;
@@ -155,6 +157,7 @@ struct __align__(16) Ctrl {
     int clk_small_error;            // the step's update_timestep, evaluated once by
     double clk_dt, clk_ftmin;       // the last block of the flux kernel and read
     long long clk_order, clk_smallsteps;  // by the update kernel
+    double clk_t0;                  // model time when that clock was evaluated
     double step_t0;                 // time at the start of a Runge-Kutta step
     unsigned int blocks_flux;       // blocks of this scenario in one flux launch
     unsigned int blocks_update;     // ... in one update launch
@@ -231,18 +234,17 @@ void launch_mass(const DevMesh &M, const DevState &S, double *out, cudaStream_t 
 void launch_mass_partials(const DevMesh &M, const DevState &S, cudaStream_t st);
 
 // Mixed path (swgpu_mixed.cu)
+// with kFused, the stage `stage` is committed by the distribute (see
+// distribute_mixed); stand-alone calls pass kEulerStage
 void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                              const DevParams &P, const BcTag *tags, Ctrl *ctrl,
-                             int flags, cudaStream_t st);
+                             int flags, const Stage &stage, cudaStream_t st);
 void launch_flux_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                        const DevParams &P, Ctrl *ctrl, int flags, cudaStream_t st);
 // the step's clock from the fused mixed flux's minimum, per scenario;
 // launched between that flux and the update of a stage that takes a new dt
 void launch_step_clock_mixed(const DevParams &P, Ctrl *ctrl, int nscen, bool pdl,
                              cudaStream_t st);
-// the stage's commit after the fused mixed update, per scenario
-void launch_step_commit_mixed(const DevParams &P, Ctrl *ctrl, int nscen, const Stage &stage,
-                              bool pdl, cudaStream_t st);
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,
                          cudaStream_t st);

@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
         if ((flags & kTrack) && (stg.kind == kStageEuler || stg.kind == kStageLast))
             track_depth(S, k, h, step_end_time(ctrl, clk, stg), P.track_threshold);
     }
-    // the stage is committed by step_commit_mixed once this grid has completed
+    // the stage is committed by the distribute (its scenario's first block)
     if (bad) set_status(ctrl, SWGPU_EDENOMINATOR);
     if (nonfinite) set_status(ctrl, SWGPU_ENONFINITE);
 }
@@ -766,10 +766,16 @@ __device__ __forceinline__ float tile_or_global(const float *tile, const float *
 // Extrapolation + balance + boundary conditions, FP32, in stage jumps.  Each
 // block stages its tile's own planes with one-dimensional TMA bulk copies
 // into shared memory and reads in-tile neighbours from there.
+//
+// In the fused step the stage `stg` is committed here (commit_stage: time,
+// counters, the stop decision, announce_halt) by the first block of each
+// scenario, once the update grid has completed; every block takes the
+// stage's order and end time from the step's clock (clk_*), which the commit
+// does not write, so no block depends on when the commit runs.
 template <int BS>
 __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, DevState S, DevMixed X,
                                                            DevParams P, const BcTag *tags,
-                                                           Ctrl *ctrl, int flags) {
+                                                           Ctrl *ctrl, int flags, Stage stg) {
     const bool fused = flags & kFused;
     pdl_launch_dependents();
     ctrl = block_ctrl(ctrl, M);
@@ -809,7 +815,21 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
     // read while the copies fly; acted on once they have landed (halt == 2:
     // the scenario stops after this distribute)
     const bool halted = fused && ctrl_halted(ctrl) == 1;
-    const int order = (int)ctrl->order;
+    int order;
+    double time;
+    if (fused) {
+        order = (int)ctrl->clk_order;
+        time = ctrl->clk_t0 + ctrl->clk_dt * (stg.kind == kStageMid ? stg.tfrac : 1.0);
+        const bool first = blockIdx.x == 0 ||
+                           (M.blk_scen && M.blk_scen[(kb - 1) >> 8] != M.blk_scen[kb >> 8]);
+        if (first && tid == 0 && !halted) {
+            commit_stage(ctrl, published_step_clock(ctrl), P, stg);
+            announce_halt(ctrl);
+        }
+    } else {
+        order = (int)ctrl->order;
+        time = ctrl->time;
+    }
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
     if (halted) return;
     int bad_bc = 0;
@@ -981,7 +1001,7 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
             X.vhe[i * SP + k] = 0.5f * (ov[a] + ov[b]);
         }
         if ((flags & kWriteBoundary) && (kind & 16))  // a boundary edge
-            bad_bc = boundary_edges_mixed(k, N, SP, ctrl->time, P.g, M.nbr, M.btag, tags, S.ze,
+            bad_bc = boundary_edges_mixed(k, N, SP, time, P.g, M.nbr, M.btag, tags, S.ze,
                                           X.he, X.uhe, X.vhe, X.nx, X.ny, S.wb, S.uhb, S.vhb,
                                           S.zb, X.hbf, X.wjb, X.uhbf, X.vhbf);
     }
@@ -1001,21 +1021,6 @@ __global__ void __launch_bounds__(128) step_clock_mixed(Ctrl *ctrl, int nscen, D
     if (halt == 2) c->halt = 1;  // the last step's distribute has run
     if (halt) return;
     publish_step_clock(c, P);
-}
-
-// The stage's commit (commit_stage: time, counters, the stop decision) of
-// each running scenario, after the update grid has completed (its status
-// flags included) and before the distribute, which reads the new time.
-__global__ void __launch_bounds__(128) step_commit_mixed(Ctrl *ctrl, int nscen, DevParams P,
-                                                         Stage stg) {
-    pdl_launch_dependents();
-    pdl_wait();
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nscen) return;
-    Ctrl *c = ctrl + s;
-    if (c->halt) return;
-    commit_stage(c, published_step_clock(c), P, stg);
-    announce_halt(c);
 }
 
 // Depth from the FP64 stage (after an upload) or from the mixed state, then
@@ -1114,15 +1119,15 @@ static void launch_k(void (*k)(KArgs...), int grid, int block, cudaStream_t st, 
 
 void launch_distribute_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                              const DevParams &P, const BcTag *tags, Ctrl *ctrl, int flags,
-                             cudaStream_t st) {
+                             const Stage &stage, cudaStream_t st) {
     const int bs = M.shape.distribute, g = (M.n_launch + bs - 1) / bs;
     const bool pdl = M.shape.pdl;
     if (bs == 128)
-        launch_k(distribute_mixed<128>, g, 128, st, pdl, M, S, X, P, tags, ctrl, flags);
+        launch_k(distribute_mixed<128>, g, 128, st, pdl, M, S, X, P, tags, ctrl, flags, stage);
     else if (bs == 512)
-        launch_k(distribute_mixed<512>, g, 512, st, pdl, M, S, X, P, tags, ctrl, flags);
+        launch_k(distribute_mixed<512>, g, 512, st, pdl, M, S, X, P, tags, ctrl, flags, stage);
     else
-        launch_k(distribute_mixed<256>, g, 256, st, pdl, M, S, X, P, tags, ctrl, flags);
+        launch_k(distribute_mixed<256>, g, 256, st, pdl, M, S, X, P, tags, ctrl, flags, stage);
 }
 void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, const DevParams &P,
                        Ctrl *ctrl, int flags, cudaStream_t st) {
@@ -1156,10 +1161,6 @@ void launch_flux_mixed(const DevMesh &M, const DevState &, const DevMixed &X, co
 void launch_step_clock_mixed(const DevParams &P, Ctrl *ctrl, int nscen, bool pdl,
                              cudaStream_t st) {
     launch_k(step_clock_mixed, (nscen + 127) / 128, 128, st, pdl, ctrl, nscen, P);
-}
-void launch_step_commit_mixed(const DevParams &P, Ctrl *ctrl, int nscen, const Stage &stage,
-                              bool pdl, cudaStream_t st) {
-    launch_k(step_commit_mixed, (nscen + 127) / 128, 128, st, pdl, ctrl, nscen, P, stage);
 }
 void launch_update_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                          const DevParams &P, Ctrl *ctrl, int flags, const Stage &stage,

@@ -470,9 +470,9 @@ def main():
                      "step_model_frac": MODEL_BYTES["mixed"] * N / (mixed_ms / K / 1000.0) / 1e9
                      / peak_gbs},
         "clocks": r["mixed"]["clocks"],
-        # the timed region launches whole graphs of 16 steps x 5 kernels
-        # (flux, step clock, update, step commit, distribute)
-        "gpu_launches": 5 * 16 * ((K + 15) // 16),
+        # the timed region launches whole graphs of 16 steps x 4 kernels
+        # (flux, step clock, update, distribute)
+        "gpu_launches": 4 * 16 * ((K + 15) // 16),
     }
     if out["e2e"]:
         line["e2e"] = {k: out["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step",

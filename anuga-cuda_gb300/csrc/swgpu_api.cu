@@ -520,10 +520,7 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         TRY(dalloc(h, &X.hf, s1));
         TRY(dalloc(h, &X.uvel, s1));
         TRY(dalloc(h, &X.vvel, s1));
-        TRY(dalloc(h, &X.he, s3));
-        TRY(dalloc(h, &X.dwe, s3));
-        TRY(dalloc(h, &X.uhe, s3));
-        TRY(dalloc(h, &X.vhe, s3));
+        TRY(dalloc(h, &X.es, s3));
         TRY(dalloc(h, &X.hbf, nb1));
         TRY(dalloc(h, &X.uhbf, nb1));
         TRY(dalloc(h, &X.vhbf, nb1));

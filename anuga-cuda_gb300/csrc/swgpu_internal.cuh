@@ -91,8 +91,8 @@ struct DevMixed {
     float *wf, *wlo;               // [N] centroid stage as hi + lo FP32 pair (single planes
                                    // are allocated with S elements too)
     float *hf, *uvel, *vvel;       // [N] centroid depth, velocities
-    float *he, *dwe;               // [3][N] edge depth, edge stage jump from the centroid
-    float *uhe, *vhe;              // [3][N] edge momentum
+    float4 *es;                    // [3][S] edge state: x depth, y stage jump from the
+                                   // centroid, z/w momentum (one 16-byte load per edge)
     float *hbf, *uhbf, *vhbf;      // [Nb] boundary depth and momentum
     float *wjb;                    // [Nb] boundary stage minus the owner's edge stage
     float *ew, *euh, *evh;         // [N] explicit_update

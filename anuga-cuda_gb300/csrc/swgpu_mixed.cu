@@ -278,7 +278,7 @@ __device__ __forceinline__ void fence_proxy_async() {
 template <int TILE>
 struct __align__(128) FluxTile {
     float wf[TILE], wlo[TILE], hf[TILE], radius[TILE], inv_area[TILE];
-    float he[3][TILE], dwe[3][TILE], uhe[3][TILE], vhe[3][TILE];
+    float4 es[3][TILE];  // edge state (depth, stage jump, momenta) per edge
     float nx[3][TILE], ny[3][TILE], len[3][TILE];
     int nbr[3][TILE];  // packed neighbours (read where used: no registers held)
 };
@@ -314,10 +314,7 @@ __device__ __forceinline__ void flux_tile_issue_dynamic(const DevMixed &X, FluxT
     bulk_load(T.hf, X.hf + k0, bytes, bar);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        bulk_load(T.he[i], X.he + i * SP + k0, bytes, bar);
-        bulk_load(T.dwe[i], X.dwe + i * SP + k0, bytes, bar);
-        bulk_load(T.uhe[i], X.uhe + i * SP + k0, bytes, bar);
-        bulk_load(T.vhe[i], X.vhe + i * SP + k0, bytes, bar);
+        bulk_load(T.es[i], X.es + i * SP + k0, 4u * bytes, bar);
     }
 }
 // The 29 bulk copies of a flux tile starting at triangle k0 (span elements
@@ -347,8 +344,8 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const float n1 = T.nx[i][tid], n2 = T.ny[i][tid], L = T.len[i][tid];
-        const float dwl = T.dwe[i][tid], hl = T.he[i][tid];
-        const float uhl = T.uhe[i][tid], vhl = T.vhe[i][tid];
+        const float4 el = T.es[i][tid];
+        const float hl = el.x, dwl = el.y, uhl = el.z, vhl = el.w;
         float hr, uhr, vhr, jump, rn = 3.0e38f;
         const int pki = T.nbr[i][tid];
         if (pki >= 0) {
@@ -357,23 +354,22 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
             const int n = pki >> 2, m = pki & 3;
             const int ln = n - k0;
             float wn, lnn, dwn;
+            float4 en;
             if ((unsigned)ln < (unsigned)cnt) {
-                hr = T.he[m][ln];
-                dwn = T.dwe[m][ln];
-                uhr = T.uhe[m][ln];
-                vhr = T.vhe[m][ln];
+                en = T.es[m][ln];
                 wn = T.wf[ln];
                 lnn = T.wlo[ln];
                 rn = T.radius[ln];
             } else {
-                hr = ro(X.he + m * SP + n);
-                dwn = ro(X.dwe + m * SP + n);
-                uhr = ro(X.uhe + m * SP + n);
-                vhr = ro(X.vhe + m * SP + n);
+                en = ro(X.es + m * SP + n);
                 wn = ro(X.wf + n);
                 lnn = ro(X.wlo + n);
                 rn = ro(X.radius + n);
             }
+            hr = en.x;
+            dwn = en.y;
+            uhr = en.z;
+            vhr = en.w;
             jump = ((wn - wk) + (lnn - lk)) + (dwn - dwl);
         } else {
             const int mb = -pki - 1;
@@ -703,8 +699,7 @@ __device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], floa
 __device__ __noinline__ int boundary_edges_mixed(int k, int N, int SP, double time, double g,
                                                  const int *nbr, const int *btag,
                                                  const BcTag *tags, const double *ze_,
-                                                 const float *he, const float *uhe_,
-                                                 const float *vhe_, const float *nx,
+                                                 const float4 *es, const float *nx,
                                                  const float *ny, double *wb_, double *uhb_,
                                                  double *vhb_, double *zb_, float *hbf,
                                                  float *wjb, float *uhbf, float *vhbf) {
@@ -713,12 +708,13 @@ __device__ __noinline__ int boundary_edges_mixed(int k, int N, int SP, double ti
         const int pk = ro(nbr + i * N + k);
         if (pk >= 0) continue;
         const int mb = -pk - 1;
-        const float hle = he[i * SP + k];  // this thread's own stores: plain loads
+        const float4 e = es[i * SP + k];  // this thread's own stores: a plain load
+        const float hle = e.x;
         const double ze = ro(ze_ + i * N + k);
         const double we = ze + widen(hle);
         const BcTag &T = tags[ro(btag + mb)];
         double wb, uhb, vhb;
-        if (!eval_boundary(T, time, we, widen(uhe_[i * SP + k]), widen(vhe_[i * SP + k]),
+        if (!eval_boundary(T, time, we, widen(e.z), widen(e.w),
                            widen(ro(nx + i * SP + k)), widen(ro(ny + i * SP + k)), ze, g, wb, uhb,
                            vhb)) {
             bad = 1;
@@ -917,9 +913,10 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
                 float e0[3], e1[3], e2[3];
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    e0[i] = X.dwe[i * SP + k];
-                    e1[i] = X.uhe[i * SP + k];
-                    e2[i] = X.vhe[i * SP + k];
+                    const float4 e = X.es[i * SP + k];  // this thread's own, before it stores
+                    e0[i] = e.y;
+                    e1[i] = e.z;
+                    e2[i] = e.w;
                 }
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
@@ -995,14 +992,13 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             const int a = (i == 0) ? 1 : 0, b = (i == 2) ? 1 : 2;
-            X.he[i * SP + k] = edge_depth(hc, dw[a], dw[b], T.dze[i][tid]);
-            X.dwe[i * SP + k] = 0.5f * (dw[a] + dw[b]);
-            X.uhe[i * SP + k] = 0.5f * (ou[a] + ou[b]);
-            X.vhe[i * SP + k] = 0.5f * (ov[a] + ov[b]);
+            X.es[i * SP + k] = make_float4(edge_depth(hc, dw[a], dw[b], T.dze[i][tid]),
+                                           0.5f * (dw[a] + dw[b]), 0.5f * (ou[a] + ou[b]),
+                                           0.5f * (ov[a] + ov[b]));
         }
         if ((flags & kWriteBoundary) && (kind & 16))  // a boundary edge
             bad_bc = boundary_edges_mixed(k, N, SP, time, P.g, M.nbr, M.btag, tags, S.ze,
-                                          X.he, X.uhe, X.vhe, X.nx, X.ny, S.wb, S.uhb, S.vhb,
+                                          X.es, X.nx, X.ny, S.wb, S.uhb, S.vhb,
                                           S.zb, X.hbf, X.wjb, X.uhbf, X.vhbf);
     }
     if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
@@ -1056,9 +1052,10 @@ __global__ void __launch_bounds__(kBlock) vertices_from_mixed(DevMesh M, DevStat
     float e0[3], e1[3], e2[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        e0[i] = X.dwe[i * SP + k];
-        e1[i] = X.uhe[i * SP + k];
-        e2[i] = X.vhe[i * SP + k];
+        const float4 e = X.es[i * SP + k];
+        e0[i] = e.y;
+        e1[i] = e.z;
+        e2[i] = e.w;
     }
 #pragma unroll
     for (int i = 0; i < 3; i++) {

@@ -515,11 +515,9 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         X.S = (int)(((size_t)N + 63) / 64 * 64);
         const size_t s1 = X.S, s3 = 3 * s1, s6 = 6 * s1;
         TRY(dalloc(h, &X.hd, s1));
-        TRY(dalloc(h, &X.wf, s1));
-        TRY(dalloc(h, &X.wlo, s1));
+        TRY(dalloc(h, &X.ws, s1));
         TRY(dalloc(h, &X.hf, s1));
-        TRY(dalloc(h, &X.uvel, s1));
-        TRY(dalloc(h, &X.vvel, s1));
+        TRY(dalloc(h, &X.vel, s1));
         TRY(dalloc(h, &X.es, s3));
         TRY(dalloc(h, &X.hbf, nb1));
         TRY(dalloc(h, &X.uhbf, nb1));

@@ -88,9 +88,9 @@ struct DevMixed {
     int S;                         // stride of the [3]/[6] planes: N rounded up to 64, so
                                    // that every plane and 16-triangle tile is 64-B aligned
     double *hd;                    // [N] FP64 depth (conserved)
-    float *wf, *wlo;               // [N] centroid stage as hi + lo FP32 pair (single planes
-                                   // are allocated with S elements too)
-    float *hf, *uvel, *vvel;       // [N] centroid depth, velocities
+    float2 *ws;                    // [S] centroid stage as an FP32 pair, x hi + y lo
+    float *hf;                     // [S] centroid depth
+    float2 *vel;                   // [S] centroid velocities, x u + y v
     float4 *es;                    // [3][S] edge state: x depth, y stage jump from the
                                    // centroid, z/w momentum (one 16-byte load per edge)
     float *hbf, *uhbf, *vhbf;      // [Nb] boundary depth and momentum

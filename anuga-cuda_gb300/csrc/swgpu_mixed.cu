@@ -277,7 +277,8 @@ __device__ __forceinline__ void fence_proxy_async() {
 // block: 64, 128 or 256), filled by 29 bulk copies.
 template <int TILE>
 struct __align__(128) FluxTile {
-    float wf[TILE], wlo[TILE], hf[TILE], radius[TILE], inv_area[TILE];
+    float2 ws[TILE];  // stage pair
+    float hf[TILE], radius[TILE], inv_area[TILE];
     float4 es[3][TILE];  // edge state (depth, stage jump, momenta) per edge
     float nx[3][TILE], ny[3][TILE], len[3][TILE];
     int nbr[3][TILE];  // packed neighbours (read where used: no registers held)
@@ -309,8 +310,7 @@ __device__ __forceinline__ void flux_tile_issue_dynamic(const DevMixed &X, FluxT
                                                         unsigned long long *bar) {
     const int SP = X.S;
     const unsigned bytes = (unsigned)span * 4u;
-    bulk_load(T.wf, X.wf + k0, bytes, bar);
-    bulk_load(T.wlo, X.wlo + k0, bytes, bar);
+    bulk_load(T.ws, X.ws + k0, 2u * bytes, bar);
     bulk_load(T.hf, X.hf + k0, bytes, bar);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -337,7 +337,8 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
     const int k = k0 + tid;
     float t = P.f_max_dt;
     const float eps = P.f_eps;
-    const float wk = T.wf[tid], lk = T.wlo[tid];
+    const float2 wsk = T.ws[tid];
+    const float wk = wsk.x, lk = wsk.y;
     const float rk = T.radius[tid];
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // flux sums
     float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
@@ -355,17 +356,18 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
             const int ln = n - k0;
             float wn, lnn, dwn;
             float4 en;
+            float2 wsn;
             if ((unsigned)ln < (unsigned)cnt) {
                 en = T.es[m][ln];
-                wn = T.wf[ln];
-                lnn = T.wlo[ln];
+                wsn = T.ws[ln];
                 rn = T.radius[ln];
             } else {
                 en = ro(X.es + m * SP + n);
-                wn = ro(X.wf + n);
-                lnn = ro(X.wlo + n);
+                wsn = ro(X.ws + n);
                 rn = ro(X.radius + n);
             }
+            wn = wsn.x;
+            lnn = wsn.y;
             hr = en.x;
             dwn = en.y;
             uhr = en.z;
@@ -565,7 +567,8 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
         bv = ro(S.bvh + kk);
     }
     const float hf0 = ro(X.hf + kk);  // FP32 copies of the pre-update state
-    const float uv0 = ro(X.uvel + kk), vv0 = ro(X.vvel + kk);
+    const float2 vel0 = ro(X.vel + kk);
+    const float uv0 = vel0.x, vv0 = vel0.y;
     const float ew = ro(X.ew + kk), euh = ro(X.euh + kk), evh = ro(X.evh + kk);
     if (halted) return;
     const float dtf = (float)clk.dt;
@@ -609,10 +612,8 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
         S.uh[k] = uh;
         S.vh[k] = vh;
         X.hf[k] = hf;
-        X.wf[k] = wf;
-        X.wlo[k] = wl;
-        X.uvel[k] = uv;
-        X.vvel[k] = vv;
+        X.ws[k] = make_float2(wf, wl);
+        X.vel[k] = make_float2(uv, vv);
         if ((flags & kTrack) && (stg.kind == kStageEuler || stg.kind == kStageLast))
             track_depth(S, k, h, step_end_time(ctrl, clk, stg), P.track_threshold);
     }
@@ -743,7 +744,9 @@ __device__ __noinline__ int boundary_edges_mixed(int k, int N, int SP, double ti
 // 21 bulk copies.
 template <int BS>
 struct __align__(128) DistTile {
-    float wf[BS], wlo[BS], hf[BS], uvel[BS], vvel[BS];
+    float2 ws[BS];   // stage pair
+    float hf[BS];
+    float2 vel[BS];  // velocities
     float gc[6][BS];
     float dzv[3][BS];
     float dze[3][BS];
@@ -753,8 +756,9 @@ struct __align__(128) DistTile {
 
 // Centroid value of neighbour n: from the tile when n is one of the block's
 // triangles (most, in Morton order), else from global memory.
-__device__ __forceinline__ float tile_or_global(const float *tile, const float *plane, int n,
-                                                int kb, int cnt) {
+template <typename V>
+__device__ __forceinline__ V tile_or_global(const V *tile, const V *plane, int n, int kb,
+                                            int cnt) {
     const int ln = n - kb;
     return (unsigned)ln < (unsigned)cnt ? tile[ln] : ro(plane + n);
 }
@@ -802,11 +806,9 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
     }
     pdl_wait();
     if (tid == 0) {
-        bulk_load(T.wf, X.wf + kb, bytes, &bar);
-        bulk_load(T.wlo, X.wlo + kb, bytes, &bar);
+        bulk_load(T.ws, X.ws + kb, 2u * bytes, &bar);
         bulk_load(T.hf, X.hf + kb, bytes, &bar);
-        bulk_load(T.uvel, X.uvel + kb, bytes, &bar);
-        bulk_load(T.vvel, X.vvel + kb, bytes, &bar);
+        bulk_load(T.vel, X.vel + kb, 2u * bytes, &bar);
     }
     // read while the copies fly; acted on once they have landed (halt == 2:
     // the scenario stops after this distribute)
@@ -832,8 +834,9 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
     if (arrived && tid < cnt) {
         const int kind = T.kind[tid];
         const float mah = P.f_mah;
-        const float wk = T.wf[tid], lk = T.wlo[tid], hc = T.hf[tid];
-        const float qu = T.uvel[tid], qv = T.vvel[tid];
+        const float2 wsk = T.ws[tid], velk = T.vel[tid];
+        const float wk = wsk.x, lk = wsk.y, hc = T.hf[tid];
+        const float qu = velk.x, qv = velk.y;
         const bool vel = P.extrapolate_velocity_second_order == 1;
         const float hk = omaxf(hc, mah);
         const float uk = qu * hk, vk = qv * hk;  // centroid momentum
@@ -862,20 +865,18 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
                     } else {
                         float hfactor = 0.0f;
                         if (hmin > 0.001f) hfactor = (hmin - 0.001f) / (hmin + 0.004f);
-                        const float w0 = tile_or_global(T.wf, X.wf, k0, kb, cnt);
-                        const float w1 = tile_or_global(T.wf, X.wf, k1, kb, cnt);
-                        const float w2 = tile_or_global(T.wf, X.wf, k2, kb, cnt);
-                        const float l0 = tile_or_global(T.wlo, X.wlo, k0, kb, cnt);
-                        const float l1 = tile_or_global(T.wlo, X.wlo, k1, kb, cnt);
-                        const float l2 = tile_or_global(T.wlo, X.wlo, k2, kb, cnt);
+                        const float2 s0 = tile_or_global(T.ws, X.ws, k0, kb, cnt);
+                        const float2 s1 = tile_or_global(T.ws, X.ws, k1, kb, cnt);
+                        const float2 s2 = tile_or_global(T.ws, X.ws, k2, kb, cnt);
+                        const float w0 = s0.x, w1 = s1.x, w2 = s2.x;
+                        const float l0 = s0.y, l1 = s1.y, l2 = s2.y;
                         aux_jumps_f((w0 - wk) + (l0 - lk), (w1 - w0) + (l1 - l0), (w2 - w0) + (l2 - l0), c,
                                     P.f_beta_w_dry + (P.f_beta_w - P.f_beta_w_dry) * hfactor, dw);
-                        float u0 = tile_or_global(T.uvel, X.uvel, k0, kb, cnt);
-                        float u1 = tile_or_global(T.uvel, X.uvel, k1, kb, cnt);
-                        float u2 = tile_or_global(T.uvel, X.uvel, k2, kb, cnt);
-                        float v0 = tile_or_global(T.vvel, X.vvel, k0, kb, cnt);
-                        float v1 = tile_or_global(T.vvel, X.vvel, k1, kb, cnt);
-                        float v2 = tile_or_global(T.vvel, X.vvel, k2, kb, cnt);
+                        const float2 q0 = tile_or_global(T.vel, X.vel, k0, kb, cnt);
+                        const float2 q1 = tile_or_global(T.vel, X.vel, k1, kb, cnt);
+                        const float2 q2 = tile_or_global(T.vel, X.vel, k2, kb, cnt);
+                        float u0 = q0.x, u1 = q1.x, u2 = q2.x;
+                        float v0 = q0.y, v1 = q1.y, v2 = q2.y;
                         if (!vel) {
                             u0 *= omaxf(h0, mah);
                             v0 *= omaxf(h0, mah);
@@ -894,11 +895,11 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
                     const int k1 = T.sur[slot][tid];
                     const float h1 = tile_or_global(T.hf, X.hf, k1, kb, cnt);
                     const float beta = P.f_beta_w;
-                    one_jumps_f((tile_or_global(T.wf, X.wf, k1, kb, cnt) - wk) +
-                                    (tile_or_global(T.wlo, X.wlo, k1, kb, cnt) - lk),
+                    const float2 s1 = tile_or_global(T.ws, X.ws, k1, kb, cnt);
+                    one_jumps_f((s1.x - wk) + (s1.y - lk),
                                 c, beta, dw);
-                    float u1 = tile_or_global(T.uvel, X.uvel, k1, kb, cnt);
-                    float v1 = tile_or_global(T.vvel, X.vvel, k1, kb, cnt);
+                    const float2 q1 = tile_or_global(T.vel, X.vel, k1, kb, cnt);
+                    float u1 = q1.x, v1 = q1.y;
                     if (!vel) {
                         u1 *= omaxf(h1, mah);
                         v1 *= omaxf(h1, mah);
@@ -1034,10 +1035,8 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
     S.uh[k] = uh;
     S.vh[k] = vh;
     X.hf[k] = hf;
-    X.wf[k] = wf;
-    X.wlo[k] = wl;
-    X.uvel[k] = uv;
-    X.vvel[k] = vv;
+    X.ws[k] = make_float2(wf, wl);
+    X.vel[k] = make_float2(uv, vv);
 }
 
 // FP64 stage centroid / vertex values and momentum vertex values for

@@ -513,7 +513,7 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
     } else {
         DevMixed &X = h->X;
         X.S = (int)(((size_t)N + 63) / 64 * 64);
-        const size_t s1 = X.S, s3 = 3 * s1, s6 = 6 * s1;
+        const size_t s1 = X.S, s3 = 3 * s1;
         TRY(dalloc(h, &X.hd, s1));
         TRY(dalloc(h, &X.ws, s1));
         TRY(dalloc(h, &X.hf, s1));
@@ -526,12 +526,11 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         TRY(dalloc(h, &X.ew, s1));
         TRY(dalloc(h, &X.euh, s1));
         TRY(dalloc(h, &X.evh, s1));
-        TRY(dalloc(h, &X.nx, s3));
-        TRY(dalloc(h, &X.ny, s3));
+        TRY(dalloc(h, &X.nrm, s3));
         TRY(dalloc(h, &X.len, s3));
         TRY(dalloc(h, &X.inv_area, s1));
         TRY(dalloc(h, &X.radius, s1));
-        TRY(dalloc(h, &X.gc, s6));
+        TRY(dalloc(h, &X.gc, s3));
         TRY(dalloc(h, &X.dzv, s3));
         TRY(dalloc(h, &X.dze, s3));
         TRY(dalloc(h, &X.fric, s1));

@@ -96,9 +96,10 @@ struct DevMixed {
     float *hbf, *uhbf, *vhbf;      // [Nb] boundary depth and momentum
     float *wjb;                    // [Nb] boundary stage minus the owner's edge stage
     float *ew, *euh, *evh;         // [N] explicit_update
-    float *nx, *ny, *len;          // [3][N] normals, edge lengths
+    float2 *nrm;                   // [3][S] unit normals (x, y)
+    float *len;                    // [3][S] edge lengths
     float *inv_area, *radius;      // [N]
-    float *gc;                     // [6][N] vertex-jump coefficients (dq1, dq2 per vertex)
+    float2 *gc;                    // [3][S] vertex-jump coefficients of vertex i (dq1, dq2)
     float *dzv;                    // [3][N] bed vertex minus bed centroid
     float *dze;                    // [3][N] bed edge minus bed centroid
     float *fric;                   // [N] Manning n

@@ -280,7 +280,8 @@ struct __align__(128) FluxTile {
     float2 ws[TILE];  // stage pair
     float hf[TILE], radius[TILE], inv_area[TILE];
     float4 es[3][TILE];  // edge state (depth, stage jump, momenta) per edge
-    float nx[3][TILE], ny[3][TILE], len[3][TILE];
+    float2 nrm[3][TILE];  // unit normals
+    float len[3][TILE];
     int nbr[3][TILE];  // packed neighbours (read where used: no registers held)
 };
 
@@ -298,8 +299,7 @@ __device__ __forceinline__ void flux_tile_issue_static(const DevMixed &X, FluxTi
     bulk_load(T.inv_area, X.inv_area + k0, bytes, bar);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        bulk_load(T.nx[i], X.nx + i * SP + k0, bytes, bar);
-        bulk_load(T.ny[i], X.ny + i * SP + k0, bytes, bar);
+        bulk_load(T.nrm[i], X.nrm + i * SP + k0, 2u * bytes, bar);
         bulk_load(T.len[i], X.len + i * SP + k0, bytes, bar);
         bulk_load(T.nbr[i], X.nbrp + i * SP + k0, bytes, bar);
     }
@@ -344,7 +344,8 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
     float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        const float n1 = T.nx[i][tid], n2 = T.ny[i][tid], L = T.len[i][tid];
+        const float2 nr = T.nrm[i][tid];
+        const float n1 = nr.x, n2 = nr.y, L = T.len[i][tid];
         const float4 el = T.es[i][tid];
         const float hl = el.x, dwl = el.y, uhl = el.z, vhl = el.w;
         float hr, uhr, vhr, jump, rn = 3.0e38f;
@@ -700,8 +701,8 @@ __device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], floa
 __device__ __noinline__ int boundary_edges_mixed(int k, int N, int SP, double time, double g,
                                                  const int *nbr, const int *btag,
                                                  const BcTag *tags, const double *ze_,
-                                                 const float4 *es, const float *nx,
-                                                 const float *ny, double *wb_, double *uhb_,
+                                                 const float4 *es, const float2 *nrm,
+                                                 double *wb_, double *uhb_,
                                                  double *vhb_, double *zb_, float *hbf,
                                                  float *wjb, float *uhbf, float *vhbf) {
     int bad = 0;
@@ -716,7 +717,8 @@ __device__ __noinline__ int boundary_edges_mixed(int k, int N, int SP, double ti
         const BcTag &T = tags[ro(btag + mb)];
         double wb, uhb, vhb;
         if (!eval_boundary(T, time, we, widen(e.z), widen(e.w),
-                           widen(ro(nx + i * SP + k)), widen(ro(ny + i * SP + k)), ze, g, wb, uhb,
+                           widen(ro(nrm + i * SP + k).x), widen(ro(nrm + i * SP + k).y), ze, g,
+                           wb, uhb,
                            vhb)) {
             bad = 1;
             wb = we;
@@ -747,7 +749,7 @@ struct __align__(128) DistTile {
     float2 ws[BS];   // stage pair
     float hf[BS];
     float2 vel[BS];  // velocities
-    float gc[6][BS];
+    float2 gc[3][BS];  // per vertex: the coefficients of dq1 and dq2
     float dzv[3][BS];
     float dze[3][BS];
     int sur[3][BS];      // surrogate neighbours
@@ -795,7 +797,7 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
     if (tid == 0) {
         mbar_arrive_expect_tx(&bar, 20u * bytes + (unsigned)span);
 #pragma unroll
-        for (int j = 0; j < 6; j++) bulk_load(T.gc[j], X.gc + j * SP + kb, bytes, &bar);
+        for (int i = 0; i < 3; i++) bulk_load(T.gc[i], X.gc + i * SP + kb, 2u * bytes, &bar);
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             bulk_load(T.dzv[i], X.dzv + i * SP + kb, bytes, &bar);
@@ -852,7 +854,11 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
             if ((kind & 3) != 2) {
                 float c[6];
 #pragma unroll
-                for (int j = 0; j < 6; j++) c[j] = T.gc[j][tid];
+                for (int i = 0; i < 3; i++) {
+                    const float2 g = T.gc[i][tid];
+                    c[2 * i] = g.x;
+                    c[2 * i + 1] = g.y;
+                }
                 if ((kind & 3) == 0) {
                     const int k0 = T.sur[0][tid], k1 = T.sur[1][tid], k2 = T.sur[2][tid];
                     const float h0 = tile_or_global(T.hf, X.hf, k0, kb, cnt);
@@ -999,7 +1005,7 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
         }
         if ((flags & kWriteBoundary) && (kind & 16))  // a boundary edge
             bad_bc = boundary_edges_mixed(k, N, SP, time, P.g, M.nbr, M.btag, tags, S.ze,
-                                          X.es, X.nx, X.ny, S.wb, S.uhb, S.vhb,
+                                          X.es, X.nrm, S.wb, S.uhb, S.vhb,
                                           S.zb, X.hbf, X.wjb, X.uhbf, X.vhbf);
     }
     if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
@@ -1204,14 +1210,15 @@ int build_mixed_geometry(Handle *h) {
         cudaMemcpy(fr.data(), h->S.fric, n1 * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
         return SWGPU_ECUDA;
     // FP32 planes use the padded stride sp (see DevMixed::S)
-    std::vector<float> nx(3 * sp), ny(3 * sp), len(3 * sp), inv_area(n1), radius(n1), gc(6 * sp),
+    std::vector<float2> nrm(3 * sp), gc(3 * sp);
+    std::vector<float> len(3 * sp), inv_area(n1), radius(n1),
         dzv(3 * sp), dze(3 * sp), fric(n1), zmoff(n1), zhi(n1), zlo(n1);
     std::vector<uint8_t> kind(n1);
     const std::vector<double> &V = h->h_vxy, &C = h->h_cxy;
     for (int k = 0; k < N; k++) {
         for (int i = 0; i < 3; i++) {
-            nx[i * sp + k] = (float)h->h_normals[(2 * i) * n1 + k];
-            ny[i * sp + k] = (float)h->h_normals[(2 * i + 1) * n1 + k];
+            nrm[i * sp + k] = make_float2((float)h->h_normals[(2 * i) * n1 + k],
+                                          (float)h->h_normals[(2 * i + 1) * n1 + k]);
             len[i * sp + k] = (float)h->h_len[i * n1 + k];
             dzv[i * sp + k] = (float)(zv[i * n1 + k] - zc[k]);
             dze[i * sp + k] = (float)(ze[i * n1 + k] - zc[k]);
@@ -1258,19 +1265,18 @@ int build_mixed_geometry(Handle *h) {
         }
         if (h->h_nb[k] > 0) kd |= 16;  // has a boundary edge
         kind[k] = kd;
-        for (int j = 0; j < 6; j++) gc[j * sp + k] = (float)c[j];
+        for (int i = 0; i < 3; i++) gc[i * sp + k] = make_float2((float)c[2 * i], (float)c[2 * i + 1]);
     }
     const DevMixed &X = h->X;
     cudaError_t e = cudaSuccess;
     auto put = [&](void *dst, const void *src, size_t bytes) {
         if (e == cudaSuccess) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
     };
-    put(X.nx, nx.data(), 3 * sp * 4);
-    put(X.ny, ny.data(), 3 * sp * 4);
+    put(X.nrm, nrm.data(), 3 * sp * 8);
     put(X.len, len.data(), 3 * sp * 4);
     put(X.inv_area, inv_area.data(), n1 * 4);
     put(X.radius, radius.data(), n1 * 4);
-    put(X.gc, gc.data(), 6 * sp * 4);
+    put(X.gc, gc.data(), 3 * sp * 8);
     put(X.dzv, dzv.data(), 3 * sp * 4);
     put(X.dze, dze.data(), 3 * sp * 4);
     put(X.fric, fric.data(), n1 * 4);

@@ -523,13 +523,11 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         TRY(dalloc(h, &X.uhbf, nb1));
         TRY(dalloc(h, &X.vhbf, nb1));
         TRY(dalloc(h, &X.wjb, nb1));
-        TRY(dalloc(h, &X.ew, s1));
-        TRY(dalloc(h, &X.euh, s1));
+        TRY(dalloc(h, &X.ewu, s1));
         TRY(dalloc(h, &X.evh, s1));
         TRY(dalloc(h, &X.nrm, s3));
         TRY(dalloc(h, &X.len, s3));
-        TRY(dalloc(h, &X.inv_area, s1));
-        TRY(dalloc(h, &X.radius, s1));
+        TRY(dalloc(h, &X.rad, s1));
         TRY(dalloc(h, &X.gc, s3));
         TRY(dalloc(h, &X.dzv, s3));
         TRY(dalloc(h, &X.dze, s3));

@@ -95,13 +95,14 @@ struct DevMixed {
                                    // centroid, z/w momentum (one 16-byte load per edge)
     float *hbf, *uhbf, *vhbf;      // [Nb] boundary depth and momentum
     float *wjb;                    // [Nb] boundary stage minus the owner's edge stage
-    float *ew, *euh, *evh;         // [N] explicit_update
+    float2 *ewu;                   // [S] explicit_update of depth (x) and x momentum (y)
+    float *evh;                    // [S] explicit_update of y momentum
     float2 *nrm;                   // [3][S] unit normals (x, y)
     float *len;                    // [3][S] edge lengths
-    float *inv_area, *radius;      // [N]
+    float2 *rad;                   // [S] x radius, y 1/area
     float2 *gc;                    // [3][S] vertex-jump coefficients of vertex i (dq1, dq2)
-    float *dzv;                    // [3][N] bed vertex minus bed centroid
-    float *dze;                    // [3][N] bed edge minus bed centroid
+    float *dzv;                    // [3][S] bed vertex minus bed centroid
+    float *dze;                    // [3][S] bed edge minus bed centroid
     float *fric;                   // [N] Manning n
     float *zmoff;                  // [N] mean(bed vertex) minus bed centroid
     float *zhi, *zlo;              // [N] bed centroid as an FP32 pair hi + lo

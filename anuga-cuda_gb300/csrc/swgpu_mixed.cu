@@ -278,7 +278,8 @@ __device__ __forceinline__ void fence_proxy_async() {
 template <int TILE>
 struct __align__(128) FluxTile {
     float2 ws[TILE];  // stage pair
-    float hf[TILE], radius[TILE], inv_area[TILE];
+    float hf[TILE];
+    float2 rad[TILE];  // radius, 1/area
     float4 es[3][TILE];  // edge state (depth, stage jump, momenta) per edge
     float2 nrm[3][TILE];  // unit normals
     float len[3][TILE];
@@ -295,8 +296,7 @@ __device__ __forceinline__ void flux_tile_issue_static(const DevMixed &X, FluxTi
     const int SP = X.S;
     const unsigned bytes = (unsigned)span * 4u;
     mbar_arrive_expect_tx(bar, 29u * bytes);  // the whole tile: 14 static + 15 dynamic planes
-    bulk_load(T.radius, X.radius + k0, bytes, bar);
-    bulk_load(T.inv_area, X.inv_area + k0, bytes, bar);
+    bulk_load(T.rad, X.rad + k0, 2u * bytes, bar);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         bulk_load(T.nrm[i], X.nrm + i * SP + k0, 2u * bytes, bar);
@@ -339,7 +339,7 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
     const float eps = P.f_eps;
     const float2 wsk = T.ws[tid];
     const float wk = wsk.x, lk = wsk.y;
-    const float rk = T.radius[tid];
+    const float rk = T.rad[tid].x;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;  // flux sums
     float gx = 0.f, gy = 0.f;            // Green sum of edge stage jumps
 #pragma unroll
@@ -361,11 +361,11 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
             if ((unsigned)ln < (unsigned)cnt) {
                 en = T.es[m][ln];
                 wsn = T.ws[ln];
-                rn = T.radius[ln];
+                rn = T.rad[ln].x;
             } else {
                 en = ro(X.es + m * SP + n);
                 wsn = ro(X.ws + n);
-                rn = ro(X.radius + n);
+                rn = ro(X.rad + n).x;
             }
             wn = wsn.x;
             lnn = wsn.y;
@@ -393,9 +393,8 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
         if (ms > eps) t = ominf(t, __fdividef(fminf(rk, rn), ms));
     }
     const float ghc = P.f_g * T.hf[tid];
-    const float inv_area = T.inv_area[tid];
-    X.ew[k] = a0 * inv_area;
-    X.euh[k] = (a1 - ghc * gx) * inv_area;
+    const float inv_area = T.rad[tid].y;
+    X.ewu[k] = make_float2(a0 * inv_area, (a1 - ghc * gx) * inv_area);
     X.evh[k] = (a2 - ghc * gy) * inv_area;
     return t;
 }
@@ -570,7 +569,8 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
     const float hf0 = ro(X.hf + kk);  // FP32 copies of the pre-update state
     const float2 vel0 = ro(X.vel + kk);
     const float uv0 = vel0.x, vv0 = vel0.y;
-    const float ew = ro(X.ew + kk), euh = ro(X.euh + kk), evh = ro(X.evh + kk);
+    const float2 ewu = ro(X.ewu + kk);
+    const float ew = ewu.x, euh = ewu.y, evh = ro(X.evh + kk);
     if (halted) return;
     const float dtf = (float)clk.dt;
     int bad = 0, nonfinite = 0;
@@ -1211,8 +1211,9 @@ int build_mixed_geometry(Handle *h) {
         return SWGPU_ECUDA;
     // FP32 planes use the padded stride sp (see DevMixed::S)
     std::vector<float2> nrm(3 * sp), gc(3 * sp);
-    std::vector<float> len(3 * sp), inv_area(n1), radius(n1),
-        dzv(3 * sp), dze(3 * sp), fric(n1), zmoff(n1), zhi(n1), zlo(n1);
+    std::vector<float2> rad(n1);
+    std::vector<float> len(3 * sp), dzv(3 * sp), dze(3 * sp), fric(n1), zmoff(n1), zhi(n1),
+        zlo(n1);
     std::vector<uint8_t> kind(n1);
     const std::vector<double> &V = h->h_vxy, &C = h->h_cxy;
     for (int k = 0; k < N; k++) {
@@ -1223,8 +1224,7 @@ int build_mixed_geometry(Handle *h) {
             dzv[i * sp + k] = (float)(zv[i * n1 + k] - zc[k]);
             dze[i * sp + k] = (float)(ze[i * n1 + k] - zc[k]);
         }
-        inv_area[k] = (float)(1.0 / h->h_areas[k]);
-        radius[k] = (float)h->h_radii[k];
+        rad[k] = make_float2((float)h->h_radii[k], (float)(1.0 / h->h_areas[k]));
         fric[k] = (float)fr[k];
         zmoff[k] = (float)((zv[k] + zv[n1 + k] + zv[2 * n1 + k]) / 3.0 - zc[k]);
         zhi[k] = (float)zc[k];
@@ -1274,8 +1274,7 @@ int build_mixed_geometry(Handle *h) {
     };
     put(X.nrm, nrm.data(), 3 * sp * 8);
     put(X.len, len.data(), 3 * sp * 4);
-    put(X.inv_area, inv_area.data(), n1 * 4);
-    put(X.radius, radius.data(), n1 * 4);
+    put(X.rad, rad.data(), n1 * 8);
     put(X.gc, gc.data(), 3 * sp * 8);
     put(X.dzv, dzv.data(), 3 * sp * 4);
     put(X.dze, dze.data(), 3 * sp * 4);

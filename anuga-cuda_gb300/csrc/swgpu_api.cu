@@ -531,10 +531,7 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         TRY(dalloc(h, &X.gc, s3));
         TRY(dalloc(h, &X.dzv, s3));
         TRY(dalloc(h, &X.dze, s3));
-        TRY(dalloc(h, &X.fric, s1));
-        TRY(dalloc(h, &X.zmoff, s1));
-        TRY(dalloc(h, &X.zhi, s1));
-        TRY(dalloc(h, &X.zlo, s1));
+        TRY(dalloc(h, &X.ust, s1));
         TRY(dalloc(h, &X.kind, s1));
         TRY(dalloc(h, &X.nbrp, s3));
         TRY(dalloc(h, &X.surrp, s3));

@@ -103,9 +103,9 @@ struct DevMixed {
     float2 *gc;                    // [3][S] vertex-jump coefficients of vertex i (dq1, dq2)
     float *dzv;                    // [3][S] bed vertex minus bed centroid
     float *dze;                    // [3][S] bed edge minus bed centroid
-    float *fric;                   // [N] Manning n
-    float *zmoff;                  // [N] mean(bed vertex) minus bed centroid
-    float *zhi, *zlo;              // [N] bed centroid as an FP32 pair hi + lo
+    float4 *ust;                   // [S] the update's static data: x Manning n, y mean(bed
+                                   // vertex) minus bed centroid, z/w bed centroid as an
+                                   // FP32 pair hi + lo
     int *nbrp;                     // [3][S] DevMesh::nbr in padded planes (TMA-staged)
     int *surrp;                    // [3][S] DevMesh::surr in padded planes (TMA-staged)
     uint8_t *kind;                 // [S] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat;

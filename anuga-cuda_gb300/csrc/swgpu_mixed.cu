@@ -549,9 +549,8 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = k < M.N;
     // static per-triangle data before the previous kernel has finished
-    const float eta = in ? ro(X.fric + k) : 0.0f;
-    const float zmoff = in ? ro(X.zmoff + k) : 0.0f;
-    const float zhi = in ? ro(X.zhi + k) : 0.0f, zlo = in ? ro(X.zlo + k) : 0.0f;
+    const float4 us = in ? ro(X.ust + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float eta = us.x, zmoff = us.y, zhi = us.z, zlo = us.w;
     pdl_wait();
     // every load first, the control block's with them (this thread is the
     // only writer of element k)
@@ -1036,7 +1035,8 @@ __global__ void __launch_bounds__(kBlock) prepare_mixed(DevMesh M, DevState S, D
     double uh = S.uh[k], vh = S.vh[k];
     float hf, wf, wl, uv, vv;
     int nonfinite = 0;
-    finish_state(P, h, uh, vh, X.zhi[k], X.zlo[k], hf, wf, wl, uv, vv, nonfinite);
+    const float4 us = X.ust[k];
+    finish_state(P, h, uh, vh, us.z, us.w, hf, wf, wl, uv, vv, nonfinite);
     X.hd[k] = h;
     S.uh[k] = uh;
     S.vh[k] = vh;
@@ -1212,8 +1212,8 @@ int build_mixed_geometry(Handle *h) {
     // FP32 planes use the padded stride sp (see DevMixed::S)
     std::vector<float2> nrm(3 * sp), gc(3 * sp);
     std::vector<float2> rad(n1);
-    std::vector<float> len(3 * sp), dzv(3 * sp), dze(3 * sp), fric(n1), zmoff(n1), zhi(n1),
-        zlo(n1);
+    std::vector<float> len(3 * sp), dzv(3 * sp), dze(3 * sp);
+    std::vector<float4> ust(n1);
     std::vector<uint8_t> kind(n1);
     const std::vector<double> &V = h->h_vxy, &C = h->h_cxy;
     for (int k = 0; k < N; k++) {
@@ -1225,10 +1225,12 @@ int build_mixed_geometry(Handle *h) {
             dze[i * sp + k] = (float)(ze[i * n1 + k] - zc[k]);
         }
         rad[k] = make_float2((float)h->h_radii[k], (float)(1.0 / h->h_areas[k]));
-        fric[k] = (float)fr[k];
-        zmoff[k] = (float)((zv[k] + zv[n1 + k] + zv[2 * n1 + k]) / 3.0 - zc[k]);
-        zhi[k] = (float)zc[k];
-        zlo[k] = (float)(zc[k] - (double)zhi[k]);
+        {
+            const float zhi = (float)zc[k];
+            ust[k] = make_float4((float)fr[k],
+                                 (float)((zv[k] + zv[n1 + k] + zv[2 * n1 + k]) / 3.0 - zc[k]), zhi,
+                                 (float)(zc[k] - (double)zhi));
+        }
         const double x = C[k], y = C[n1 + k];
         double dxv[3], dyv[3];
         for (int i = 0; i < 3; i++) {
@@ -1278,10 +1280,7 @@ int build_mixed_geometry(Handle *h) {
     put(X.gc, gc.data(), 3 * sp * 8);
     put(X.dzv, dzv.data(), 3 * sp * 4);
     put(X.dze, dze.data(), 3 * sp * 4);
-    put(X.fric, fric.data(), n1 * 4);
-    put(X.zmoff, zmoff.data(), n1 * 4);
-    put(X.zhi, zhi.data(), n1 * 4);
-    put(X.zlo, zlo.data(), n1 * 4);
+    put(X.ust, ust.data(), n1 * 16);
     put(X.kind, kind.data(), n1);
     return e == cudaSuccess ? SWGPU_OK : SWGPU_ECUDA;
 }

@@ -53,7 +53,7 @@ MIXED_BYTES = {"flux": 128, "update": 104, "distribute": 114}
 # DRAM bytes (read + write) per launch from one ncu capture of the 1,000,000-
 # triangle case (500x500 cells), scaled by 4 to the 4,000,000-triangle mesh;
 # traffic grows in proportion to the triangles a launch processes
-NCU_TRAFFIC_1M = {"flux": 121.99e6, "update": 65.89e6, "distribute": 105.00e6}
+NCU_TRAFFIC_1M = {"flux": 122.54e6, "update": 66.80e6, "distribute": 108.37e6}
 FP64_BYTES = {"flux": 296, "update": 120, "distribute": 253}
 MODEL_BYTES = {"mixed": 368, "fp64": 568}   # whole-step byte model
 ACC_STEPS = 1000                             # steps of the mixed-vs-FP64 accuracy check

@@ -526,17 +526,14 @@ static int create_impl(const swgpu_mesh *mesh, const swgpu_params *params, int p
         TRY(dalloc(h, &X.ewu, s1));
         TRY(dalloc(h, &X.evh, s1));
         TRY(dalloc(h, &X.nrm, s3));
-        TRY(dalloc(h, &X.len, s3));
+        TRY(dalloc(h, &X.lnb, s3));
         TRY(dalloc(h, &X.rad, s1));
         TRY(dalloc(h, &X.gc, s3));
         TRY(dalloc(h, &X.dzv, s3));
         TRY(dalloc(h, &X.dze, s3));
         TRY(dalloc(h, &X.ust, s1));
         TRY(dalloc(h, &X.kind, s1));
-        TRY(dalloc(h, &X.nbrp, s3));
         TRY(dalloc(h, &X.surrp, s3));
-        CK(cudaMemcpy2DAsync(X.nbrp, X.S * sizeof(int), M.nbr, (size_t)N * sizeof(int),
-                             (size_t)N * sizeof(int), 3, cudaMemcpyDeviceToDevice, h->stream));
         CK(cudaMemcpy2DAsync(X.surrp, X.S * sizeof(int), M.surr, (size_t)N * sizeof(int),
                              (size_t)N * sizeof(int), 3, cudaMemcpyDeviceToDevice, h->stream));
         // FP64 vertex planes are kept for downloads (stage = depth + bed)

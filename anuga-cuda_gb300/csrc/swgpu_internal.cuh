@@ -98,7 +98,8 @@ struct DevMixed {
     float2 *ewu;                   // [S] explicit_update of depth (x) and x momentum (y)
     float *evh;                    // [S] explicit_update of y momentum
     float2 *nrm;                   // [3][S] unit normals (x, y)
-    float *len;                    // [3][S] edge lengths
+    int2 *lnb;                     // [3][S] per edge: x the length (float bits), y the packed
+                                   // neighbour of DevMesh::nbr
     float2 *rad;                   // [S] x radius, y 1/area
     float2 *gc;                    // [3][S] vertex-jump coefficients of vertex i (dq1, dq2)
     float *dzv;                    // [3][S] bed vertex minus bed centroid
@@ -106,7 +107,7 @@ struct DevMixed {
     float4 *ust;                   // [S] the update's static data: x Manning n, y mean(bed
                                    // vertex) minus bed centroid, z/w bed centroid as an
                                    // FP32 pair hi + lo
-    int *nbrp;                     // [3][S] DevMesh::nbr in padded planes (TMA-staged)
+
     int *surrp;                    // [3][S] DevMesh::surr in padded planes (TMA-staged)
     uint8_t *kind;                 // [S] 0 aux triangle, 1 one neighbour (slot<<2), 2 flat;
                                    // | 16: the triangle has a boundary edge

@@ -29,6 +29,7 @@
 // Bytes per triangle-step (own arrays; neighbour gathers hit L1/L2):
 //   distribute ~114, flux ~128, update ~104.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
@@ -282,8 +283,7 @@ struct __align__(128) FluxTile {
     float2 rad[TILE];  // radius, 1/area
     float4 es[3][TILE];  // edge state (depth, stage jump, momenta) per edge
     float2 nrm[3][TILE];  // unit normals
-    float len[3][TILE];
-    int nbr[3][TILE];  // packed neighbours (read where used: no registers held)
+    int2 lnb[3][TILE];  // edge length (float bits), packed neighbour (read where used)
 };
 
 // The bulk copies of a flux tile starting at triangle k0 (span elements of
@@ -300,8 +300,7 @@ __device__ __forceinline__ void flux_tile_issue_static(const DevMixed &X, FluxTi
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         bulk_load(T.nrm[i], X.nrm + i * SP + k0, 2u * bytes, bar);
-        bulk_load(T.len[i], X.len + i * SP + k0, bytes, bar);
-        bulk_load(T.nbr[i], X.nbrp + i * SP + k0, bytes, bar);
+        bulk_load(T.lnb[i], X.lnb + i * SP + k0, 2u * bytes, bar);
     }
 }
 template <int TILE>
@@ -345,11 +344,12 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const float2 nr = T.nrm[i][tid];
-        const float n1 = nr.x, n2 = nr.y, L = T.len[i][tid];
+        const int2 lq = T.lnb[i][tid];
+        const float n1 = nr.x, n2 = nr.y, L = __int_as_float(lq.x);
         const float4 el = T.es[i][tid];
         const float hl = el.x, dwl = el.y, uhl = el.z, vhl = el.w;
         float hr, uhr, vhr, jump, rn = 3.0e38f;
-        const int pki = T.nbr[i][tid];
+        const int pki = lq.y;
         if (pki >= 0) {
             // the neighbour's stored edge state: the very numbers it uses
             // itself, so both sides see the same two states
@@ -365,7 +365,7 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
             } else {
                 en = ro(X.es + m * SP + n);
                 wsn = ro(X.ws + n);
-                rn = ro(X.rad + n).x;
+                rn = ro(reinterpret_cast<const float *>(X.rad + n));  // the radius only
             }
             wn = wsn.x;
             lnn = wsn.y;
@@ -1212,7 +1212,8 @@ int build_mixed_geometry(Handle *h) {
     // FP32 planes use the padded stride sp (see DevMixed::S)
     std::vector<float2> nrm(3 * sp), gc(3 * sp);
     std::vector<float2> rad(n1);
-    std::vector<float> len(3 * sp), dzv(3 * sp), dze(3 * sp);
+    std::vector<int2> lnb(3 * sp, make_int2(0, 0));
+    std::vector<float> dzv(3 * sp), dze(3 * sp);
     std::vector<float4> ust(n1);
     std::vector<uint8_t> kind(n1);
     const std::vector<double> &V = h->h_vxy, &C = h->h_cxy;
@@ -1220,7 +1221,10 @@ int build_mixed_geometry(Handle *h) {
         for (int i = 0; i < 3; i++) {
             nrm[i * sp + k] = make_float2((float)h->h_normals[(2 * i) * n1 + k],
                                           (float)h->h_normals[(2 * i + 1) * n1 + k]);
-            len[i * sp + k] = (float)h->h_len[i * n1 + k];
+            const float L = (float)h->h_len[i * n1 + k];
+            int lbits;
+            std::memcpy(&lbits, &L, sizeof lbits);
+            lnb[i * sp + k] = make_int2(lbits, h->h_nbr[i * n1 + k]);
             dzv[i * sp + k] = (float)(zv[i * n1 + k] - zc[k]);
             dze[i * sp + k] = (float)(ze[i * n1 + k] - zc[k]);
         }
@@ -1275,7 +1279,7 @@ int build_mixed_geometry(Handle *h) {
         if (e == cudaSuccess) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
     };
     put(X.nrm, nrm.data(), 3 * sp * 8);
-    put(X.len, len.data(), 3 * sp * 4);
+    put(X.lnb, lnb.data(), 3 * sp * 8);
     put(X.rad, rad.data(), n1 * 8);
     put(X.gc, gc.data(), 3 * sp * 8);
     put(X.dzv, dzv.data(), 3 * sp * 4);

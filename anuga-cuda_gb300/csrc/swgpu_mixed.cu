@@ -675,19 +675,21 @@ __device__ __forceinline__ void limit_f(float (&d)[3], float qmin, float qmax, f
 }
 
 // jumps on the auxiliary triangle: d_i = c_i0*dq1 + c_i1*dq2, limited
-__device__ __forceinline__ void aux_jumps_f(float dq0, float dq1, float dq2, const float (&c)[6],
+template <typename C>
+__device__ __forceinline__ void aux_jumps_f(float dq0, float dq1, float dq2, const C &c,
                                             float beta, float (&d)[3]) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) d[i] = c[2 * i] * dq1 + c[2 * i + 1] * dq2;
+    for (int i = 0; i < 3; i++) d[i] = c(2 * i) * dq1 + c(2 * i + 1) * dq2;
     float qmin, qmax;
     qminmax_f(dq0, dq1, dq2, qmin, qmax);
     limit_f(d, qmin, qmax, beta);
 }
 
-__device__ __forceinline__ void one_jumps_f(float dq1, const float (&c)[6], float beta,
+template <typename C>
+__device__ __forceinline__ void one_jumps_f(float dq1, const C &c, float beta,
                                             float (&d)[3]) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) d[i] = c[2 * i] * dq1;
+    for (int i = 0; i < 3; i++) d[i] = c(2 * i) * dq1;
     const float qmin = dq1 >= 0.0f ? 0.0f : dq1, qmax = dq1 >= 0.0f ? dq1 : 0.0f;
     limit_f(d, qmin, qmax, beta);
 }
@@ -776,10 +778,10 @@ __device__ __forceinline__ V tile_or_global(const V *tile, const V *plane, int n
 template <int BS>
 __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, DevState S, DevMixed X,
                                                            DevParams P, const BcTag *tags,
-                                                           Ctrl *ctrl, int flags, Stage stg) {
+                                                           Ctrl *ctrls, int flags, Stage stg) {
     const bool fused = flags & kFused;
     pdl_launch_dependents();
-    ctrl = block_ctrl(ctrl, M);
+    Ctrl *ctrl = block_ctrl(ctrls, M);
     __shared__ DistTile<BS> T;
     __shared__ __align__(8) unsigned long long bar;
     const int N = M.N, SP = X.S;
@@ -815,10 +817,8 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
     // the scenario stops after this distribute)
     const bool halted = fused && ctrl_halted(ctrl) == 1;
     int order;
-    double time;
     if (fused) {
         order = (int)ctrl->clk_order;
-        time = ctrl->clk_t0 + ctrl->clk_dt * (stg.kind == kStageMid ? stg.tfrac : 1.0);
         const bool first = blockIdx.x == 0 ||
                            (M.blk_scen && M.blk_scen[(kb - 1) >> 8] != M.blk_scen[kb >> 8]);
         if (first && tid == 0 && !halted) {
@@ -827,7 +827,6 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
         }
     } else {
         order = (int)ctrl->order;
-        time = ctrl->time;
     }
     const bool arrived = mbar_wait_bounded(&bar, ctrl);
     if (halted) return;
@@ -841,9 +840,6 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
         const bool vel = P.extrapolate_velocity_second_order == 1;
         const float hk = omaxf(hc, mah);
         const float uk = qu * hk, vk = qv * hk;  // centroid momentum
-        float dzv[3];
-#pragma unroll
-        for (int i = 0; i < 3; i++) dzv[i] = T.dzv[i][tid];
         float dw[3] = {0.f, 0.f, 0.f};  // vertex stage jumps
         float ou[3], ov[3];             // vertex momentum (or velocity)
         if (order != 1) {
@@ -851,13 +847,11 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
             float du[3] = {0.f, 0.f, 0.f}, dv[3] = {0.f, 0.f, 0.f};
             bool keep = false;  // dry neighbourhood: previous vertex values stay
             if ((kind & 3) != 2) {
-                float c[6];
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    const float2 g = T.gc[i][tid];
-                    c[2 * i] = g.x;
-                    c[2 * i + 1] = g.y;
-                }
+                // reconstruction coefficients, read from the tile at each use
+                const auto c = [&](int j) {
+                    const float2 g = T.gc[j >> 1][tid];
+                    return (j & 1) ? g.y : g.x;
+                };
                 if ((kind & 3) == 0) {
                     const int k0 = T.sur[0][tid], k1 = T.sur[1][tid], k2 = T.sur[2][tid];
                     const float h0 = tile_or_global(T.hf, X.hf, k0, kb, cnt);
@@ -942,7 +936,7 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
                 // velocity -> momentum with the vertex depth hc + dw - dzv
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    const float d = omaxf((hc + dw[i]) - dzv[i], 0.0f);
+                    const float d = omaxf((hc + dw[i]) - T.dzv[i][tid], 0.0f);
                     ou[i] *= d;
                     ov[i] *= d;
                 }
@@ -958,6 +952,11 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
         // depth h_i = hc + (dw_i - dzv_i); the blend keeps the form
         // dw_i <- alpha*(dw_i - dzv_i) + dzv_i
         {
+            // the bed offsets at the vertices, read from the tile here rather
+            // than held in registers through the reconstruction
+            float dzv[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) dzv[i] = T.dzv[i][tid];
             float rel[3];  // h_i - hc
 #pragma unroll
             for (int i = 0; i < 3; i++) rel[i] = dw[i] - dzv[i];
@@ -1002,12 +1001,20 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
                                            0.5f * (dw[a] + dw[b]), 0.5f * (ou[a] + ou[b]),
                                            0.5f * (ov[a] + ov[b]));
         }
-        if ((flags & kWriteBoundary) && (kind & 16))  // a boundary edge
+        if ((flags & kWriteBoundary) && (kind & 16)) {  // a boundary edge
+            // the control block and the boundary's time are looked up again
+            // here rather than held in registers through the reconstruction
+            // (neither changes during the kernel)
+            const Ctrl *c = block_ctrl(ctrls, M);
+            const double time =
+                fused ? c->clk_t0 + c->clk_dt * (stg.kind == kStageMid ? stg.tfrac : 1.0)
+                      : c->time;
             bad_bc = boundary_edges_mixed(k, N, SP, time, P.g, M.nbr, M.btag, tags, S.ze,
                                           X.es, X.nrm, S.wb, S.uhb, S.vhb,
                                           S.zb, X.hbf, X.wjb, X.uhbf, X.vhbf);
+        }
     }
-    if (bad_bc) set_status(ctrl, SWGPU_EBOUNDARY);
+    if (bad_bc) set_status(block_ctrl(ctrls, M), SWGPU_EBOUNDARY);
 }
 
 // update_timestep (the step's clock) of each running scenario, evaluated

@@ -50,10 +50,9 @@ UNIT = "triangle-steps/s"
 # algorithmic bytes per triangle-step of each kernel (own arrays, neighbour
 # gathers counted as cache hits)
 MIXED_BYTES = {"flux": 128, "update": 104, "distribute": 114}
-# DRAM bytes (read + write) per launch from one ncu capture of the 1,000,000-
-# triangle case (500x500 cells), scaled by 4 to the 4,000,000-triangle mesh;
-# traffic grows in proportion to the triangles a launch processes
-NCU_TRAFFIC_1M = {"flux": 122.54e6, "update": 66.80e6, "distribute": 108.37e6}
+# DRAM bytes (read + write) per launch from one ncu capture of the 4,000,000-
+# triangle mesh (1000x1000 cells); scaled by the triangles for other meshes
+NCU_TRAFFIC_4M = {"flux": 509.35e6, "update": 377.39e6, "distribute": 520.23e6}
 FP64_BYTES = {"flux": 296, "update": 120, "distribute": 253}
 MODEL_BYTES = {"mixed": 368, "fp64": 568}   # whole-step byte model
 ACC_STEPS = 1000                             # steps of the mixed-vs-FP64 accuracy check
@@ -463,9 +462,10 @@ def main():
         "kernel_ms": dict(zip(names, kms)),
         "roofline": {"bound": "hbm", "kernel": names[dom] + "_mixed", "achieved": achieved,
                      "peak": peak_gbs, "unit": "GB/s", "frac": achieved / peak_gbs,
-                     "traffic": NCU_TRAFFIC_1M[names[dom]] * N / 1.0e6,
+                     "traffic": NCU_TRAFFIC_4M[names[dom]] * N / 4.0e6,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                       "1,000,000-triangle capture scaled to this mesh",
+                                       "capture of the 4,000,000-triangle mesh"
+                                       + ("" if N == 4000000 else ", scaled to this mesh"),
                      "peak_source": "measured" if peaks else "fallback",
                      "step_model_frac": MODEL_BYTES["mixed"] * N / (mixed_ms / K / 1000.0) / 1e9
                      / peak_gbs},

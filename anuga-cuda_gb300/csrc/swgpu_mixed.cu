@@ -275,7 +275,8 @@ __device__ __forceinline__ void fence_proxy_async() {
 }
 
 // The flux kernel's own data for one tile of TILE triangles (= threads per
-// block: 64, 128 or 256), filled by 29 bulk copies.
+// block: 64, 128 or 256), filled by 12 bulk copies (7 static, 5 of state)
+// that together move 29 four-byte values per triangle.
 template <int TILE>
 struct __align__(128) FluxTile {
     float2 ws[TILE];  // stage pair
@@ -316,7 +317,7 @@ __device__ __forceinline__ void flux_tile_issue_dynamic(const DevMixed &X, FluxT
         bulk_load(T.es[i], X.es + i * SP + k0, 4u * bytes, bar);
     }
 }
-// The 29 bulk copies of a flux tile starting at triangle k0 (span elements
+// All 12 bulk copies of a flux tile starting at triangle k0 (span elements
 // of each padded plane), completing on bar.  Called by one thread.
 template <int TILE>
 __device__ __forceinline__ void flux_tile_issue(const DevMixed &X, FluxTile<TILE> &T, int k0,
@@ -744,7 +745,7 @@ __device__ __noinline__ int boundary_edges_mixed(int k, int N, int SP, double ti
 }
 
 // The distribute kernel's own data for one tile of BS triangles, filled by
-// 21 bulk copies.
+// 16 bulk copies (20 four-byte values and one byte per triangle).
 template <int BS>
 struct __align__(128) DistTile {
     float2 ws[BS];   // stage pair

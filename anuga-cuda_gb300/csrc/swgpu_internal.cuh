@@ -157,9 +157,10 @@ struct __align__(16) Ctrl {
     int stop_reason;
     int status;                     // first device-side failure (swgpu_status)
     unsigned int done_update, done_distribute, done_flux;
-    int clk_small_error;            // the step's update_timestep, evaluated once by
-    double clk_dt, clk_ftmin;       // the last block of the flux kernel and read
-    long long clk_order, clk_smallsteps;  // by the update kernel
+    int clk_small_error;            // the step's update_timestep, evaluated once
+    double clk_dt, clk_ftmin;       // after the flux grid (FP64: its last block;
+    long long clk_order, clk_smallsteps;  // mixed: step_clock_mixed) and read by
+                                          // the update and distribute kernels
     double clk_t0;                  // model time when that clock was evaluated
     double step_t0;                 // time at the start of a Runge-Kutta step
     unsigned int blocks_flux;       // blocks of this scenario in one flux launch

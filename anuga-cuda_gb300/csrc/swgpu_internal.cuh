@@ -85,8 +85,9 @@ struct DevState {
 // centroid bed, so that hydrostatic pressure and bed-slope terms never
 // subtract two large FP32 numbers.
 struct DevMixed {
-    int S;                         // stride of the [3]/[6] planes: N rounded up to 64, so
-                                   // that every plane and 16-triangle tile is 64-B aligned
+    int S;                         // stride of the padded planes: N rounded up to 64, so
+                                   // that every plane and every tile of 64-512 triangles
+                                   // starts 256-B aligned
     double *hd;                    // [N] FP64 depth (conserved)
     float2 *ws;                    // [S] centroid stage as an FP32 pair, x hi + y lo
     float *hf;                     // [S] centroid depth

@@ -87,7 +87,7 @@ struct DevState {
 struct DevMixed {
     int S;                         // stride of the padded planes: N rounded up to 64, so
                                    // that every plane and every tile of 64-512 triangles
-                                   // starts 256-B aligned
+                                   // starts on a multiple of 64 elements (TMA-aligned)
     double *hd;                    // [N] FP64 depth (conserved)
     float2 *ws;                    // [S] centroid stage as an FP32 pair, x hi + y lo
     float *hf;                     // [S] centroid depth

@@ -1,7 +1,7 @@
 """NumPy FP64 restatement of the surrogate MLP (forward, loss, backward).
 
-TEST INFRASTRUCTURE ONLY: the checker of anuga-cuda_gb300/csrc/swgpu_mlp.cu,
-used by tests; never imported by the package.
+TEST INFRASTRUCTURE ONLY: the oracle that tests compare
+anuga-cuda_gb300/csrc/swgpu_mlp.cu against; never imported by the package.
 
 The network and its rounding points follow the CUDA kernels: features in
 FP32, rounded to BF16; weights rounded to BF16; each layer's sum in FP64

@@ -131,7 +131,7 @@ __device__ __forceinline__ StepClock device_update_timestep(const Ctrl *c, const
     return s;
 }
 
-// The step's clock as published by the flux kernel's last block.
+// The step's clock as published by publish_step_clock.
 __device__ __forceinline__ StepClock published_step_clock(const Ctrl *c) {
     StepClock s;
     s.dt = c->clk_dt;
@@ -163,8 +163,9 @@ __device__ __forceinline__ bool last_block_done(unsigned int *counter, unsigned 
     return false;
 }
 
-// Last block of the flux kernel (all atomicMins of the step are done):
-// evaluate update_timestep once and publish it for the update kernel.
+// Once all atomicMins of the step are done (FP64: the flux kernel's last
+// block; mixed: step_clock_mixed, after the flux grid): evaluate
+// update_timestep once and publish it for the update kernel.
 __device__ __forceinline__ void publish_step_clock(Ctrl *c, const DevParams &P) {
     const StepClock s = device_update_timestep(c, P);
     c->clk_dt = s.dt;
@@ -234,8 +235,9 @@ __device__ __forceinline__ int ctrl_halted(const Ctrl *c) {
     return *(volatile const int *)&c->halt;
 }
 
-// Last block of the update kernel: commit the new time and counters and
-// decide whether the loop stops after this step's distribute.
+// Commit the new time and counters and decide whether the loop stops after
+// this step's distribute (FP64: the update kernel's last block; mixed: the
+// first block of the scenario in the distribute, through commit_stage).
 __device__ __forceinline__ void commit_step(Ctrl *c, const StepClock &s, const DevParams &P) {
     c->rec_max = omax(s.dt, c->rec_max);
     c->rec_min = omin(s.dt, c->rec_min);
@@ -265,7 +267,8 @@ __device__ __forceinline__ void commit_step(Ctrl *c, const StepClock &s, const D
     if (reason != kStopNone) c->halt_pending = reason;
 }
 
-// Last block of the update kernel in a fused step, per stage kind.  The
+// The stage commit of a fused step, per stage kind (FP64: the update
+// kernel's last block; mixed: the distribute's first block).  The
 // first Runge-Kutta stage records the step's clock (the distribute that
 // follows reads the order) and moves time to t0 + dt, the middle RK3 stage
 // to t0 + dt/2; the last stage commits the step from t0 as an Euler step
@@ -296,7 +299,7 @@ __device__ __forceinline__ void track_depth(const DevState &S, int k, double h, 
 }
 
 // Model time at the end of the step a stage belongs to, read by every
-// block before the update's last block commits it.
+// block before the stage is committed.
 __device__ __forceinline__ double step_end_time(const Ctrl *c, const StepClock &s,
                                                 const Stage &stg) {
     return (stg.kind == kStageLast ? c->step_t0 : c->time) + s.dt;

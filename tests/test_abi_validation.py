@@ -69,6 +69,21 @@ def test_bad_precision_and_sizes_refused(arrays):
     st, msg = _create(bad)
     assert st == EINVAL and "bad sizes" in msg
     assert _create(dict(arrays, Nb=3 * arrays["N"] + 1))[0] == EINVAL
+    assert _create(dict(arrays, Nb=-1))[0] == EINVAL
+    # the largest mesh a handle takes: 2^29 - 1 triangles (int32 packed neighbours)
+    st, msg = _create(dict(arrays, N=1 << 29))
+    assert st == EINVAL and "bad sizes" in msg
+
+
+def test_noalloc_volume_refuses_before_touching_memory(swgpu_built):
+    # the pointers are never dereferenced: sizes and nulls are checked first
+    fake = C.c_void_p(4096)
+    L = lib()
+    assert L.swgpu_water_volume_noalloc(fake, fake, fake, 4_194_305, fake, None) == EINVAL
+    assert b"4194304" in L.swgpu_last_error(None)
+    assert L.swgpu_water_volume_noalloc(fake, fake, fake, 0, fake, None) == EINVAL
+    assert L.swgpu_water_volume_noalloc(None, fake, fake, 4, fake, None) == EINVAL
+    assert b"null" in L.swgpu_last_error(None)
 
 
 def _wrong_neighbour_edge(a):

@@ -204,19 +204,30 @@ static int issue_fused_step(Handle *h) {
     return check_launch(h, "evolve step");
 }
 
-static int build_graph(Handle *h) {
-    if (h->graph) return SWGPU_OK;
+// Captures `steps` fused steps into *exec (left as is when already built).
+static int capture_steps(Handle *h, int steps, cudaGraphExec_t *exec) {
+    if (*exec) return SWGPU_OK;
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < h->steps_per_graph; s++) issue_step(h);
+    for (int s = 0; s < steps; s++) issue_step(h);
     CK(cudaStreamEndCapture(h->stream, &g));
-    cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaError_t e = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
-        h->graph = nullptr;
+        *exec = nullptr;
         return fail(h, SWGPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
     return SWGPU_OK;
+}
+
+static int build_graph(Handle *h) { return capture_steps(h, h->steps_per_graph, &h->graph); }
+
+// Drops the captured graphs after a change of what a step issues (launch
+// shape, extent, stages, tracking); they are recaptured on the next run.
+// The stream must be idle.
+static void drop_graphs(Handle *h) {
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
 }
 
 // distribute as the stand-alone method: protect + velocities, then the
@@ -688,7 +699,7 @@ int swgpu_destroy(void *handle) {
     if (!handle) return SWGPU_OK;
     Handle *h = static_cast<Handle *>(handle);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    if (h->graph) cudaGraphExecDestroy(h->graph);
+    drop_graphs(h);
     for (void *p : h->allocs) cudaFree(p);
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
     if (h->h_summary) cudaFreeHost(h->h_summary);
@@ -772,9 +783,16 @@ int swgpu_get_quantity(void *handle, int q, double *centroid, double *vertex, do
     const int64_t N = h->M.N;
     DevState &S = h->S;
     int rc;
-    if (h->precision == SWGPU_MIXED && !h->mixed_from_stage && q <= SWGPU_YMOMENTUM) {
-        launch_vertices_from_mixed(h->M, h->S, h->X, h->stream);
-        if ((rc = check_launch(h, "mixed vertex values"))) return rc;
+    if (h->precision == SWGPU_MIXED && !h->mixed_from_stage) {
+        // the FP64 views of the mixed state: vertex and edge values when
+        // asked for, else the centroid stage alone (momentum is FP64 state)
+        if ((vertex || edge) && q <= SWGPU_YMOMENTUM) {
+            launch_vertices_from_mixed(h->M, h->S, h->X, h->stream);
+            if ((rc = check_launch(h, "mixed vertex values"))) return rc;
+        } else if (q == SWGPU_STAGE || q >= SWGPU_HEIGHT) {
+            launch_stage_from_mixed(h->M, h->S, h->X, h->stream);
+            if ((rc = check_launch(h, "mixed centroid stage"))) return rc;
+        }
     }
     // the 'tsunami' distribute stores its extrapolated edge values, which are
     // not the interpolation of the vertex values
@@ -984,10 +1002,9 @@ int swgpu_set_timestepping_method(void *handle, int method) {
     if (!h) return fail(h, SWGPU_EINVAL, "null handle");
     if (method != SWGPU_EULER && method != SWGPU_RK2 && method != SWGPU_RK3)
         return fail(h, SWGPU_EINVAL, "timestepping method %d (1 euler, 2 rk2, 3 rk3)", method);
-    if (method != h->timestepping_method && h->graph) {
+    if (method != h->timestepping_method) {
         CK(cudaStreamSynchronize(h->stream));
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;  // rebuilt with the new stages on the next run
+        drop_graphs(h);  // rebuilt with the new stages on the next run
     }
     h->timestepping_method = method;
     return SWGPU_OK;
@@ -996,6 +1013,8 @@ int swgpu_set_timestepping_method(void *handle, int method) {
 int swgpu_update_other_quantities(void *handle) {
     Handle *h = static_cast<Handle *>(handle);
     if (!h) return fail(h, SWGPU_EINVAL, "null handle");
+    if (h->precision == SWGPU_MIXED && !h->mixed_from_stage)
+        launch_stage_from_mixed(h->M, h->S, h->X, h->stream);
     launch_other_quantities(h->M, h->S, h->stream);
     int rc = check_launch(h, "update_other_quantities");
     if (rc) return rc;
@@ -1113,10 +1132,7 @@ int swgpu_set_launch_config(void *handle, const swgpu_launch_config *cfg) {
                     "distribute 128/256/512 (at most 256 for an ensemble), 1..64 steps per graph");
     int rc = sync_ctrl(h);
     if (rc) return rc;
-    if (h->graph) {
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;  // recaptured with the new shape on the next run
-    }
+    drop_graphs(h);  // recaptured with the new shape on the next run
     h->M.shape.flux = cfg->flux_block;
     h->M.shape.update = cfg->update_block;
     h->M.shape.distribute = cfg->distribute_block;
@@ -1147,10 +1163,7 @@ int swgpu_set_tracking(void *handle, int on, double threshold) {
         h->S.hmax = h->S.tarr = nullptr;  // the buffers stay for a later call
     }
     CK(cudaStreamSynchronize(h->stream));
-    if (h->graph) {
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;  // recaptured with the new tracking state and threshold
-    }
+    drop_graphs(h);  // recaptured with the new tracking state and threshold
     return SWGPU_OK;
 }
 
@@ -1238,8 +1251,7 @@ static int set_launch_extent(Handle *h, int n) {
     if (h->M.n_launch == n) return SWGPU_OK;
     if (h->graph) {
         CK(cudaStreamSynchronize(h->stream));
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
+        drop_graphs(h);
     }
     h->M.n_launch = n;
     return SWGPU_OK;
@@ -1357,6 +1369,14 @@ static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *
     int rc = prepare_run(h, max_steps);
     if (rc) return rc;
     if ((rc = build_graph(h))) return rc;
+    // with a step budget the device stops itself after max_steps steps; the
+    // host issues max_steps / steps-per-graph whole graphs and then the
+    // remaining steps' kernels one by one (no capture for a remainder that
+    // may differ between runs), so that no step is issued beyond the budget
+    const int spg = h->steps_per_graph;
+    const int64_t full_graphs = max_steps > 0 ? max_steps / spg : INT64_MAX;
+    const int tail = max_steps > 0 ? (int)(max_steps % spg) : 0;
+    const int64_t max_graphs = max_steps > 0 ? full_graphs + (tail ? 1 : 0) : INT64_MAX;
     // keep two graphs in flight: while graph i runs, the host waits on the
     // control-block copy that follows graph i-1
     cudaEvent_t ev[2], t0, t1;
@@ -1366,15 +1386,16 @@ static int run_graphs(Handle *h, int64_t max_steps, swgpu_state *state, double *
     CK(cudaEventCreate(&t1));
     CK(cudaEventRecord(t0, h->stream));
     int64_t launched = 0;
-    // with a step budget the device stops itself after max_steps steps, so
-    // exactly ceil(max_steps / steps-per-graph) graphs are launched
-    const int64_t max_graphs =
-        max_steps > 0 ? (max_steps + h->steps_per_graph - 1) / h->steps_per_graph : INT64_MAX;
     cudaError_t e = cudaSuccess;
     int inflight = 0, slot = 0;
     bool halted = false;
     while (!halted && launched < max_graphs) {
-        e = cudaGraphLaunch(h->graph, h->stream);
+        if (launched < full_graphs) {
+            e = cudaGraphLaunch(h->graph, h->stream);
+        } else {
+            for (int s = 0; s < tail; s++) issue_step(h);
+            e = cudaGetLastError();
+        }
         if (e != cudaSuccess) break;
         e = cudaMemcpyAsync(h->h_summary, h->d_summary, sizeof(RunSummary),
                             cudaMemcpyDeviceToHost, h->stream);

@@ -235,6 +235,12 @@ __device__ __forceinline__ int ctrl_halted(const Ctrl *c) {
     return *(volatile const int *)&c->halt;
 }
 
+// The halt flag read after griddepcontrol.wait, when no kernel still running
+// can change it: a plain load, served from L1 for all but the first warp of
+// each SM (a volatile load from every warp would queue on the one L2 line
+// that holds the control block).
+__device__ __forceinline__ int ctrl_halt_settled(const Ctrl *c) { return c->halt; }
+
 // Commit the new time and counters and decide whether the loop stops after
 // this step's distribute (FP64: the update kernel's last block; mixed: the
 // first block of the scenario in the distribute, through commit_stage).

@@ -37,7 +37,7 @@ struct Handle {
     double *d_scalar = nullptr;  // mass / misc
     double *h_scalar = nullptr;  // pinned
     std::vector<void *> allocs;
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;  // steps_per_graph fused steps
     bool resume_after_yield = false;
     bool vertices_stale = true;
     bool mixed_from_stage = true;  // mixed: FP64 stage upload not yet converted to depth

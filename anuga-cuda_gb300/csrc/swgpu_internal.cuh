@@ -260,6 +260,10 @@ void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X
 // FP64 stage / vertex / edge values from the mixed state, for downloads
 void launch_vertices_from_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                                 cudaStream_t st);
+// FP64 centroid stage only (w = h + z), for centroid downloads and the
+// derived quantities
+void launch_stage_from_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                             cudaStream_t st);
 void launch_mass_mixed(const DevMesh &M, const DevState &S, const DevMixed &X, double *out,
                        cudaStream_t st);
 void launch_mass_partials_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,

@@ -227,6 +227,21 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, u
                  "r"(bytes)
                  : "memory");
 }
+// Raises the bytes the current phase waits for, without arriving.
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// Arrives without adding bytes.
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+    unsigned long long state;
+    asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];"
+                 : "=l"(state)
+                 : "r"(smem_u32(bar))
+                 : "memory");
+    (void)state;
+}
 // Global -> shared bulk copy completing on the mbarrier.  dst, src 16-byte
 // aligned, bytes a multiple of 16 (planes are padded to 64 elements and
 // tiles start at multiples of 128 elements).
@@ -296,7 +311,7 @@ __device__ __forceinline__ void flux_tile_issue_static(const DevMixed &X, FluxTi
                                                        unsigned long long *bar) {
     const int SP = X.S;
     const unsigned bytes = (unsigned)span * 4u;
-    mbar_arrive_expect_tx(bar, 29u * bytes);  // the whole tile: 14 static + 15 dynamic planes
+    mbar_expect_tx(bar, 14u * bytes);  // 14 four-byte static values per triangle
     bulk_load(T.rad, X.rad + k0, 2u * bytes, bar);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -310,6 +325,7 @@ __device__ __forceinline__ void flux_tile_issue_dynamic(const DevMixed &X, FluxT
                                                         unsigned long long *bar) {
     const int SP = X.S;
     const unsigned bytes = (unsigned)span * 4u;
+    mbar_arrive_expect_tx(bar, 15u * bytes);  // 15 dynamic values; the tile's one arrival
     bulk_load(T.ws, X.ws + k0, 2u * bytes, bar);
     bulk_load(T.hf, X.hf + k0, bytes, bar);
 #pragma unroll
@@ -416,15 +432,30 @@ __global__ void __launch_bounds__(TILE, 1536 / TILE) flux_mixed(DevMesh M, DevMi
     const int k0 = blockIdx.x * TILE;
     const int cnt = min(TILE, N - k0);
     const int span = min(TILE, X.S - k0);  // tile length in the padded planes (x64)
-    if (tid == 0) mbar_init(&bar, 1);
+    // A scenario that has stopped stays stopped for the rest of the run (only
+    // the host clears the flag, between runs), so a flag already raised
+    // before the previous kernel has finished means a block with nothing to
+    // do and nothing to fetch.  Thread 0 reads it for the whole block.
+    __shared__ int stopped_early;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        stopped_early = (flags & kFused) ? ctrl_halted(ctrl) : 0;
+        // geometry and neighbour indices do not change between steps:
+        // fetched while the previous kernel may still run
+        if (!stopped_early) flux_tile_issue_static<TILE>(X, T, k0, span, &bar);
+    }
     __syncthreads();
-    // geometry and neighbour indices do not change between steps: fetched
-    // while the previous kernel may still run
-    if (tid == 0) flux_tile_issue_static<TILE>(X, T, k0, span, &bar);
     pdl_wait();
-    if (tid == 0) flux_tile_issue_dynamic<TILE>(X, T, k0, span, &bar);
-    // read while the copies fly; acted on once they have landed
-    const bool halted = (flags & kFused) && ctrl_halted(ctrl);
+    if (stopped_early) return;  // no copy was issued
+    // the flag as the previous kernels left it (no kernel of this step
+    // changes it before this grid completes): the same for every thread
+    const bool halted = (flags & kFused) && ctrl_halt_settled(ctrl);
+    if (tid == 0) {
+        if (halted)
+            mbar_arrive(&bar);  // the static copies only
+        else
+            flux_tile_issue_dynamic<TILE>(X, T, k0, span, &bar);
+    }
     // the running timestep minimum, read (by the thread that will reduce)
     // while the copies fly: the block's atomic is skipped when it cannot
     // lower it, without a read at the end
@@ -553,9 +584,11 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
     const float4 us = in ? ro(X.ust + k) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float eta = us.x, zmoff = us.y, zhi = us.z, zlo = us.w;
     pdl_wait();
+    // a stopped scenario's threads load nothing more (the flag is settled:
+    // only the step clock kernel and the distribute change it)
+    if ((flags & kFused) && ctrl_halt_settled(ctrl)) return;
     // every load first, the control block's with them (this thread is the
     // only writer of element k)
-    const bool halted = (flags & kFused) && ctrl_halted(ctrl);
     const StepClock clk = published_step_clock(ctrl);
     const int kk = in ? k : 0;
     const double h0 = ro(X.hd + kk), uh0 = ro(S.uh + kk), vh0 = ro(S.vh + kk);
@@ -571,7 +604,6 @@ __global__ void __launch_bounds__(BS, 2048 / BS) update_mixed(DevMesh M, DevStat
     const float uv0 = vel0.x, vv0 = vel0.y;
     const float2 ewu = ro(X.ewu + kk);
     const float ew = ewu.x, euh = ewu.y, evh = ro(X.evh + kk);
-    if (halted) return;
     const float dtf = (float)clk.dt;
     int bad = 0, nonfinite = 0;
     if (in) {
@@ -792,12 +824,19 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
     const int span = min(BS, SP - kb);  // a multiple of 64 elements
     const int k = kb + tid;
     const unsigned bytes = (unsigned)span * 4u;
-    if (tid == 0) mbar_init(&bar, 1);
+    // a scenario stopped before the previous kernel finished (halt == 1: its
+    // last distribute has run) stays stopped for the rest of the run: its
+    // blocks fetch nothing.  Thread 0 reads the flag for the whole block.
+    __shared__ int stopped_early;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        stopped_early = fused && ctrl_halted(ctrl) == 1;
+    }
     __syncthreads();
     // static planes (reconstruction coefficients, bed offsets) and index
     // planes before the previous kernel has finished
-    if (tid == 0) {
-        mbar_arrive_expect_tx(&bar, 20u * bytes + (unsigned)span);
+    if (tid == 0 && !stopped_early) {
+        mbar_expect_tx(&bar, 15u * bytes + (unsigned)span);
 #pragma unroll
         for (int i = 0; i < 3; i++) bulk_load(T.gc[i], X.gc + i * SP + kb, 2u * bytes, &bar);
 #pragma unroll
@@ -809,14 +848,20 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
         bulk_load(T.kind, X.kind + kb, (unsigned)span, &bar);  // span: a multiple of 64 bytes
     }
     pdl_wait();
+    if (stopped_early) return;  // no copy was issued
+    // halt == 1 only from a step clock kernel, which has completed: the same
+    // for every thread (halt == 2: the scenario stops after this distribute)
+    const bool halted = fused && ctrl_halt_settled(ctrl) == 1;
     if (tid == 0) {
-        bulk_load(T.ws, X.ws + kb, 2u * bytes, &bar);
-        bulk_load(T.hf, X.hf + kb, bytes, &bar);
-        bulk_load(T.vel, X.vel + kb, 2u * bytes, &bar);
+        if (halted) {
+            mbar_arrive(&bar);  // the static copies only
+        } else {
+            mbar_arrive_expect_tx(&bar, 5u * bytes);
+            bulk_load(T.ws, X.ws + kb, 2u * bytes, &bar);
+            bulk_load(T.hf, X.hf + kb, bytes, &bar);
+            bulk_load(T.vel, X.vel + kb, 2u * bytes, &bar);
+        }
     }
-    // read while the copies fly; acted on once they have landed (halt == 2:
-    // the scenario stops after this distribute)
-    const bool halted = fused && ctrl_halted(ctrl) == 1;
     int order;
     if (fused) {
         order = (int)ctrl->clk_order;
@@ -1079,6 +1124,15 @@ __global__ void __launch_bounds__(kBlock) vertices_from_mixed(DevMesh M, DevStat
     }
 }
 
+// FP64 centroid stage w = h + z from the mixed state (downloads of the
+// centroid values, update_other_quantities).
+__global__ void __launch_bounds__(kBlock) stage_from_mixed(int N, const double *__restrict__ hd,
+                                                           const double *__restrict__ zc,
+                                                           double *__restrict__ w) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < N) w[k] = hd[k] + zc[k];
+}
+
 __global__ void __launch_bounds__(kBlock) mass_partials_mixed(DevMesh M, DevState S, DevMixed X) {
     __shared__ double sh[kBlock];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1191,6 +1245,10 @@ void launch_prepare_mixed(const DevMesh &M, const DevState &S, const DevMixed &X
 void launch_vertices_from_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                                 cudaStream_t st) {
     vertices_from_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M, S, X);
+}
+void launch_stage_from_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
+                             cudaStream_t st) {
+    stage_from_mixed<<<grid_for(M.N), kBlock, 0, st>>>(M.N, X.hd, S.zc, S.w);
 }
 void launch_mass_partials_mixed(const DevMesh &M, const DevState &S, const DevMixed &X,
                                 cudaStream_t st) {

@@ -142,6 +142,9 @@ _SIGNATURES = [
     ("swgpu_update_boundary", C.c_int, [_VP]),
     ("swgpu_compute_fluxes", C.c_int, [_VP, _f64p]),
     ("swgpu_compute_forcing_terms", C.c_int, [_VP]),
+    ("swgpu_manning_friction_explicit", C.c_int, [_VP]),
+    ("swgpu_extrapolate_second_order_sw", C.c_int, [_VP]),
+    ("swgpu_balance_deep_and_shallow", C.c_int, [_VP]),
     ("swgpu_update_conserved_quantities", C.c_int, [_VP, C.c_double]),
     ("swgpu_update_other_quantities", C.c_int, [_VP]),
     ("swgpu_backup_conserved_quantities", C.c_int, [_VP]),

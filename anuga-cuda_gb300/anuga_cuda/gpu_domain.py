@@ -434,6 +434,22 @@ class GPU_domain:
 
     manning_friction_implicit = compute_forcing_terms
 
+    def manning_friction_explicit(self):
+        """gpu_domain_advanced.py:1330-1388: Manning friction added to the
+        explicit updates of the momenta."""
+        check(lib().swgpu_manning_friction_explicit(self._h), self._h)
+
+    def extrapolate_second_order_sw(self):
+        """gpu_domain_advanced.py:1061-1161: the limited second-order
+        reconstruction of stage and momentum (through velocity when
+        extrapolate_velocity_second_order) at the vertices; no protect, no
+        balance."""
+        check(lib().swgpu_extrapolate_second_order_sw(self._h), self._h)
+
+    def balance_deep_and_shallow(self):
+        """gpu_domain_advanced.py:957-995 on the current vertex values."""
+        check(lib().swgpu_balance_deep_and_shallow(self._h), self._h)
+
     @property
     def max_speed(self):
         """Per-triangle max_speed of the last compute_fluxes (FP64)."""

@@ -27,7 +27,7 @@ from .boundaries import Reflective_boundary, Time_stage_sine_boundary
 from .mesh import Mesh, rectangular_cross
 
 __all__ = ["Scenario", "dam_break", "tidal_harbour", "wet_dry", "poisson_disk",
-           "gaussian_random_field", "small_basin"]
+           "poisson_disk_grid", "harbour_points", "gaussian_random_field", "small_basin"]
 
 
 @dataclasses.dataclass
@@ -150,6 +150,54 @@ def poisson_disk(width, height, r, seed, k=30):
     return np.asarray(pts)
 
 
+def poisson_disk_grid(width, height, r, seed, rounds=30):
+    """Poisson-disk points (minimum spacing r) in [0,width] x [0,height] by
+    phased dart throwing on a background grid of cells r/sqrt(2) wide, which
+    hold at most one point each: every round visits the nine cell classes
+    (i mod 3, j mod 3) in turn and throws one uniform dart into every empty
+    cell of the class, keeping the darts with no point within r (cells of one
+    class lie three cells apart, so the darts of one phase never conflict;
+    a point within r lies at most two cells away).  Evenly spaced points on
+    the rectangle's edges come first, as in :func:`poisson_disk`.  Vectorised
+    over cells: about a second for 10^5 points."""
+    rng = np.random.default_rng(seed)
+    cell = r / np.sqrt(2.0)
+    gw, gh = int(np.ceil(width / cell)), int(np.ceil(height / cell))
+    px = np.full((gw + 4, gh + 4), np.nan)   # two guard cells on every side
+    py = np.full((gw + 4, gh + 4), np.nan)
+    nx_, ny_ = max(int(round(width / r)), 1), max(int(round(height / r)), 1)
+    bx = np.linspace(0.0, width, nx_ + 1)
+    by = np.linspace(0.0, height, ny_ + 1)[1:-1]
+    edge = np.concatenate([np.stack([bx, np.zeros_like(bx)], 1),
+                           np.stack([bx, np.full_like(bx, height)], 1),
+                           np.stack([np.zeros_like(by), by], 1),
+                           np.stack([np.full_like(by, width), by], 1)])
+    ei = np.minimum((edge[:, 0] / cell).astype(np.int64), gw - 1) + 2
+    ej = np.minimum((edge[:, 1] / cell).astype(np.int64), gh - 1) + 2
+    px[ei, ej], py[ei, ej] = edge[:, 0], edge[:, 1]
+    margin = 0.5 * r
+    offsets = [(di, dj) for di in range(-2, 3) for dj in range(-2, 3) if di or dj]
+    for _ in range(rounds):
+        for ci in range(3):
+            for cj in range(3):
+                I, J = np.meshgrid(np.arange(ci, gw) [::3], np.arange(cj, gh)[::3],
+                                   indexing="ij")
+                I, J = I.ravel() + 2, J.ravel() + 2
+                empty = np.isnan(px[I, J])
+                I, J = I[empty], J[empty]
+                x = (I - 2 + rng.random(I.size)) * cell
+                y = (J - 2 + rng.random(J.size)) * cell
+                ok = (x > margin) & (x < width - margin) & (y > margin) & (y < height - margin)
+                for di, dj in offsets:
+                    dx = px[I + di, J + dj] - x
+                    dy = py[I + di, J + dj] - y
+                    ok &= ~(dx * dx + dy * dy < r * r)   # NaN (empty): no conflict
+                px[I[ok], J[ok]], py[I[ok], J[ok]] = x[ok], y[ok]
+    inner = ~np.isnan(px)
+    inner[ei, ej] = False
+    return np.concatenate([edge, np.stack([px[inner], py[inner]], axis=1)])
+
+
 def gaussian_random_field(shape, spacing, corr, mean, sd, seed):
     """Stationary Gaussian random field on a grid by spectral synthesis with
     a Gaussian covariance of correlation length ``corr``."""
@@ -187,12 +235,26 @@ def dam_break(m=100, n=100):
         boundaries={t: Reflective_boundary() for t in mesh.tag_names}, finaltime=5.0)
 
 
-def tidal_harbour(target_triangles=45000, seed=2, width=2000.0, height=1000.0):
-    # Delaunay of P points in a rectangle gives ~2P triangles; spacing from
-    # the Poisson-disk packing density (~0.70 r^-2 points per unit area)
-    P = target_triangles / 2.0
-    r = np.sqrt(0.70 * width * height / P)
-    pts = poisson_disk(width, height, r, seed)
+def harbour_points(width, height, target_triangles, seed, points="grid"):
+    """Seeded Poisson-disk points whose Delaunay triangulation has about
+    ``target_triangles`` triangles: ``points="grid"`` the vectorised
+    :func:`poisson_disk_grid` (about 0.68 r^-2 points per unit area, 1.96
+    triangles per point), ``"bridson"`` the serial :func:`poisson_disk` with
+    the spacing rule of the committed golden fixtures (0.70 r^-2, 2 triangles
+    per point; about 10% fewer triangles than the target)."""
+    if points == "bridson":
+        return poisson_disk(width, height, np.sqrt(0.70 * width * height /
+                                                    (target_triangles / 2.0)), seed)
+    if points != "grid":
+        raise ValueError(f"points={points!r}: 'grid' or 'bridson'")
+    r = np.sqrt(0.68 * width * height * 1.96 / target_triangles)
+    return poisson_disk_grid(width, height, r, seed)
+
+
+def tidal_harbour(target_triangles=45000, seed=2, width=2000.0, height=1000.0, points="grid"):
+    # Delaunay of the Poisson-disk points (~2 triangles per point)
+    pts = harbour_points(width, height, target_triangles, seed, points)
+    r = np.sqrt(width * height * 1.4 / target_triangles)   # the mean spacing
     from scipy.spatial import Delaunay
     tri = Delaunay(pts).simplices
     V = pts[tri]
@@ -307,49 +369,17 @@ def channel_inflow(m=14, n=5, seed=0, peak=0.5, rise=2.0):
                     "bottom": Reflective_boundary()}, steps=50)
 
 
-def jittered_points(width, height, target_triangles, seed, jitter=0.3):
-    """About target_triangles/2 points in [0,width] x [0,height]: a
-    hexagonal lattice with uniform jitter of +-jitter spacings (a fast
-    stand-in for Poisson-disk sampling at large sizes), plus evenly spaced
-    points on the rectangle's edges."""
-    rng = np.random.default_rng(seed)
-    P = target_triangles / 2.0
-    d = np.sqrt(2.0 * width * height / (np.sqrt(3.0) * P))
-    dy = d * np.sqrt(3.0) / 2.0
-    ny = max(int(round(height / dy)), 1)
-    nx = max(int(round(width / d)), 1)
-    dx, dy = width / nx, height / ny
-    jj, ii = np.meshgrid(np.arange(1, ny), np.arange(1, nx), indexing="ij")
-    x = (ii + 0.5 * (jj % 2) - 0.25) * dx
-    y = jj * dy
-    x = x.ravel() + rng.uniform(-jitter, jitter, x.size) * dx
-    y = y.ravel() + rng.uniform(-jitter, jitter, y.size) * dy
-    keep = (x > 0.2 * dx) & (x < width - 0.2 * dx)
-    inner = np.stack([x[keep], y[keep]], axis=1)
-    bx = np.linspace(0.0, width, nx + 1)
-    by = np.linspace(0.0, height, ny + 1)[1:-1]
-    edge = np.concatenate([np.stack([bx, np.zeros_like(bx)], 1),
-                           np.stack([bx, np.full_like(bx, height)], 1),
-                           np.stack([np.zeros_like(by), by], 1),
-                           np.stack([np.full_like(by, width), by], 1)])
-    return np.concatenate([edge, inner])
-
-
 def inflow_harbour(target_triangles=45000, seed=4, peak=200.0, rise=900.0, friction=0.025,
-                   width=2000.0, height=1000.0, fast_points=True):
+                   width=2000.0, height=1000.0, points="grid"):
     """The tidal harbour's extent, Delaunay mesh and Gaussian-random-field
     bed (mean -5 m, sd 3 m, correlation 100 m, clipped at +1 m), water at
     rest at level 0, fed through its west edge by a triangular inflow
     hydrograph (``peak`` m^3/s after ``rise`` s, back to 0 after another
-    2*rise s), walls elsewhere, uniform Manning ``friction``.  Jittered
-    lattice points by default (fast at 10^5 triangles)."""
+    2*rise s), walls elsewhere, uniform Manning ``friction``.  Seeded
+    Poisson-disk points (:func:`harbour_points`)."""
     from scipy.spatial import Delaunay
     from .boundaries import Inflow_hydrograph_boundary
-    if fast_points:
-        pts = jittered_points(width, height, target_triangles, seed)
-    else:
-        P = target_triangles / 2.0
-        pts = poisson_disk(width, height, np.sqrt(0.70 * width * height / P), seed)
+    pts = harbour_points(width, height, target_triangles, seed, points)
     tri = Delaunay(pts).simplices
     V = pts[tri]
     area = 0.5 * np.abs((V[:, 1, 0] - V[:, 0, 0]) * (V[:, 2, 1] - V[:, 0, 1]) -

@@ -854,6 +854,10 @@ int swgpu_get_boundary_values(void *handle, int q, double *out) {
         case SWGPU_XMOMENTUM: src = h->S.uhb; break;
         case SWGPU_YMOMENTUM: src = h->S.vhb; break;
         case SWGPU_ELEVATION: src = h->S.zb; break;
+        // derived: as of the last update_other_quantities
+        case SWGPU_HEIGHT: src = h->S.hb; break;
+        case SWGPU_XVELOCITY: src = h->S.ub; break;
+        case SWGPU_YVELOCITY: src = h->S.vb; break;
         default: return fail(h, SWGPU_EINVAL, "no boundary values for quantity %d", q);
     }
     return download(h, out, src, (size_t)h->M.Nb);
@@ -957,8 +961,44 @@ int swgpu_compute_forcing_terms(void *handle) {
     Handle *h = static_cast<Handle *>(handle);
     int rc = require_fp64(h, "compute_forcing_terms");
     if (rc) return rc;
-    launch_forcing_fp64(h->M, h->S, h->P, h->stream);
+    launch_forcing_fp64(h->M, h->S, h->P, false, h->stream);
     if ((rc = check_launch(h, "compute_forcing_terms"))) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+int swgpu_manning_friction_explicit(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "manning_friction_explicit");
+    if (rc) return rc;
+    launch_forcing_fp64(h->M, h->S, h->P, true, h->stream);
+    if ((rc = check_launch(h, "manning_friction_explicit"))) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return SWGPU_OK;
+}
+
+int swgpu_extrapolate_second_order_sw(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "extrapolate_second_order_sw");
+    if (rc) return rc;
+    if (h->P.flow_algorithm)
+        return fail(h, SWGPU_EINVAL,
+                    "extrapolate_second_order_sw: the 'tsunami' flow algorithm extrapolates "
+                    "to edges inside distribute_to_vertices_and_edges");
+    if (h->P.extrapolate_velocity_second_order) launch_velocities_fp64(h->M, h->S, h->P, h->stream);
+    launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl, kExtrapolateOnly, h->stream);
+    if ((rc = check_launch(h, "extrapolate_second_order_sw"))) return rc;
+    h->vertices_stale = false;
+    if ((rc = sync_ctrl(h))) return rc;
+    return device_status(h);
+}
+
+int swgpu_balance_deep_and_shallow(void *handle) {
+    Handle *h = static_cast<Handle *>(handle);
+    int rc = require_fp64(h, "balance_deep_and_shallow");
+    if (rc) return rc;
+    launch_balance_fp64(h->M, h->S, h->P, h->stream);
+    if ((rc = check_launch(h, "balance_deep_and_shallow"))) return rc;
     CK(cudaStreamSynchronize(h->stream));
     return SWGPU_OK;
 }

@@ -331,16 +331,22 @@ __device__ __forceinline__ double manning_S(const DevMesh &M, const DevState &S,
     return Sf;
 }
 
-// compute_forcing_terms for the per-method API: semi_implicit_update += S*q.
-__global__ void __launch_bounds__(kBlock) forcing_fp64(DevMesh M, DevState S, DevParams P) {
+// compute_forcing_terms for the per-method API: semi_implicit_update += S*q
+// (manning_friction_implicit, gpu_domain_advanced.py:1255-1324), or with
+// explicit_target explicit_update += S*q (manning_friction_explicit, :1330-1388:
+// the same _manning_friction_flat / _sloped kernels given the explicit arrays).
+__global__ void __launch_bounds__(kBlock) forcing_fp64(DevMesh M, DevState S, DevParams P,
+                                                       int explicit_target) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M.N) return;
     bool applied;
     const double uh = S.uh[k], vh = S.vh[k];
     const double Sf = manning_S(M, S, P, k, S.w[k], uh, vh, applied);
     if (applied) {
-        S.suh[k] += Sf * uh;
-        S.svh[k] += Sf * vh;
+        double *xu = explicit_target ? S.euh : S.suh;
+        double *yu = explicit_target ? S.evh : S.svh;
+        xu[k] += Sf * uh;
+        yu[k] += Sf * vh;
     }
 }
 
@@ -544,6 +550,17 @@ __global__ void __launch_bounds__(kBlock) prepare_fp64(DevMesh M, DevState S, De
     const double dk = omax(w - zc, P.minimum_allowed_height);
     S.uvel[k] = uh / dk;
     S.vvel[k] = vh / dk;
+}
+
+// The centroid velocities alone: extrapolate_velocity_second_order_true
+// (extrapolate_second_order_sw.cu:77-104) as the stand-alone
+// extrapolate_second_order_sw runs it, on the state as it is (no protect).
+__global__ void __launch_bounds__(kBlock) velocities_fp64(DevMesh M, DevState S, DevParams P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M.N) return;
+    const double dk = omax(S.w[k] - S.zc[k], P.minimum_allowed_height);
+    S.uvel[k] = S.uh[k] / dk;
+    S.vvel[k] = S.vh[k] / dk;
 }
 
 // --------------------------------------------------------- distribute ---
@@ -898,6 +915,81 @@ __device__ __forceinline__ bool limit_by_neighbours(const DevMesh &M, const doub
     return ok;
 }
 
+// balance_deep_and_shallow (src/anuga_HMPP/shallow_water_ext.c:1462-1636)
+// of one triangle: centroid stage wk, bed zk, momentum uk, vk; bed vertex
+// values zvk; stage / momentum vertex values ow, ou, ov blended in place.
+__device__ __forceinline__ void balance_one(const DevParams &P, double wk, double zk, double uk,
+                                            double vk, const double (&zvk)[3], double (&ow)[3],
+                                            double (&ou)[3], double (&ov)[3]) {
+    const double eps = 1.0e-6;
+    const double hc = wk - zk;
+    double dz = 0.0, hv[3];
+    if (P.tight_slope_limiters == 0) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) dz = omax(dz, fabs(zvk[i] - zk));
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) hv[i] = ow[i] - zvk[i];
+    const double hmin = omin(hv[0], omin(hv[1], hv[2]));
+    double alpha;
+    if (P.tight_slope_limiters == 0) {
+        alpha = dz > 0.0 ? omax(omin(P.alpha_balance * hmin / dz, 1.0), 0.0) : 1.0;
+    } else if (hmin < P.H0) {
+        alpha = 1.0;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const double hd = hc - hv[i];
+            if (!(hd <= 0)) alpha = omin(alpha, (hc - P.H0) / hd);
+        }
+        if (alpha > 1.0) alpha = 1.0;
+        if (alpha < 0.0) alpha = 0.0;
+    } else {
+        alpha = 1.0;
+    }
+    if (alpha < 1) {
+        double uc = 0.0, vc = 0.0;
+        if (P.use_centroid_velocities == 1 && hc > eps) {
+            uc = uk / hc;
+            vc = vk / hc;
+        }
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            ow[i] = zvk[i] + (1 - alpha) * hc + alpha * hv[i];
+            if (P.use_centroid_velocities == 1) {
+                const double h = ow[i] - zvk[i];
+                ou[i] = uc * h;
+                ov[i] = vc * h;
+            } else {
+                ou[i] = (1 - alpha) * uk + alpha * ou[i];
+                ov[i] = (1 - alpha) * vk + alpha * ov[i];
+            }
+        }
+    }
+}
+
+// balance_deep_and_shallow as the stand-alone method
+// (gpu_domain_advanced.py:957-995): reads the stored vertex values.
+__global__ void __launch_bounds__(kBlock) balance_fp64(DevMesh M, DevState S, DevParams P) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = M.N;
+    if (k >= N) return;
+    double zvk[3], ow[3], ou[3], ov[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        zvk[i] = S.zv[i * N + k];
+        ow[i] = S.wv[i * N + k];
+        ou[i] = S.uhv[i * N + k];
+        ov[i] = S.vhv[i * N + k];
+    }
+    balance_one(P, S.w[k], S.zc[k], S.uh[k], S.vh[k], zvk, ow, ou, ov);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        S.wv[i * N + k] = ow[i];
+        S.uhv[i * N + k] = ou[i];
+        S.vhv[i * N + k] = ov[i];
+    }
+}
+
 template <int BS>
 __global__ void __launch_bounds__(BS) distribute_fp64(DevMesh M, DevState S, DevParams P,
                                                           const BcTag *tags, Ctrl *ctrl,
@@ -916,14 +1008,17 @@ __global__ void __launch_bounds__(BS) distribute_fp64(DevMesh M, DevState S, Dev
 #pragma unroll
         for (int i = 0; i < 3; i++) zvk[i] = S.zv[i * N + k];
         double ow[3], ou[3], ov[3];
-        if (order == 1) {
+        // the stand-alone extrapolate_second_order_sw is second order with
+        // the optimised limiter whatever the domain's order and limiter
+        const bool extrapolate_only = flags & kExtrapolateOnly;
+        if (order == 1 && !extrapolate_only) {
 #pragma unroll
             for (int i = 0; i < 3; i++) {
                 ow[i] = wk;
                 ou[i] = uk;
                 ov[i] = vk;
             }
-        } else if (P.limiter != kLimiterOptimised) {
+        } else if (P.limiter != kLimiterOptimised && !extrapolate_only) {
             const bool by_edge = P.limiter == kLimiterEdge;
             bool ok = limit_by_neighbours(M, S.w, k, P.beta_w, by_edge, ow);
             ok &= limit_by_neighbours(M, S.uh, k, P.beta_uh, by_edge, ou);
@@ -1033,53 +1128,7 @@ __global__ void __launch_bounds__(BS) distribute_fp64(DevMesh M, DevState S, Dev
             }
         }
 
-        // balance_deep_and_shallow
-        {
-            const double eps = 1.0e-6;
-            const double hc = wk - zk;
-            double dz = 0.0, hv[3];
-            if (P.tight_slope_limiters == 0) {
-#pragma unroll
-                for (int i = 0; i < 3; i++) dz = omax(dz, fabs(zvk[i] - zk));
-            }
-#pragma unroll
-            for (int i = 0; i < 3; i++) hv[i] = ow[i] - zvk[i];
-            const double hmin = omin(hv[0], omin(hv[1], hv[2]));
-            double alpha;
-            if (P.tight_slope_limiters == 0) {
-                alpha = dz > 0.0 ? omax(omin(P.alpha_balance * hmin / dz, 1.0), 0.0) : 1.0;
-            } else if (hmin < P.H0) {
-                alpha = 1.0;
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    const double hd = hc - hv[i];
-                    if (!(hd <= 0)) alpha = omin(alpha, (hc - P.H0) / hd);
-                }
-                if (alpha > 1.0) alpha = 1.0;
-                if (alpha < 0.0) alpha = 0.0;
-            } else {
-                alpha = 1.0;
-            }
-            if (alpha < 1) {
-                double uc = 0.0, vc = 0.0;
-                if (P.use_centroid_velocities == 1 && hc > eps) {
-                    uc = uk / hc;
-                    vc = vk / hc;
-                }
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    ow[i] = zvk[i] + (1 - alpha) * hc + alpha * hv[i];
-                    if (P.use_centroid_velocities == 1) {
-                        const double h = ow[i] - zvk[i];
-                        ou[i] = uc * h;
-                        ov[i] = vc * h;
-                    } else {
-                        ou[i] = (1 - alpha) * uk + alpha * ou[i];
-                        ov[i] = (1 - alpha) * vk + alpha * ov[i];
-                    }
-                }
-            }
-        }
+        if (!(flags & kExtrapolateOnly)) balance_one(P, wk, zk, uk, vk, zvk, ow, ou, ov);
 
 #pragma unroll
         for (int i = 0; i < 3; i++) {
@@ -1269,8 +1318,16 @@ void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P, C
         flux_fp64<256><<<g, 256, 0, st>>>(M, S, P, ctrl, flags);
 }
 void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                         bool explicit_target, cudaStream_t st) {
+    forcing_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P, explicit_target ? 1 : 0);
+}
+void launch_velocities_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                            cudaStream_t st) {
+    velocities_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P);
+}
+void launch_balance_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                          cudaStream_t st) {
-    forcing_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P);
+    balance_fp64<<<grid_for(M.N), kBlock, 0, st>>>(M, S, P);
 }
 void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P, Ctrl *ctrl,
                         double dt, int flags, const Stage &stage, cudaStream_t st) {

@@ -183,6 +183,8 @@ enum : int {
     kWriteMaxSpeed = 16,  // flux writes max_speed
     kNoTimestep = 32,     // flux skips the timestep reduction (later Runge-Kutta stages)
     kTrack = 64,          // update records maximum depth and arrival time (whole steps)
+    kExtrapolateOnly = 128,  // FP64 distribute: the second-order extrapolation alone
+                             // (extrapolate_second_order_sw), no balance, vertex values only
 };
 
 // One stage of a fused step.  An Euler step is one stage; ANUGA's RK2 and
@@ -222,7 +224,16 @@ void launch_boundary_fp64(const DevMesh &M, const DevState &S, const DevParams &
                           Ctrl *ctrl, cudaStream_t st);
 void launch_flux_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                       Ctrl *ctrl, int flags, cudaStream_t st);
+// Manning friction (S * momentum) added to the semi-implicit updates, or with
+// explicit_target to the explicit updates (manning_friction_explicit)
 void launch_forcing_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                         bool explicit_target, cudaStream_t st);
+// centroid velocities uh / max(h, minimum_allowed_height) alone (the head of
+// the stand-alone extrapolate_second_order_sw; no protect)
+void launch_velocities_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
+                            cudaStream_t st);
+// balance_deep_and_shallow on the stored vertex values
+void launch_balance_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                          cudaStream_t st);
 void launch_update_fp64(const DevMesh &M, const DevState &S, const DevParams &P,
                         Ctrl *ctrl, double dt, int flags, const Stage &stage,

@@ -15,7 +15,11 @@
 // loading this library holds until the process exits.  One partial per
 // 256-element block limits a call to kNoAllocMaxElements = 4,194,304
 // elements; larger sizes are rejected with SWGPU_EINVAL.  The arithmetic and
-// reduction order are those of swgpu_mass, so the results are identical.
+// the reduction order (256-element block sums in a fixed tree, then one block
+// summing the partials) are those of swgpu_mass on an FP64 handle, so given
+// that handle's own centroid arrays, in its triangle order, the two results
+// are bit-identical.  (A mixed-precision handle's swgpu_mass sums area times
+// its FP64 depth instead of stage minus bed.)
 #include <cstdio>
 #include <mutex>
 
@@ -67,6 +71,9 @@ __global__ void __launch_bounds__(kNoAllocBlock)
 // Device address of g_volume_partials per device, looked up once per device
 // with that device current.  In host code the symbol's name is a host-side
 // stand-in, not a device address, so kernels only ever receive this pointer.
+// The address belongs to the device's primary context as it was at the
+// first call: a cudaDeviceReset after that call is not supported (the
+// library's module, and the array, are loaded again in the new context).
 struct ScratchSlot {
     int device;
     double *ptr;
@@ -125,6 +132,18 @@ extern "C" int swgpu_water_volume_noalloc(const double *areas, const double *sta
                  (long long)n, kNoAllocMaxElements, kNoAllocMaxPartials, kNoAllocBlock);
         swgpu::record_global_error(msg);
         return SWGPU_EINVAL;
+    }
+    // an error left by the caller's earlier work is reported as such and left
+    // in place, not taken for this call's launch failure
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "swgpu_water_volume_noalloc: a CUDA error was already pending before the "
+                 "call (%s); nothing launched",
+                 cudaGetErrorString(pending));
+        swgpu::record_global_error(msg);
+        return SWGPU_ECUDA;
     }
     double *partials = nullptr;
     int rc = scratch_for_current_device(&partials);

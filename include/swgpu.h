@@ -304,7 +304,9 @@ int swgpu_set_quantity(void *handle, int quantity, const double *centroid,
 int swgpu_get_quantity(void *handle, int quantity, double *centroid,
                        double *vertex, double *edge);
 
-/* Boundary values of slot m for stage/xmomentum/ymomentum/elevation. */
+/* Boundary values of slot m for stage/xmomentum/ymomentum/elevation, and
+ * for height/xvelocity/yvelocity as of the last
+ * swgpu_update_other_quantities. */
 int swgpu_get_boundary_values(void *handle, int quantity, double *out);
 
 /* explicit_update (stage/xmom/ymom) or semi_implicit_update (xmom/ymom). */
@@ -342,6 +344,22 @@ int swgpu_compute_fluxes(void *handle, double *flux_timestep);
 
 /* compute_forcing_terms -> manning_friction_implicit (:1255-1324). */
 int swgpu_compute_forcing_terms(void *handle);
+
+/* manning_friction_explicit (:1330-1388): the same Manning friction term
+ * S * momentum added to the explicit updates of x and y momentum (FP64
+ * handles). */
+int swgpu_manning_friction_explicit(void *handle);
+
+/* extrapolate_second_order_sw (:1061-1161): centroid velocities (when
+ * extrapolate_velocity_second_order) and the limited second-order
+ * reconstruction of stage and momentum at the vertices, with no protect
+ * and no balance; vertex values only (FP64 handles, default flow
+ * algorithm). */
+int swgpu_extrapolate_second_order_sw(void *handle);
+
+/* balance_deep_and_shallow (:957-995) on the current vertex values (FP64
+ * handles). */
+int swgpu_balance_deep_and_shallow(void *handle);
 
 /* update_conserved_quantities (:1412-1442) with the given dt. */
 int swgpu_update_conserved_quantities(void *handle, double timestep);
@@ -429,8 +447,14 @@ int swgpu_synchronize(void *handle);
  * address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  All calls on a device share the one
  * array, so calls that overlap on the GPU (different streams or threads
- * without ordering) race; calls ordered on one stream do not.  Results are
- * identical to swgpu_mass on the same data.  Errors: swgpu_last_error(NULL). */
+ * without ordering) race; calls ordered on one stream do not.  The sum is
+ * taken in swgpu_mass's order: given an FP64 handle's own centroid arrays in
+ * that handle's triangle order, the result is bit-identical to its
+ * swgpu_mass (a mixed-precision handle's swgpu_mass sums area times its FP64
+ * depth instead).  A CUDA error already pending when the call is made is
+ * reported (SWGPU_ECUDA) and left pending; nothing is launched.  The scratch
+ * address belongs to the device's context at the first call: do not call
+ * cudaDeviceReset afterwards.  Errors: swgpu_last_error(NULL). */
 int swgpu_water_volume_noalloc(const double *areas, const double *stage,
                                const double *elevation, int64_t n, double *volume,
                                void *stream);

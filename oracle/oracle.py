@@ -29,7 +29,10 @@ SWCPU_SO = os.path.join(HERE, "_build", "libswcpu.so")
 REF_SW_SO = os.path.join(HERE, "_ref", "libref_sw.so")
 REF_Q_SO = os.path.join(HERE, "_ref", "libref_quantity.so")
 REF_SWB2_SO = os.path.join(HERE, "_ref", "libref_swb2.so")
-REFERENCE_SRC = "/root/reference/src/anuga_HMPP"
+# the reference project's root (its vendored ANUGA C kernels are compiled
+# from there when present): $ANUGA_CUDA_REFERENCE, default /root/reference
+REFERENCE_ROOT = os.environ.get("ANUGA_CUDA_REFERENCE", "/root/reference")
+REFERENCE_SRC = os.path.join(REFERENCE_ROOT, "src", "anuga_HMPP")
 
 BC_REFLECTIVE, BC_DIRICHLET, BC_TIME_STAGE_SINE = 0, 1, 2
 
@@ -125,7 +128,8 @@ def swcpu():
             build(ref=False)
         L = C.CDLL(SWCPU_SO)
         P = C.POINTER(OrcDomain)
-        for name in ["swcpu_gravity_wb", "swcpu_manning_friction", "swcpu_protect",
+        for name in ["swcpu_gravity_wb", "swcpu_manning_friction",
+                     "swcpu_manning_friction_explicit", "swcpu_protect",
                      "swcpu_extrapolate_second_order_sw", "swcpu_extrapolate_first_order",
                      "swcpu_balance_deep_and_shallow", "swcpu_interpolate_to_edges",
                      "swcpu_distribute_to_vertices_and_edges", "swcpu_update_boundary"]:
@@ -160,8 +164,19 @@ def swcpu():
         L.swcpu_mass.restype = C.c_double
         L.swcpu_velocities_and_height.argtypes = [P, _d, _d, _d]
         L.swcpu_velocities_and_height.restype = None
+        L.swcpu_boundary_velocities_and_height.argtypes = [P, _d, _d, _d]
+        L.swcpu_boundary_velocities_and_height.restype = None
+        L.swcpu_set_libm_ulps.argtypes = [C.c_int]
+        L.swcpu_set_libm_ulps.restype = None
         _SWCPU = L
     return _SWCPU
+
+
+def set_libm_ulps(n: int) -> None:
+    """Move every pow and sin result of the oracle by n ulps (0 restores
+    the host libm's results): a one-ulp libm difference, the kind CUDA's pow
+    and sin have against the host's, applied to the oracle alone."""
+    swcpu().swcpu_set_libm_ulps(int(n))
 
 
 def _params_struct(p) -> OrcParams:
@@ -277,6 +292,21 @@ class OracleDomain:
 
     def manning_friction(self):
         self.L.swcpu_manning_friction(self._ref())
+
+    def manning_friction_explicit(self):
+        self.L.swcpu_manning_friction_explicit(self._ref())
+
+    def update_other_quantities(self):
+        """Height and velocities at centroids and boundary slots
+        (update_other_quantities' kernel): dict name -> (centroid, boundary)."""
+        N, Nb = self.N, max(self.Nb, 1)
+        c = [np.zeros(N) for _ in range(3)]
+        b = [np.zeros(Nb) for _ in range(3)]
+        self.L.swcpu_velocities_and_height(self._ref(), *(a.ctypes.data_as(_d) for a in c))
+        self.L.swcpu_boundary_velocities_and_height(self._ref(),
+                                                    *(a.ctypes.data_as(_d) for a in b))
+        return {n: (c[i], b[i][:self.Nb]) for i, n in
+                enumerate(("height", "xvelocity", "yvelocity"))}
 
     def update_conserved_quantities(self, dt):
         return self.L.swcpu_update_conserved_quantities(self._ref(), dt)
@@ -590,11 +620,15 @@ class ReferenceKernels:
                                     "stage_centroid_values", "bed_centroid_values",
                                     "xmom_centroid_values", "ymom_centroid_values"]))
 
-    def manning_friction(self, od: OracleDomain) -> None:
+    def manning_friction(self, od: OracleDomain, explicit: bool = False) -> None:
+        """_manning_friction_flat / _sloped into the semi-implicit updates
+        (manning_friction_implicit) or, with ``explicit``, into the explicit
+        updates (manning_friction_explicit, gpu_domain_advanced.py:1330-1388)."""
         p, A = od.params, od.arrays
+        kind = "explicit" if explicit else "semi_implicit"
         names = ["stage_centroid_values", "bed_vertex_values", "xmom_centroid_values",
                  "ymom_centroid_values", "friction_centroid_values",
-                 "xmom_semi_implicit_update", "ymom_semi_implicit_update"]
+                 f"xmom_{kind}_update", f"ymom_{kind}_update"]
         if p.use_sloped_mannings:
             self.sw._manning_friction_sloped(p.g, p.minimum_allowed_height, od.N,
                                              self._ptr(A["vertex_coordinates"]),

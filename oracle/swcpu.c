@@ -22,6 +22,25 @@
 
 #include "swcpu.h"
 
+/* Sensitivity knob for tests: every pow and sin result of the oracle is
+ * moved by libm_ulps units in the last place (0, the default, leaves them as
+ * the host libm returns them).  A test sets it to measure how far a one-ulp
+ * difference in a libm result -- CUDA's pow and sin against the host's --
+ * carries through an evolve on its own. */
+static int libm_ulps = 0;
+
+void swcpu_set_libm_ulps(int n) { libm_ulps = n; }
+
+static double libm_result(double x)
+{
+    int i;
+    for (i = 0; i < libm_ulps; i++)
+        x = nextafter(x, INFINITY);
+    for (i = 0; i > libm_ulps; i--)
+        x = nextafter(x, -INFINITY);
+    return x;
+}
+
 /* src/anuga_HMPP/util_ext.h:45-59 -- max/min as plain comparisons (not
  * fmax/fmin): the result for equal or signed-zero arguments is the second
  * argument. */
@@ -267,7 +286,7 @@ void swcpu_gravity_wb(swcpu_domain *D)
  * :1272-1317 (_manning_friction_sloped): semi-implicit Manning friction,
  * eps = minimum_allowed_height as the reference GPU path passes it
  * (src/anuga_cuda/gpu_domain_advanced.py:1276-1318). */
-void swcpu_manning_friction(swcpu_domain *D)
+static void manning_friction_into(swcpu_domain *D, double *xmom_update, double *ymom_update)
 {
     const swcpu_params *P = D->params;
     const double g = P->g, eps = P->minimum_allowed_height;
@@ -298,11 +317,25 @@ void swcpu_manning_friction(swcpu_domain *D)
                 S = -g * eta * eta * zs * sqrt((uh * uh + vh * vh));
             else
                 S = -g * eta * eta * sqrt((uh * uh + vh * vh));
-            S /= pow(h, 7.0 / 3);
-            D->xmom_semi_implicit_update[k] += S * uh;
-            D->ymom_semi_implicit_update[k] += S * vh;
+            S /= libm_result(pow(h, 7.0 / 3));
+            xmom_update[k] += S * uh;
+            ymom_update[k] += S * vh;
         }
     }
+}
+
+/* manning_friction_implicit (gpu_domain_advanced.py:1255-1324): the term
+ * goes to the semi-implicit updates. */
+void swcpu_manning_friction(swcpu_domain *D)
+{
+    manning_friction_into(D, D->xmom_semi_implicit_update, D->ymom_semi_implicit_update);
+}
+
+/* manning_friction_explicit (gpu_domain_advanced.py:1330-1388): the same
+ * kernels given the explicit updates. */
+void swcpu_manning_friction_explicit(swcpu_domain *D)
+{
+    manning_friction_into(D, D->xmom_explicit_update, D->ymom_explicit_update);
 }
 
 /* src/anuga_HMPP/quantity.c:769-820 (_update) for one quantity.  Returns
@@ -1146,7 +1179,7 @@ void swcpu_update_boundary(swcpu_domain *D)
         } else if (T->type == SWCPU_BC_TIME_STAGE_SINE) {
             const double two_pi = 6.283185307179586;
             D->stage_boundary_values[m] =
-                T->p[0] + T->p[1] * sin(two_pi * D->time / T->p[2] + T->p[3]);
+                T->p[0] + T->p[1] * libm_result(sin(two_pi * D->time / T->p[2] + T->p[3]));
             D->xmom_boundary_values[m] = 0.0;
             D->ymom_boundary_values[m] = 0.0;
         } else if (T->type == SWCPU_BC_TRANSMISSIVE) {
@@ -1373,6 +1406,25 @@ double swcpu_mass(const swcpu_domain *D)
         s += D->areas[k] *
              (D->stage_centroid_values[k] - D->bed_centroid_values[k]);
     return s;
+}
+
+/* src/anuga_cuda/update_centroids_of_velocities_and_height/
+ * update_centroids_of_velocities_and_height.cu:1-52 (boundary part): depth,
+ * velocities at the boundary slots from the boundary values. */
+void swcpu_boundary_velocities_and_height(const swcpu_domain *D, double *h, double *u,
+                                          double *v)
+{
+    const double H0 = 1.0e-8;
+    long m;
+    for (m = 0; m < D->number_of_boundary_elements; m++) {
+        double hm = D->stage_boundary_values[m] - D->bed_boundary_values[m], f;
+        if (hm < 0)
+            hm = 0;
+        f = hm / (hm * hm + H0);
+        h[m] = hm;
+        u[m] = D->xmom_boundary_values[m] * f;
+        v[m] = D->ymom_boundary_values[m] * f;
+    }
 }
 
 /* src/anuga_cuda/update_centroids_of_velocities_and_height/

@@ -134,6 +134,11 @@ void swcpu_evolve_start(swcpu_domain *D, double yieldstep);
 int swcpu_evolve_steps(swcpu_domain *D, double yieldstep, double finaltime,
                        long max_steps, double time_epsilon);
 double swcpu_mass(const swcpu_domain *D);
+void swcpu_manning_friction_explicit(swcpu_domain *D);
+void swcpu_boundary_velocities_and_height(const swcpu_domain *D, double *h, double *u,
+                                          double *v);
+/* test knob: pow and sin results moved by n ulps (0: as the host libm) */
+void swcpu_set_libm_ulps(int n);
 void swcpu_velocities_and_height(const swcpu_domain *D, double *h, double *u,
                                  double *v);
 

@@ -93,7 +93,8 @@ def cases():
     yield "basin_momentum_limiter", scenarios.small_basin(9, 7, seed=7), DEFAULT.replace(
         extrapolate_velocity_second_order=0, tight_slope_limiters=0,
         use_centroid_velocities=0, use_sloped_mannings=1)
-    yield "harbour_small", scenarios.tidal_harbour(target_triangles=1500, seed=11), DEFAULT
+    yield "harbour_small", scenarios.tidal_harbour(target_triangles=1500, seed=11,
+                                                   points="bridson"), DEFAULT
     yield "basin_edge_limiter", scenarios.small_basin(9, 7, seed=8), DEFAULT.replace(
         use_edge_limiter=1, beta_w=0.8, beta_uh=1.1, beta_vh=1.3)
     yield "channel_vertex_limiter", scenarios.channel_inflow(14, 5, seed=1), DEFAULT.replace(

@@ -18,7 +18,8 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "anuga-cuda_gb300")]
 
 from anuga_cuda.io import read_tsh, tsh_to_mesh_arrays  # noqa: E402
 
-SRC = "/root/reference/tests/CUDA/merimbula/merimbula_10785.tsh"
+SRC = os.path.join(os.environ.get("ANUGA_CUDA_REFERENCE", "/root/reference"),
+                   "tests", "CUDA", "merimbula", "merimbula_10785.tsh")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 if __name__ == "__main__":

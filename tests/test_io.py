@@ -5,7 +5,8 @@ import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TSH = "/root/reference/tests/CUDA/merimbula/merimbula_10785.tsh"
+REF_TSH = os.path.join(os.environ.get("ANUGA_CUDA_REFERENCE", "/root/reference"),
+                       "tests", "CUDA", "merimbula", "merimbula_10785.tsh")
 
 SQUARE_TSH = """5 1 # <# of verts> <# of vert attributes>, next lines <vertex #> <x> <y> [attributes] ...Triangulation Vertices...
 0 0.0 0.0 -1.0

@@ -61,6 +61,9 @@ def test_each_kernel_bitwise(oracle_mod, ref, variant, seed):
         for q in ("xmom", "ymom"):
             assert bits_equal(a.arrays[q + "_semi_implicit_update"],
                               b.arrays[q + "_semi_implicit_update"])
+        a.manning_friction_explicit(); ref.manning_friction(b, explicit=True)
+        for q in ("xmom", "ymom"):
+            assert bits_equal(a.arrays[q + "_explicit_update"], b.arrays[q + "_explicit_update"])
         dt = 0.9 * fa
         assert a.update_conserved_quantities(dt) == 0 and ref.update(b, dt) == 0
         for q in ("stage", "xmom", "ymom"):

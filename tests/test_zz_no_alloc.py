@@ -3,10 +3,12 @@
 It exists for callers that cannot allocate device memory when they need the
 volume (inside a CUDA stream capture, under a device-memory pool they do not
 own, in loops that must avoid cudaMalloc's synchronisation); its scratch is a
-static device array, so it must agree with swgpu_mass, which uses scratch the
-handle allocated.  This file is collected last on purpose (a failure here
-leaves every other test already run) and passes alone in a fresh process as
-well as after the rest of the suite.
+static device array.  It sums in swgpu_mass's order, so on an FP64 handle's
+own centroid arrays, in the handle's triangle order (a GPU_domain built from a
+Mesh keeps the Mesh's order), it must return exactly swgpu_mass's value.
+This file is collected last on purpose (a failure here leaves every other
+test already run) and passes alone in a fresh process as well as after the
+rest of the suite.
 """
 import ctypes as C
 
@@ -15,7 +17,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-REL_MASS = 1e-12   # the water-volume tolerance of the parity tests
+REL_SUBSET = 1e-12  # a sub-range against numpy's own (differently ordered) sum
 
 
 def _dev(torch, a):
@@ -47,7 +49,7 @@ def test_noalloc_volume_matches_handle_volume_twice(swgpu_built):
         assert rc == 0, L.swgpu_last_error(None)
         torch.cuda.synchronize()
         got = float(out.item())
-        assert abs(got - expected) <= REL_MASS * abs(expected), (call, got, expected)
+        assert got == expected, (call, got, expected)
     # a different size on the same (shared) scratch, then the first again
     half = N // 2
     rc = L.swgpu_water_volume_noalloc(areas.data_ptr(), stage.data_ptr(), bed.data_ptr(), half,
@@ -57,7 +59,13 @@ def test_noalloc_volume_matches_handle_volume_twice(swgpu_built):
     a, w, z = sc.mesh.areas, d.quantities["stage"].centroid_values, \
         d.quantities["elevation"].centroid_values
     ref_half = float(np.sum(a[:half] * (w[:half] - z[:half])))
-    assert abs(out.item() - ref_half) <= 1e-11 * abs(ref_half)
+    assert abs(out.item() - ref_half) <= REL_SUBSET * abs(ref_half)
+    # the full size again on the same scratch: the same value as before
+    rc = L.swgpu_water_volume_noalloc(areas.data_ptr(), stage.data_ptr(), bed.data_ptr(), N,
+                                      out.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert float(out.item()) == expected
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(swgpu_built):

@@ -1,13 +1,18 @@
 """Launch-shape autotuner for the fused evolve step.
 
 The knobs are the block sizes of the three kernels of a step (flux,
-update, distribute) and the number of steps captured per CUDA graph
-(``swgpu_set_launch_config``).  Results do not depend on them, so tuning is
-pure measurement: each kernel's candidates are timed with CUDA events on the
-handle's own stream (``swgpu_profile_steps`` gives per-kernel times), one
-kernel at a time from the current best, and the fastest shape is kept.  The
-steps the measurement runs advance the model: tune a throwaway copy of a
-domain (``tune_domain`` does), or tune before setting the initial state.
+update, distribute), the persistent double-buffered mixed flux, and the
+number of steps captured per CUDA graph (``swgpu_set_launch_config``).
+Results do not depend on them, so tuning is pure measurement: each
+candidate shape runs whole steps through the device-resident loop (CUDA
+graphs, programmatic dependent launches, exactly as evolve issues them),
+timed with CUDA events on the handle's stream (``swgpu_evolve_run_timed``),
+one knob at a time from the current best; a candidate is kept when its step
+is at least 1% faster.  Timing kernels one by one instead would miss what the
+graph overlaps (a persistent flux that looks faster alone holds the SMs
+against the next kernel's early blocks).  The steps the measurement runs
+advance the model: tune a throwaway copy of a domain (``tune_domain``
+does), or tune before setting the initial state.
 
 Chosen shapes are cached in a JSON file keyed by device, precision, method
 and mesh size (rounded to a power of two), at ``$ANUGA_CUDA_TUNE_CACHE`` or
@@ -24,11 +29,10 @@ from . import _lib
 from ._lib import check, lib
 
 __all__ = ["get_config", "set_config", "tune_handle", "tune_domain", "cache_path",
-           "cached_config", "DEFAULT_CANDIDATES"]
+           "cached_config", "DEFAULT_CANDIDATES", "STEPS_PER_GRAPH"]
 
 DEFAULT_CANDIDATES = {"flux": (64, 128, 256), "update": (128, 256, 512),
                       "distribute": (128, 256, 512)}
-_KERNEL_INDEX = {"flux": 0, "update": 1, "distribute": 2}
 _FIELD = {"flux": "flux_block", "update": "update_block", "distribute": "distribute_block"}
 
 
@@ -48,16 +52,30 @@ def set_config(h, cfg: dict) -> None:
     check(lib().swgpu_set_launch_config(h, C.byref(c)), h)
 
 
-def _kernel_ms(h, steps):
-    ms = (C.c_double * 3)()
-    check(lib().swgpu_profile_steps(h, int(steps), ms), h)
-    return [ms[i] / steps for i in range(3)]
+STEPS_PER_GRAPH = (8, 16, 32)
+KEEP = 0.99   # a candidate replaces the best when its step time is below KEEP x best
 
 
-def tune_handle(h, steps=24, candidates=None, ensemble=False) -> dict:
+def _step_ms(h, steps):
+    """Device milliseconds per step of ``steps`` steps of the evolve loop."""
+    st, ms = _lib.State_t(), C.c_double()
+    check(lib().swgpu_evolve_run_timed(h, int(steps), C.byref(st), C.byref(ms)), h)
+    return ms.value / max(int(steps), 1)
+
+
+def _time_shape(h, cfg, steps):
+    """Best of two timed runs of ``steps`` steps with shape ``cfg``, after one
+    untimed graph (capture and first launch)."""
+    set_config(h, cfg)
+    _step_ms(h, cfg.get("steps_per_graph", 16))
+    return min(_step_ms(h, steps), _step_ms(h, steps))
+
+
+def tune_handle(h, steps=64, candidates=None, ensemble=False) -> dict:
     """Tune the launch shape of handle ``h`` in place (its evolve must have
-    been started); returns {"config", "kernel_ms", "default_ms", "tuned_ms"}
-    with per-kernel milliseconds per step of the starting and the chosen
+    been started, with no yield or final time within the steps tuning
+    runs); returns {"config", "default_ms", "tuned_ms"}: the chosen shape and
+    the device milliseconds per whole step of the starting and the chosen
     shape.  ``ensemble`` limits update/distribute blocks to 256."""
     cand = dict(DEFAULT_CANDIDATES)
     cand.update(candidates or {})
@@ -65,29 +83,29 @@ def tune_handle(h, steps=24, candidates=None, ensemble=False) -> dict:
         cand["update"] = tuple(b for b in cand["update"] if b <= 256)
         cand["distribute"] = tuple(b for b in cand["distribute"] if b <= 256)
     best = get_config(h)
-    _kernel_ms(h, max(steps // 4, 2))            # warm-up of the starting shape
-    start = _kernel_ms(h, steps)
-    best_ms = list(start)
+    best_ms = start_ms = _time_shape(h, best, steps)
+    trials = []
     for kernel, values in cand.items():
-        i = _KERNEL_INDEX[kernel]
-        trials = [{_FIELD[kernel]: v} for v in values if v != best[_FIELD[kernel]]]
+        trials += [{_FIELD[kernel]: v} for v in values]
         if kernel == "flux":
             # persistent double-buffered flux (mixed precision, tiles <= 128)
             trials += [{"flux_block": v, "flux_pipelined": 1} for v in values if v <= 128]
-        for change in trials:
-            trial = dict(best, **change)
-            if trial == best:
-                continue
-            try:
-                set_config(h, trial)
-            except _lib.SwgpuError:
-                continue
-            _kernel_ms(h, 2)
-            t = _kernel_ms(h, steps)[i]
-            if t < best_ms[i]:
-                best, best_ms[i] = trial, t
-        set_config(h, best)
-    return {"config": best, "default_ms": start, "tuned_ms": best_ms}
+    trials += [{"steps_per_graph": n} for n in STEPS_PER_GRAPH]
+    for change in trials:
+        trial = dict(best, **change)
+        if "flux_block" in change and "flux_pipelined" not in change:
+            trial["flux_pipelined"] = 0
+        if trial == best:
+            continue
+        try:
+            t = _time_shape(h, trial, steps)
+        except _lib.SwgpuError:
+            set_config(h, best)
+            continue
+        if t < KEEP * best_ms:
+            best, best_ms = trial, t
+    set_config(h, best)
+    return {"config": best, "default_ms": start_ms, "tuned_ms": best_ms}
 
 
 def cache_path() -> str:
@@ -129,7 +147,7 @@ def _store(key, cfg):
     os.replace(tmp, path)
 
 
-def tune_domain(domain, steps=24, use_cache=True) -> dict:
+def tune_domain(domain, steps=64, use_cache=True) -> dict:
     """Choose the launch shape of a GPU_domain: from the cache when it holds
     one for this device, precision, timestepping method and size; otherwise
     by tuning a copy of the domain (same mesh, parameters, state and

@@ -1365,42 +1365,48 @@ int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms) {
     if (!h || !ms || nsteps <= 0) return fail(h, SWGPU_EINVAL, "bad argument");
     int rc = prepare_run(h, nsteps);
     if (rc) return rc;
-    cudaEvent_t ev[4];
-    for (int i = 0; i < 4; i++) CK(cudaEventCreate(&ev[i]));
-    double acc[3] = {0, 0, 0};
+    // events around each kernel: flux, step clock (mixed), update, distribute
+    cudaEvent_t ev[5];
+    for (int i = 0; i < 5; i++) CK(cudaEventCreate(&ev[i]));
+    double acc[4] = {0, 0, 0, 0};
+    const bool mixed = h->precision != SWGPU_FP64;
     for (int64_t s = 0; s < nsteps; s++) {
         CK(cudaEventRecord(ev[0], h->stream));
-        if (h->precision == SWGPU_FP64)
+        if (!mixed)
             launch_flux_fp64(h->M, h->S, h->P, h->d_ctrl, kFused, h->stream);
-        else {
+        else
             launch_flux_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused, h->stream);
-            launch_step_clock_mixed(h->P, h->d_ctrl, h->nscen, h->M.shape.pdl, h->stream);
-        }
         CK(cudaEventRecord(ev[1], h->stream));
-        if (h->precision == SWGPU_FP64)
+        if (mixed) launch_step_clock_mixed(h->P, h->d_ctrl, h->nscen, h->M.shape.pdl, h->stream);
+        CK(cudaEventRecord(ev[2], h->stream));
+        if (!mixed)
             launch_update_fp64(h->M, h->S, h->P, h->d_ctrl, 0.0, kFused | kFrictionInline,
                                kEulerStage, h->stream);
         else
             launch_update_mixed(h->M, h->S, h->X, h->P, h->d_ctrl, kFused | kFrictionInline,
                                 kEulerStage, h->stream);
-        CK(cudaEventRecord(ev[2], h->stream));
-        if (h->precision == SWGPU_FP64)
+        CK(cudaEventRecord(ev[3], h->stream));
+        if (!mixed)
             launch_distribute_fp64(h->M, h->S, h->P, h->d_tags, h->d_ctrl,
                                    kFused | kWriteBoundary, h->stream);
         else
             launch_distribute_mixed(h->M, h->S, h->X, h->P, h->d_tags, h->d_ctrl,
                                     kFused | kWriteBoundary, kEulerStage, h->stream);
-        CK(cudaEventRecord(ev[3], h->stream));
+        CK(cudaEventRecord(ev[4], h->stream));
         if ((rc = check_launch(h, "profile step"))) return rc;
-        CK(cudaEventSynchronize(ev[3]));
+        CK(cudaEventSynchronize(ev[4]));
         float t;
-        for (int i = 0; i < 3; i++) {
+        for (int i = 0; i < 4; i++) {
             CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
             acc[i] += t;
         }
     }
-    for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
-    for (int i = 0; i < 3; i++) ms[i] = acc[i];
+    for (int i = 0; i < 5; i++) cudaEventDestroy(ev[i]);
+    // ms[0] flux, ms[1] update, ms[2] distribute, ms[3] step clock
+    ms[0] = acc[0];
+    ms[1] = acc[2];
+    ms[2] = acc[3];
+    ms[3] = acc[1];
     return finish_run(h, nullptr);
 }
 

@@ -70,11 +70,12 @@ ACC_STEPS = 1000                             # steps of the mixed-vs-FP64 accura
 WET_FLOOR = 0.01                             # m: wet triangles of the per-element depth error
 # FP64-pipe thread instructions per triangle of each FP64 kernel (ncu
 # sm__thread_inst_executed_pipe_fp64_pred_on.sum / triangles, 1,000,000-
-# triangle wet/dry mesh) and the FP64 pipe's rate: GB300's nominal 1.25 TFLOP/s
-# dense FP64 is 0.625 T FMA thread instructions/s (2 per SM per clock at
-# 2.07 GHz); DADD, DMUL, DFMA and the pipe's other instructions take one slot
-FP64_PIPE_INST = {"flux": None, "update": None, "distribute": None}
-FP64_PIPE_PEAK = 0.625e12
+# triangle wet/dry mesh after 48 steps) and the FP64 pipe's rate: GB300 runs
+# FP64 at 1/64 of the FP32 rate, 2 thread instructions per SM per clock
+# (DADD, DMUL, DFMA and the pipe's other instructions one slot each):
+# 152 SMs x 2 x 2.07 GHz
+FP64_PIPE_INST = {"flux": 494.99, "update": 166.79, "distribute": 317.03}
+FP64_PIPE_PEAK = 152 * 2 * 2.07e9
 
 
 def parse():
@@ -222,11 +223,11 @@ def run_ours(args, rank, world, local, sc):
         else:
             ms_max = ms.value
         assert st.total_steps == W + K, (st.total_steps, W + K)
-        kms = (C.c_double * 3)()
+        kms = (C.c_double * 4)()
         kp = min(K, 32)
         check(L.swgpu_profile_steps(d._h, kp, kms), d._h)
         results[prec] = {"ms": ms_max, "clocks": clk.summary(),
-                         "kernel_ms": [kms[i] / kp for i in range(3)], "time": st.time}
+                         "kernel_ms": [kms[i] / kp for i in range(4)], "time": st.time}
         del d
 
     # accuracy: fresh runs of exactly ACC_STEPS steps in both precisions
@@ -371,7 +372,7 @@ def run_autotune(sc, steps):
     d = GPU_domain(mesh=sc.mesh, parameters=DEFAULT, precision="mixed")
     sc.apply_to(d)
     d.evolve_steps(0)
-    rec = autotune.tune_handle(d._h, steps=16)
+    rec = autotune.tune_handle(d._h, steps=32)
     shapes = {"fixed_256": {"flux_block": 256, "update_block": 256, "distribute_block": 256,
                             "steps_per_graph": 16, "flux_pipelined": 0},
               "tuned": rec["config"]}
@@ -656,7 +657,7 @@ def main():
             fp64_pipe[k] = {"achieved": a, "frac": a / FP64_PIPE_PEAK}
     if fp64_pipe:
         fp64_pipe.update({"unit": "FP64-pipe thread instructions/s", "peak": FP64_PIPE_PEAK,
-                          "peak_source": "nominal (1.25 TFLOP/s dense FP64)",
+                          "peak_source": "152 SMs x 2 FP64 lanes per SM per clock x 2.07 GHz",
                           "instructions_source": "ncu sm__thread_inst_executed_pipe_fp64_pred_on"
                                                  ".sum per triangle, 1,000,000-triangle mesh"})
     line = {
@@ -672,7 +673,7 @@ def main():
                  "hbm_frac": MODEL_BYTES["fp64"] * N / (fp64_ms / K / 1000.0) / 1e9 / peak_gbs,
                  "fp64_pipe_roofline": fp64_pipe or None},
         "mixed_error": out["mixed_error"],
-        "kernel_ms": dict(zip(names, kms)),
+        "kernel_ms": dict(zip(names + ["step_clock"], kms)),
         "roofline": {"bound": "hbm", "kernel": names[dom] + "_mixed", "achieved": achieved,
                      "peak": peak_gbs, "unit": "GB/s", "frac": achieved / peak_gbs,
                      "traffic": NCU_TRAFFIC_4M[names[dom]] * N / 4.0e6,

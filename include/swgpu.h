@@ -420,10 +420,12 @@ int swgpu_evolve_run_timed(void *handle, int64_t max_steps, swgpu_state *state,
                            double *elapsed_ms);
 
 /* Runs nsteps Euler steps kernel by kernel (no graph) with a CUDA event
- * between kernels and returns the summed device time of each kernel:
- * ms[0] flux + gravity, ms[1] update, ms[2] extrapolation/balance/boundary.
- * For per-kernel rooflines.  No reference counterpart (the reference's
- * per-kernel times come from the legacy command-line profiler). */
+ * around each kernel and returns the summed device time of each: ms[0]
+ * flux + gravity, ms[1] update, ms[2] extrapolation/balance/boundary, ms[3]
+ * the mixed path's step clock (0 for FP64 handles, whose flux kernel
+ * evaluates the clock itself); ms holds 4 doubles.  For per-kernel
+ * rooflines.  No reference counterpart (the reference's per-kernel times
+ * come from the legacy command-line profiler). */
 int swgpu_profile_steps(void *handle, int64_t nsteps, double *ms);
 
 /* Synchronises the handle's stream. */

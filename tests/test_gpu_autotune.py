@@ -75,7 +75,7 @@ def test_tune_domain_and_cache(tmp_path, monkeypatch, swgpu_built):
     rec = tune_domain(d, steps=4)
     assert set(rec["config"]) == {"flux_block", "update_block", "distribute_block",
                                   "steps_per_graph", "flux_pipelined", "dependent_launch"}
-    assert all(t > 0 for t in rec["tuned_ms"])
+    assert 0 < rec["tuned_ms"] <= rec["default_ms"]
     assert json.load(open(cache_path()))
     again = tune_domain(gpu_from_scenario(sc, DEFAULT, "mixed"), steps=4)
     assert again.get("cached") and again["config"] == rec["config"]

@@ -85,7 +85,21 @@ static int check_launch(Handle *h, const char *what) {
     return SWGPU_OK;
 }
 
+// A handle whose kernels reported SWGPU_ETIMEOUT (a bounded wait for a
+// tile's bulk copies ran out twice) may have left copies in flight into the
+// shared memory of blocks that have exited; nothing it computes afterwards
+// can be trusted, so every later call that reaches the device fails and
+// only swgpu_destroy remains.
+static int check_usable(Handle *h) {
+    if (h->unusable)
+        return fail(h, SWGPU_ETIMEOUT,
+                    "handle unusable: a bounded device-side wait ran out earlier (bulk copies "
+                    "may still have been in flight); destroy the handle");
+    return SWGPU_OK;
+}
+
 static int sync_ctrl(Handle *h) {
+    if (int rc = check_usable(h)) return rc;
     CK(cudaMemcpyAsync(h->h_ctrl, h->d_ctrl, sizeof(Ctrl) * h->nscen, cudaMemcpyDeviceToHost,
                        h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -93,6 +107,7 @@ static int sync_ctrl(Handle *h) {
 }
 
 static int push_ctrl(Handle *h) {
+    if (int rc = check_usable(h)) return rc;
     CK(cudaMemcpyAsync(h->d_ctrl, h->h_ctrl, sizeof(Ctrl) * h->nscen, cudaMemcpyHostToDevice,
                        h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -119,9 +134,11 @@ static const char *status_text(int s) {
 
 // Device-side failures recorded in Ctrl.status become the call's status.
 static int device_status(Handle *h) {
+    if (int rc = check_usable(h)) return rc;
     for (int i = 0; i < h->nscen; i++) {
         if (h->h_ctrl[i].status != 0) {
             const int s = h->h_ctrl[i].status;
+            if (s == SWGPU_ETIMEOUT) h->unusable = true;
             if (h->nscen > 1)
                 return fail(h, s, "scenario %d: device reported: %s", i, status_text(s));
             return fail(h, s, "device reported: %s", status_text(s));

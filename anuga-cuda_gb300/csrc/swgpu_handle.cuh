@@ -42,6 +42,7 @@ struct Handle {
     bool vertices_stale = true;
     bool mixed_from_stage = true;  // mixed: FP64 stage upload not yet converted to depth
     bool elevation_set = false;
+    bool unusable = false;  // a kernel reported SWGPU_ETIMEOUT: only destroy is allowed
     std::string err;
     // host copies needed to rebuild mixed geometry
     std::vector<double> h_vxy, h_cxy, h_normals, h_len, h_areas, h_radii;

@@ -263,7 +263,11 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
 // Bounded wait for phase 0: every thread gives up after kWaitLimit polls
 // (each poll may suspend in hardware), reports SWGPU_ETIMEOUT, and polls once
 // more as long again so that copies still in flight land before the block
-// leaves.  Returns true when the data arrived.
+// leaves.  Returns true when the data arrived; on false the caller skips
+// every later use of the tile.  Should the second wait run out as well, the
+// block leaves with copies possibly still in flight into shared memory that
+// a later block may be given: the host then marks the handle unusable on
+// reading the status (every later call fails; only destroy remains).
 constexpr int kWaitLimit = 1 << 22;
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, Ctrl *ctrl,
                                                   unsigned parity = 0) {

@@ -44,7 +44,9 @@ enum swgpu_status {
     SWGPU_EBOUNDARY = 8,       /* unknown boundary type                     */
     SWGPU_EOVERSHOOT = 9,      /* model time overshot finaltime             */
     SWGPU_EMESH = 10,          /* inconsistent mesh arrays                  */
-    SWGPU_ETIMEOUT = 11        /* a bounded device-side wait ran out        */
+    SWGPU_ETIMEOUT = 11        /* a bounded device-side wait ran out; the   */
+                               /* handle is unusable from then on: every    */
+                               /* later call fails, destroy it              */
 };
 
 /* ---- precision of the evolve path ------------------------------------ */

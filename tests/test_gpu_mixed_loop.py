@@ -79,3 +79,29 @@ def test_mixed_dependent_launch_off_identical(swgpu_built):
         out.append((times, d.quantities["xmomentum"].centroid_values.copy()))
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_timeout_status_leaves_handle_unusable(swgpu_built):
+    """A kernel's SWGPU_ETIMEOUT (a bounded wait for a tile's bulk copies ran
+    out) leaves the handle unusable: the status is planted in the control
+    block from the host (no wait is made to run out on the GPU), and the run
+    that reads it and every later call that reaches the device fail."""
+    import ctypes as C
+    from anuga_cuda import DEFAULT, scenarios
+    from anuga_cuda._lib import State_t, SwgpuError, lib
+    ETIMEOUT = 11
+    sc = scenarios.small_basin(8, 6, seed=1)
+    d = gpu_from_scenario(sc, DEFAULT, "mixed")
+    d.evolve_steps(0)
+    st = d._state()
+    st.status = ETIMEOUT
+    d._set_state(st)
+    out = State_t()
+    assert lib().swgpu_evolve_run(d._h, 4, C.byref(out)) == ETIMEOUT
+    assert "wait ran out" in lib().swgpu_last_error(d._h).decode()
+    for call in (lambda: d.evolve_steps(2), d.distribute_to_vertices_and_edges,
+                 lambda: d._set_state(st)):
+        with pytest.raises(SwgpuError) as e:
+            call()
+        assert e.value.status == ETIMEOUT
+        assert "destroy" in str(e.value)

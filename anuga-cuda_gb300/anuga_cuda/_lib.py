@@ -19,6 +19,7 @@ __all__ = [
     "STAGE", "XMOMENTUM", "YMOMENTUM", "ELEVATION", "FRICTION", "HEIGHT", "XVELOCITY",
     "YVELOCITY", "FP64", "MIXED", "BC_REFLECTIVE", "BC_DIRICHLET", "BC_TIME_STAGE_SINE",
     "BC_TRANSMISSIVE", "BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM", "BC_INFLOW_HYDROGRAPH",
+    "BC_TIME_STAGE_FOURIER",
     "STOP_NONE", "STOP_YIELD", "STOP_FINAL", "STOP_BUDGET", "STOP_ERROR", "EXPORTED_SYMBOLS",
     "EULER", "RK2", "RK3",
 ]
@@ -28,6 +29,7 @@ FP64, MIXED = 0, 1
 EULER, RK2, RK3 = 1, 2, 3
 BC_REFLECTIVE, BC_DIRICHLET, BC_TIME_STAGE_SINE = 0, 1, 2
 BC_TRANSMISSIVE, BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM, BC_INFLOW_HYDROGRAPH = 3, 4, 5
+BC_TIME_STAGE_FOURIER = 6
 STOP_NONE, STOP_YIELD, STOP_FINAL, STOP_BUDGET, STOP_ERROR = range(5)
 
 STATUS_NAMES = {
@@ -98,7 +100,7 @@ class LaunchConfig_t(C.Structure):
 
 
 class BoundaryTag_t(C.Structure):
-    _fields_ = [("type", C.c_int64), ("p", C.c_double * 4)]
+    _fields_ = [("type", C.c_int64), ("p", C.c_double * 8)]
 
 
 # every function declared in include/swgpu.h: (name, restype, argtypes)

@@ -15,7 +15,7 @@ from . import _lib
 
 __all__ = ["Reflective_boundary", "Dirichlet_boundary", "Time_stage_sine_boundary",
            "Transmissive_boundary", "Transmissive_stage_zero_momentum_boundary",
-           "Inflow_hydrograph_boundary"]
+           "Inflow_hydrograph_boundary", "Time_stage_fourier_boundary"]
 
 
 class Boundary:
@@ -91,6 +91,36 @@ class Time_stage_sine_boundary(Boundary):
     def __repr__(self):
         return (f"Time_stage_sine_boundary(mean={self.mean}, amplitude={self.amplitude}, "
                 f"period={self.period}, phase={self.phase})")
+
+
+class Time_stage_fourier_boundary(Boundary):
+    """Time-dependent stage given by five coefficients of a truncated
+    Fourier series, c0 + c1 sin(wt) + c2 cos(wt) + c3 sin(2wt) + c4 cos(2wt)
+    with w = 2 pi / period, and zero momentum: ANUGA's Time_boundary with
+    that function of the model time, evaluated on the device (a tide with
+    its first overtide on an open edge)."""
+
+    type = _lib.BC_TIME_STAGE_FOURIER
+
+    def __init__(self, domain=None, coefficients=(0.0, 0.0, 0.0, 0.0, 0.0), period=3600.0):
+        c = [float(v) for v in coefficients]
+        if len(c) != 5:
+            raise ValueError("five coefficients c0..c4")
+        if not period:
+            raise ValueError("period must be nonzero")
+        self.domain = domain
+        self.coefficients, self.period = c, float(period)
+
+    def params(self, mesh=None, tag=None):
+        return tuple(self.coefficients) + (self.period,)
+
+    def evaluate(self, t):
+        c, wt = self.coefficients, 2 * math.pi * t / self.period
+        return [c[0] + c[1] * math.sin(wt) + c[2] * math.cos(wt) + c[3] * math.sin(2 * wt)
+                + c[4] * math.cos(2 * wt), 0.0, 0.0]
+
+    def __repr__(self):
+        return f"Time_stage_fourier_boundary(coefficients={self.coefficients}, period={self.period})"
 
 
 class Transmissive_boundary(Boundary):

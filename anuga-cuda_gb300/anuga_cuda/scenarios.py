@@ -283,11 +283,10 @@ def tidal_harbour(target_triangles=45000, seed=2, width=2000.0, height=1000.0, p
                     "wall": Reflective_boundary()}, steps=2000)
 
 
-def wet_dry(m=1000, n=None, seed=3, length=10000.0):
-    n = m if n is None else n
-    pts, tris, bnd = rectangular_cross(m, n, length, length)
-    mesh = Mesh(pts, tris, bnd)
-    rng = np.random.default_rng(seed)
+def wet_dry_bed(rng, length=10000.0):
+    """The wet/dry bed as a function of (x, y): a 1:100 beach rising in x
+    (the shoreline at 0.8 length) plus 40 Gaussian bumps of +-2 m (sigma 200
+    m at 10 km), their centres and signs drawn from ``rng``."""
     nb = 40
     bx, by = rng.uniform(0, length, nb), rng.uniform(0, length, nb)
     amp = 2.0 * rng.choice([-1.0, 1.0], nb)
@@ -304,6 +303,16 @@ def wet_dry(m=1000, n=None, seed=3, length=10000.0):
             z[near] += amp[i] * np.exp(-(dx * dx + dy * dy) / (2 * s * s))
         return z
 
+    return bed
+
+
+def wet_dry(m=1000, n=None, seed=3, length=10000.0):
+    n = m if n is None else n
+    pts, tris, bnd = rectangular_cross(m, n, length, length)
+    mesh = Mesh(pts, tris, bnd)
+    rng = np.random.default_rng(seed)
+    bed = wet_dry_bed(rng, length)
+    scale = length / 10000.0
     zp = bed(mesh.points[:, 0].copy(), mesh.points[:, 1].copy())
     z = zp[mesh.triangles]
     zc = z.mean(axis=1)

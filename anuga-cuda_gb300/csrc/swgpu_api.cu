@@ -734,17 +734,19 @@ int swgpu_set_boundary_tags(void *handle, const swgpu_boundary_tag *tags, int nt
         return fail(h, SWGPU_EINVAL, "mesh uses %d boundary tags, %d given", h->ntags, ntags);
     std::vector<BcTag> t((size_t)ntags);
     for (int i = 0; i < ntags; i++) {
-        if (tags[i].type < SWGPU_BC_REFLECTIVE || tags[i].type > SWGPU_BC_INFLOW_HYDROGRAPH)
+        if (tags[i].type < SWGPU_BC_REFLECTIVE || tags[i].type > SWGPU_BC_TIME_STAGE_FOURIER)
             return fail(h, SWGPU_EBOUNDARY, "tag %d: unknown boundary type %lld", i,
                         (long long)tags[i].type);
         if (tags[i].type == SWGPU_BC_TIME_STAGE_SINE && !(tags[i].p[2] != 0.0))
             return fail(h, SWGPU_EINVAL, "tag %d: sine boundary needs a nonzero period", i);
+        if (tags[i].type == SWGPU_BC_TIME_STAGE_FOURIER && !(tags[i].p[5] != 0.0))
+            return fail(h, SWGPU_EINVAL, "tag %d: Fourier boundary needs a nonzero period", i);
         if (tags[i].type == SWGPU_BC_INFLOW_HYDROGRAPH &&
             !(tags[i].p[0] >= 0.0 && tags[i].p[1] > 0.0 && tags[i].p[2] > 0.0))
             return fail(h, SWGPU_EINVAL,
                         "tag %d: hydrograph needs peak >= 0 and positive rise and fall", i);
         t[i].type = (int)tags[i].type;
-        for (int j = 0; j < 4; j++) t[i].p[j] = tags[i].p[j];
+        for (int j = 0; j < 8; j++) t[i].p[j] = tags[i].p[j];
     }
     const int n = std::max(h->ntags, 1);
     return upload(h, h->d_tags, t.data(), (size_t)std::min(ntags, n));

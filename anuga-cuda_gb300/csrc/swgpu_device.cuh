@@ -33,7 +33,7 @@ __device__ __forceinline__ double hydrograph(const double p[4], double t) {
 // values (reflective: src/anuga_cuda/evaluate_segment/evaluate_segment.cu:3-76;
 // Dirichlet: :80-115; ANUGA's transmissive boundaries: the inside edge
 // values, with or without momentum; the time-dependent stage and the inflow
-// hydrograph have no reference GPU counterpart: the hydrograph's unit
+// hydrograph and the Fourier stage have no reference GPU counterpart: the hydrograph's unit
 // discharge q(t) enters along the inward normal with the inside edge's
 // stage, or critical depth (q^2/g)^(1/3) above the edge bed ze where that
 // is higher, i.e. on a dry or shallow edge).  Returns false for an unknown
@@ -59,6 +59,14 @@ __device__ __forceinline__ bool eval_boundary(const BcTag &T, double time, doubl
     if (T.type == SWGPU_BC_TIME_STAGE_SINE) {
         const double two_pi = 6.283185307179586;
         wb = T.p[0] + T.p[1] * sin(two_pi * time / T.p[2] + T.p[3]);
+        uhb = 0.0;
+        vhb = 0.0;
+        return true;
+    }
+    if (T.type == SWGPU_BC_TIME_STAGE_FOURIER) {
+        const double wt = 6.283185307179586 * time / T.p[5];
+        wb = T.p[0] + T.p[1] * sin(wt) + T.p[2] * cos(wt) + T.p[3] * sin(2.0 * wt) +
+             T.p[4] * cos(2.0 * wt);
         uhb = 0.0;
         vhb = 0.0;
         return true;

@@ -132,7 +132,7 @@ struct DevParams {
 
 struct BcTag {
     int type;
-    double p[4];
+    double p[8];
 };
 
 // Whole-run summary for the host's polling: how many scenarios (Ctrl

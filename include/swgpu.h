@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define SWGPU_ABI_VERSION 1
+#define SWGPU_ABI_VERSION 2
 
 /* ---- status codes --------------------------------------------------- */
 enum swgpu_status {
@@ -85,18 +85,23 @@ enum swgpu_boundary_type {
                                     edge's stage and momentum              */
     SWGPU_BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM = 4, /* anuga
                                     Transmissive_stage_zero_momentum_boundary */
-    SWGPU_BC_INFLOW_HYDROGRAPH = 5 /* triangular hydrograph of unit discharge
+    SWGPU_BC_INFLOW_HYDROGRAPH = 5, /* triangular hydrograph of unit discharge
                                     q(t) (p0 peak in m^2/s, p1 rise, p2 fall,
                                     p3 start time) entering along the inward
                                     normal; stage the inside edge's, or
                                     critical depth (q^2/g)^(1/3) above the
                                     edge bed where higher; no reference
                                     counterpart                            */
+    SWGPU_BC_TIME_STAGE_FOURIER = 6 /* stage = p0 + p1*sin(wt) + p2*cos(wt)
+                                    + p3*sin(2wt) + p4*cos(2wt), w =
+                                    2*pi/p5, momentum 0, t = model time (an
+                                    ANUGA Time_boundary of that function)  */
 };
 
 typedef struct {
     int64_t type;      /* swgpu_boundary_type */
-    double p[4];       /* parameters, see swgpu_boundary_type */
+    double p[8];       /* parameters, see swgpu_boundary_type (unused
+                          entries ignored) */
 } swgpu_boundary_tag;
 
 /* Mesh arrays (anuga Mesh / struct domain in src/anuga_HMPP/sw_domain.h:16-180).

@@ -73,7 +73,7 @@ class OrcParams(C.Structure):
 
 
 class OrcTag(C.Structure):
-    _fields_ = [("type", C.c_long), ("p", C.c_double * 4)]
+    _fields_ = [("type", C.c_long), ("p", C.c_double * 8)]
 
 
 _MESH_L = ["neighbours", "neighbour_edges", "surrogate_neighbours", "number_of_boundaries",

@@ -1182,6 +1182,16 @@ void swcpu_update_boundary(swcpu_domain *D)
                 T->p[0] + T->p[1] * libm_result(sin(two_pi * D->time / T->p[2] + T->p[3]));
             D->xmom_boundary_values[m] = 0.0;
             D->ymom_boundary_values[m] = 0.0;
+        } else if (T->type == SWCPU_BC_TIME_STAGE_FOURIER) {
+            /* an ANUGA Time_boundary whose function is the truncated
+             * Fourier series c0 + c1 sin(wt) + c2 cos(wt) + c3 sin(2wt) +
+             * c4 cos(2wt), w = 2 pi / period, with zero momentum */
+            const double wt = 6.283185307179586 * D->time / T->p[5];
+            D->stage_boundary_values[m] =
+                T->p[0] + T->p[1] * libm_result(sin(wt)) + T->p[2] * libm_result(cos(wt)) +
+                T->p[3] * libm_result(sin(2.0 * wt)) + T->p[4] * libm_result(cos(2.0 * wt));
+            D->xmom_boundary_values[m] = 0.0;
+            D->ymom_boundary_values[m] = 0.0;
         } else if (T->type == SWCPU_BC_TRANSMISSIVE) {
             /* anuga Transmissive_boundary: the inside edge values */
             D->stage_boundary_values[m] = D->stage_edge_values[ki];

@@ -20,6 +20,7 @@ enum {
     SWCPU_BC_TRANSMISSIVE = 3,
     SWCPU_BC_TRANSMISSIVE_STAGE_ZERO_MOMENTUM = 4,
     SWCPU_BC_INFLOW_HYDROGRAPH = 5,
+    SWCPU_BC_TIME_STAGE_FOURIER = 6,
 };
 
 enum {
@@ -58,8 +59,9 @@ typedef struct {
 
 typedef struct {
     long type;     /* SWCPU_BC_* */
-    double p[4];   /* Dirichlet: stage, xmom, ymom; sine: mean, amp, period, phase;
-                      hydrograph: peak unit discharge, rise, fall, start time */
+    double p[8];   /* Dirichlet: stage, xmom, ymom; sine: mean, amp, period, phase;
+                      hydrograph: peak unit discharge, rise, fall, start time;
+                      Fourier: c0..c4, period */
 } swcpu_boundary_tag;
 
 typedef struct {

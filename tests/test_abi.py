@@ -33,7 +33,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.Mesh_t) == 8 * (2 + 14)
     assert ctypes.sizeof(_lib.Params_t) == 8 * (15 + 10)
     assert ctypes.sizeof(_lib.State_t) == 8 * (7 + 6)
-    assert ctypes.sizeof(_lib.BoundaryTag_t) == 8 * 5
+    assert ctypes.sizeof(_lib.BoundaryTag_t) == 8 * 9
     from anuga_cuda.config import Parameters
     import dataclasses
     assert [f.name for f in dataclasses.fields(Parameters)] == [n for n, _ in _lib.PARAM_FIELDS]

@@ -146,3 +146,50 @@ def test_transmissive_and_inflow_channel_evolve_matches_oracle(oracle_mod, swgpu
         assert max_rel(d.quantities[n].centroid_values,
                        od.arrays[p + "_centroid_values"]) <= REL_NSTEP, n
     assert d.get_water_volume() > 0
+
+
+def _channel_with_tide():
+    """The inflow channel whose downstream (right) edge is an open boundary
+    with a five-coefficient Fourier stage (a tide and its first overtide)."""
+    from anuga_cuda import Time_stage_fourier_boundary
+    sc = _channel()
+    sc.boundaries = dict(sc.boundaries)
+    sc.boundaries["right"] = Time_stage_fourier_boundary(
+        coefficients=(0.08, 0.03, -0.02, 0.01, 0.015), period=7.0)
+    return sc
+
+
+def test_fourier_stage_boundary_values_match_oracle(oracle_mod, swgpu_built):
+    from anuga_cuda import DEFAULT
+    sc = _channel_with_tide()
+    od = oracle_from_scenario(oracle_mod, sc, DEFAULT)
+    d = gpu_from_scenario(sc, DEFAULT)
+    b = sc.boundaries["right"]
+    for t in (0.0, 1.3, 4.9):
+        od.D.time = t
+        d.set_time(t)
+        od.distribute_to_vertices_and_edges()
+        od.update_boundary()
+        d.distribute_to_vertices_and_edges()
+        d.update_boundary()
+        for n, p in QUANTITIES:
+            assert max_rel(d.quantities[n].boundary_values, od.arrays[p + "_boundary_values"],
+                           floor=1e-300) <= REL_LIBM, (t, n)
+        # the open edge's stage is the series at t
+        m = sc.mesh.boundary_tag == sc.mesh.tag_names.index("right")
+        assert np.allclose(d.quantities["stage"].boundary_values[m], b.evaluate(t)[0],
+                           rtol=0, atol=1e-14)
+
+
+def test_fourier_stage_channel_evolve_matches_oracle(oracle_mod, swgpu_built):
+    from anuga_cuda import DEFAULT
+    sc = _channel_with_tide()
+    od = oracle_from_scenario(oracle_mod, sc, DEFAULT)
+    od.run_steps(60)
+    d = gpu_from_scenario(sc, DEFAULT)
+    st = d.evolve_steps(60)
+    assert st.total_steps == 60 and st.status == 0
+    assert abs(st.time - od.D.time) <= 1e-12 * max(od.D.time, 1.0)
+    for n, p in QUANTITIES:
+        assert max_rel(d.quantities[n].centroid_values,
+                       od.arrays[p + "_centroid_values"]) <= REL_NSTEP, n

@@ -120,3 +120,24 @@ def test_golden_cases_cover_wet_dry_and_boundaries():
     nb = np.concatenate([load_golden(c)["mesh/number_of_boundaries"] for c in GOLDEN_CASES])
     assert set(nb.tolist()) == {0, 1, 2, 3}, "every number_of_boundaries branch"
     assert np.isfinite(g["run/final/mass"]).all()
+
+
+def test_oracle_fourier_stage_boundary(oracle_mod):
+    """The oracle's Fourier stage boundary is the five-coefficient series of
+    the model time on every edge of its tag, with zero momentum."""
+    from anuga_cuda import DEFAULT, Time_stage_fourier_boundary, scenarios
+    from helpers import oracle_from_scenario
+    sc = scenarios.channel_inflow(10, 4, seed=2)
+    b = Time_stage_fourier_boundary(coefficients=(0.1, 0.04, -0.03, 0.02, -0.01), period=5.0)
+    sc.boundaries = dict(sc.boundaries, right=b)
+    od = oracle_from_scenario(oracle_mod, sc, DEFAULT)
+    m = sc.mesh.boundary_tag == sc.mesh.tag_names.index("right")
+    assert m.any()
+    for t in (0.0, 0.7, 3.1):
+        od.D.time = t
+        od.distribute_to_vertices_and_edges()
+        od.update_boundary()
+        A = od.arrays
+        assert np.allclose(A["stage_boundary_values"][m], b.evaluate(t)[0], rtol=0, atol=1e-14)
+        assert not A["xmom_boundary_values"][m].any()
+        assert not A["ymom_boundary_values"][m].any()

@@ -124,12 +124,11 @@ _SIGNATURES = [
     ("swgpu_mlp_last_error", C.c_char_p, [_VP]),
     ("swgpu_mlp_set_data", C.c_int, [_VP, _f32p, C.c_int64, _f32p, C.c_int64, _f32p]),
     ("swgpu_mlp_predict", C.c_int, [_VP, C.c_int64, C.c_int64, _VP, _f32p]),
-    ("swgpu_mlp_gradients", C.c_int, [_VP, _i64p, C.c_int64, C.c_float, C.c_float, _f32p,
-                                      _f32p, _f32p]),
+    ("swgpu_mlp_gradients", C.c_int, [_VP, _i64p, C.c_int64, C.c_float, C.c_float,
+                                       C.c_float, _f32p, _f32p, _f32p]),
     ("swgpu_mlp_train", C.c_int, [_VP, C.c_int, C.c_int64, C.c_uint64, C.c_float, C.c_float,
-                                  C.c_float, _f32p, _f32p]),
+                                  C.c_float, C.c_float, _f32p, _f32p]),
     ("swgpu_mlp_get_params", C.c_int, [_VP, _f32p]),
-    ("swgpu_mlp_set_tensor_path", C.c_int, [_VP, C.c_int]),
     ("swgpu_last_error", C.c_char_p, [_VP]),
     ("swgpu_device_info", C.c_int, [C.c_char_p, C.c_int]),
     ("swgpu_set_quantity", C.c_int, [_VP, C.c_int, _f64p, _f64p, _f64p]),

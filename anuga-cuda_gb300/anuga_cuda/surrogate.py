@@ -1,46 +1,71 @@
-"""BF16 MLP surrogate of the solver's maximum depth and arrival time.
+"""BF16 surrogate of the solver's maximum depth and arrival time, with the
+solver as its fallback and judge.
 
-A family of flood scenarios shares one mesh and bed (the wet/dry beach
-with bumps) and differs in 9 parameters: height, centre x and y, radius
-and aspect of an initial hump of water, Manning n, sea level, and the
-hump's initial x and y velocity.  The solver (an ``Ensemble`` with
-per-triangle tracking) gives, per scenario and triangle, the maximum depth
-and the first time the depth exceeded a threshold.  The surrogate
-(``libswgpu`` ``swgpu_mlp_*``: 16 -> 128 -> 128 -> 2, BF16 tensor cores)
-learns both from the scenario parameters and the triangle's bed,
-coordinates and distance to the hump centre (the depth as its excess over
-the initial depth, which the parameters fix exactly), and predicts them
-for new parameters in one pass over all (scenario, triangle) rows.
+The scenario family shares one mesh and bed: the wet/dry beach with bumps
+(a 1:100 beach rising to the east, the shoreline at x = 8 km, 40 seeded
+bumps of +-2 m) on ``cells`` x ``cells`` rectangular_cross cells over
+10 km x 10 km (200,704 triangles at 224).  Scenarios differ in 9
+parameters:
 
-``fallback_report`` compares predictions with solver fields on held-out
-scenarios: the blocks of 256 triangles whose maximum-depth error exceeds a
-tolerance (5 cm) are counted, and a scenario containing any such block is
-counted as rerun by the solver; time to answer is the surrogate's inference
-time plus the solver time of the rerun scenarios, against solver-only.
+* an inflow hydrograph through a 1 km segment of the east (land) edge: peak
+  discharge, rise time and total duration (a triangular hydrograph);
+* Manning's n, uniform over the mesh;
+* five coefficients c0..c4 of the stage on the west (sea) edge,
+  c0 + c1 sin(wt) + c2 cos(wt) + c3 sin(2wt) + c4 cos(2wt) with a period of
+  one hour (a tide and its first overtide); the sea starts at rest at the
+  boundary's stage at t = 0.
+
+The solver (an ``Ensemble`` with per-triangle tracking) gives, per scenario
+and triangle, the maximum depth and the first time the depth exceeded a
+threshold.  The network (``libswgpu`` ``swgpu_mlp_*``: 16 -> 256 -> 256 ->
+256 -> 3, BF16 on tcgen05 tensor cores) learns both from the scenario
+parameters and the triangle's centroid, bed and distance to the inflow (the
+depth as its excess over the still-water depth at the highest tide, which
+the parameters fix), and a third output learns the absolute error
+of its depth.
+
+``fallback`` turns predictions into an answer within a depth tolerance:
+blocks of 256 triangles (Morton order: compact patches of the mesh) whose
+calibrated error estimate exceeds the tolerance are re-solved by the solver
+on a band of the mesh (full width in x, from the west boundary to the
+inflow, reflective walls at the band's north and south edges) that covers
+the flagged blocks and the inflow segment with a margin; the band's values
+replace the predictions in the flagged blocks.  ``evaluate`` reports the
+time to the answer against the solver alone, and the answer's error against
+the full solve.
 """
 from __future__ import annotations
 
 import ctypes as C
-import time
 
 import numpy as np
 
 from . import _lib
 from ._lib import lib
+from .boundaries import (Inflow_hydrograph_boundary, Reflective_boundary,
+                         Time_stage_fourier_boundary)
 from .config import DEFAULT
 from .ensemble import ALIGN, Ensemble
-from .scenarios import Scenario, wet_dry
+from .mesh import Mesh, rectangular_cross
+from .scenarios import Scenario, wet_dry_bed
 
 __all__ = ["PARAM_NAMES", "PARAM_RANGES", "FamilyMesh", "sample_params", "family_scenario",
-           "solve", "Surrogate", "init_params", "fallback_report", "still_depth", "initial_depth",
-           "targets_from"]
+           "solve", "Surrogate", "init_params", "initial_depth", "static_depth", "max_tide",
+           "targets_from",
+           "block_index", "calibrate", "band_scenarios", "fallback", "evaluate",
+           "FINALTIME", "TIDE_PERIOD", "THRESHOLD", "DEPTH_SCALE", "NEVER"]
 
-PARAM_NAMES = ("height", "x0", "y0", "radius", "manning", "sea_level", "aspect", "u0", "v0")
-PARAM_RANGES = np.array([(0.5, 3.0), (3000.0, 7000.0), (3000.0, 7000.0), (150.0, 500.0),
-                         (0.01, 0.05), (-0.5, 0.5), (0.5, 1.5), (-0.5, 0.5), (-0.5, 0.5)])
-F, H, OUT = 16, 128, 2
-DEPTH_SCALE = 2.0        # depth target: (max depth - still-water depth) / DEPTH_SCALE
-NEVER = 1.25             # arrival target (arrival / finaltime) of a triangle that stays dry
+PARAM_NAMES = ("peak", "rise", "duration", "manning", "c0", "c1", "c2", "c3", "c4")
+PARAM_RANGES = np.array([(50.0, 500.0), (300.0, 1800.0), (450.0, 5400.0), (0.01, 0.05),
+                         (-0.5, 0.5), (-0.4, 0.4), (-0.4, 0.4), (-0.4, 0.4), (-0.4, 0.4)])
+DURATION_RATIO = (1.5, 3.0)     # duration / rise
+TIDE_PERIOD = 3600.0            # s
+FINALTIME = 3600.0              # s
+THRESHOLD = 0.02                # m: depth that counts as arrival
+INFLOW_Y = (4500.0, 5500.0)     # the inflow segment of the east edge, m
+F, H, OUT = 16, 256, 3
+DEPTH_SCALE = 1.0   # depth target: (max depth - still depth at the highest tide) / DEPTH_SCALE
+NEVER = 1.25        # arrival target (arrival / finaltime) of a triangle that stays dry
 
 
 def _f32p(a):
@@ -48,42 +73,86 @@ def _f32p(a):
 
 
 class FamilyMesh:
-    """The shared mesh and bed (wet_dry with ``cells`` x ``cells`` cells on
-    10 km x 10 km)."""
+    """The shared mesh and bed, and the per-triangle feature table."""
 
-    def __init__(self, cells=224, seed=3):
-        base = wet_dry(m=cells, seed=seed)
-        self.mesh = base.mesh
-        self.elevation_vertex = base.elevation_vertex
-        self.zc = base.elevation_arrays()[0]
-        self.N = base.N
+    def __init__(self, cells=224, seed=3, length=10000.0):
+        pts, tris, bnd = rectangular_cross(cells, cells, length, length)
+        y0, y1 = (v * length / 10000.0 for v in INFLOW_Y)
+        for (t, e), tag in list(bnd.items()):
+            if tag == "right":
+                a, b = [tris[t][j] for j in range(3) if j != e]
+                ym = 0.5 * (pts[a, 1] + pts[b, 1])
+                if y0 <= ym <= y1:
+                    bnd[(t, e)] = "inflow"
+        self.length = float(length)
+        self.mesh = Mesh(pts, tris, bnd)
+        bed = wet_dry_bed(np.random.default_rng(seed), length)
+        zp = bed(self.mesh.points[:, 0].copy(), self.mesh.points[:, 1].copy())
+        self.elevation_vertex = zp[self.mesh.triangles]
+        self.zc = self.elevation_vertex.mean(axis=1)
+        self.N = self.mesh.number_of_elements
         c = self.mesh.centroid_coordinates.reshape(-1, 2)
         self.xy = c
-        self.tri = np.stack([c[:, 0], c[:, 1], self.zc], axis=1).astype(np.float32)
+        dx = length - c[:, 0]
+        dy = np.maximum(np.maximum(y0 - c[:, 1], c[:, 1] - y1), 0.0)
+        self.d_inflow = np.hypot(dx, dy)
+        self.tri = np.stack([c[:, 0], c[:, 1], self.zc, self.d_inflow],
+                            axis=1).astype(np.float32)
+        self.inflow_y = (y0, y1)
 
 
 def sample_params(count, seed):
+    """Seeded parameter vectors [count][9] (PARAM_NAMES order)."""
     rng = np.random.default_rng(seed)
-    lo, hi = PARAM_RANGES[:, 0], PARAM_RANGES[:, 1]
-    return lo + (hi - lo) * rng.uniform(size=(count, len(lo)))
+    th = np.empty((count, 9))
+    th[:, 0] = rng.uniform(*PARAM_RANGES[0], count)
+    th[:, 1] = rng.uniform(*PARAM_RANGES[1], count)
+    th[:, 2] = th[:, 1] * rng.uniform(*DURATION_RATIO, count)
+    th[:, 3] = rng.uniform(*PARAM_RANGES[3], count)
+    th[:, 4] = rng.uniform(*PARAM_RANGES[4], count)
+    th[:, 5:9] = rng.uniform(-0.4, 0.4, (count, 4))
+    return th
 
 
-def family_scenario(fm: FamilyMesh, theta, finaltime=600.0):
-    A, x0, y0, rad, n, eta, asp, u0, v0 = (float(v) for v in theta)
-    dx, dy = fm.xy[:, 0] - x0, fm.xy[:, 1] - y0
-    shape = np.exp(-(dx * dx / (2 * rad * rad) + dy * dy / (2 * (asp * rad) ** 2)))
-    w = np.maximum(fm.zc, eta + A * shape)
-    h = w - fm.zc
-    N = fm.N
-    from .boundaries import Reflective_boundary
-    return Scenario(name="surrogate_family", mesh=fm.mesh, elevation_vertex=fm.elevation_vertex,
-                    stage_centroid=w, xmom_centroid=h * u0 * shape, ymom_centroid=h * v0 * shape,
-                    friction=np.full(N, n),
-                    boundaries={t: Reflective_boundary() for t in fm.mesh.tag_names},
-                    finaltime=finaltime)
+def tide(theta, t):
+    c0, c1, c2, c3, c4 = (float(v) for v in theta[4:9])
+    wt = 2.0 * np.pi * np.asarray(t, np.float64) / TIDE_PERIOD
+    return c0 + c1 * np.sin(wt) + c2 * np.cos(wt) + c3 * np.sin(2 * wt) + c4 * np.cos(2 * wt)
 
 
-def solve(fm: FamilyMesh, thetas, finaltime=600.0, threshold=0.05, batch=32,
+def _boundaries(theta):
+    peak, rise, dur, _n = (float(v) for v in theta[:4])
+    return {"left": Time_stage_fourier_boundary(coefficients=tuple(float(v) for v in theta[4:9]),
+                                                period=TIDE_PERIOD),
+            "inflow": Inflow_hydrograph_boundary(peak=peak, rise=rise, fall=dur - rise),
+            "right": Reflective_boundary(), "top": Reflective_boundary(),
+            "bottom": Reflective_boundary(), "exterior": Reflective_boundary()}
+
+
+def family_scenario(fm: FamilyMesh, theta, finaltime=FINALTIME, mesh=None, zv=None):
+    """The scenario of one parameter vector (on a sub-mesh when mesh and its
+    vertex bed zv are given)."""
+    mesh = fm.mesh if mesh is None else mesh
+    zv = fm.elevation_vertex if zv is None else zv
+    zc = zv.mean(axis=1)
+    w = np.maximum(zc, float(tide(theta, 0.0)))
+    N = mesh.number_of_elements
+    b = {t: v for t, v in _boundaries(theta).items() if t in mesh.tag_names}
+    return Scenario(name="surrogate_family", mesh=mesh, elevation_vertex=zv,
+                    stage_centroid=w, xmom_centroid=np.zeros(N), ymom_centroid=np.zeros(N),
+                    friction=np.full(N, float(theta[3])), boundaries=b, finaltime=finaltime)
+
+
+def _run(scenarios, finaltime, threshold, precision):
+    ens = Ensemble(scenarios, DEFAULT, precision)
+    ens.set_tracking(threshold)
+    ms = ens.run_timed(finaltime)
+    out = ens.get_tracking()
+    del ens
+    return out, ms
+
+
+def solve(fm: FamilyMesh, thetas, finaltime=FINALTIME, threshold=THRESHOLD, batch=32,
           precision="mixed"):
     """Solver fields for each parameter vector: (max_depth [S][N],
     arrival [S][N] (-1: never), device milliseconds)."""
@@ -93,42 +162,41 @@ def solve(fm: FamilyMesh, thetas, finaltime=600.0, threshold=0.05, batch=32,
     ms = 0.0
     for b0 in range(0, S, batch):
         scs = [family_scenario(fm, th, finaltime) for th in thetas[b0:b0 + batch]]
-        ens = Ensemble(scs, DEFAULT, precision)
-        ens.set_tracking(threshold)
-        ms += ens.run_timed(finaltime)
-        for i, (hm, ta) in enumerate(ens.get_tracking()):
+        out, t = _run(scs, finaltime, threshold, precision)
+        ms += t
+        for i, (hm, ta) in enumerate(out):
             hmax[b0 + i], tarr[b0 + i] = hm, ta
-        del ens
     return hmax, tarr, ms
 
 
-def still_depth(fm: FamilyMesh, thetas):
-    """Depth of the sea at rest at each scenario's sea level, [S][N]: the
-    part of the maximum depth that the bathymetry alone fixes."""
-    eta = np.asarray(thetas, np.float64)[:, 5:6]
-    return np.maximum(eta - fm.zc[None, :], 0.0).astype(np.float32)
-
-
 def initial_depth(fm: FamilyMesh, thetas):
-    """Depth of each scenario's initial state, [S][N]: the hump over the sea
-    at rest (as family_scenario builds it).  The maximum depth is at least
-    this, and the part the network learns is its excess: the sharp Gaussian
-    of the hump itself is known exactly from the parameters."""
+    """Depth of each scenario's initial state, [S][N]: the sea at rest at the
+    west boundary's stage at t = 0."""
     th = np.asarray(thetas, np.float64)
-    x, y = fm.xy[:, 0], fm.xy[:, 1]
-    out = np.empty((len(th), fm.N), np.float32)
-    for s, (A, x0, y0, rad, _n, eta, asp, _u, _v) in enumerate(th):
-        dx, dy = x - x0, y - y0
-        shape = np.exp(-(dx * dx / (2 * rad * rad) + dy * dy / (2 * (asp * rad) ** 2)))
-        out[s] = np.maximum(eta + A * shape - fm.zc, 0.0)
-    return out
+    w0 = th[:, 4] + th[:, 6] + th[:, 8]   # c0 + c2 + c4: the series at t = 0
+    return np.maximum(w0[:, None] - fm.zc[None, :], 0.0).astype(np.float32)
 
 
-def targets_from(fm: FamilyMesh, thetas, hmax, tarr, finaltime):
+def max_tide(thetas, finaltime=FINALTIME, samples=3601):
+    """Highest stage of each scenario's west boundary over [0, finaltime]."""
+    t = np.linspace(0.0, finaltime, samples)
+    return np.array([tide(th, t).max() for th in np.asarray(thetas, np.float64)])
+
+
+def static_depth(fm: FamilyMesh, thetas, finaltime=FINALTIME):
+    """Still-water depth at each scenario's highest tide, [S][N]: the part of
+    the maximum depth that the tide alone sets in a sea a hundred times
+    shorter than the tide's wavelength.  The network learns the rest (the
+    river flood, and the sea's departures from the still level)."""
+    wm = max_tide(thetas, finaltime)
+    return np.maximum(wm[:, None] - fm.zc[None, :], 0.0).astype(np.float32)
+
+
+def targets_from(fm: FamilyMesh, thetas, hmax, tarr, finaltime=FINALTIME):
     """Normalised targets [S][N][2]: the maximum depth in excess of the
-    initial depth, and the arrival time."""
+    still-water depth at the highest tide, and the arrival time."""
     t = np.empty(hmax.shape + (2,), np.float32)
-    t[..., 0] = (hmax - initial_depth(fm, thetas)) / DEPTH_SCALE
+    t[..., 0] = (hmax - static_depth(fm, thetas, finaltime)) / DEPTH_SCALE
     t[..., 1] = np.where(tarr >= 0, tarr / finaltime, NEVER)
     return t
 
@@ -139,23 +207,23 @@ def init_params(seed=0):
     W1 = rng.standard_normal((F, H)) * np.sqrt(2.0 / 13)
     W1[13:] = 0.0
     parts = [W1, np.zeros(H), rng.standard_normal((H, H)) * np.sqrt(2.0 / H), np.zeros(H),
+             rng.standard_normal((H, H)) * np.sqrt(2.0 / H), np.zeros(H),
              rng.standard_normal((H, OUT)) * np.sqrt(1.0 / H), np.zeros(OUT)]
     return np.concatenate([p.ravel() for p in parts]).astype(np.float32)
 
 
 def feature_normalisation(fm: FamilyMesh):
     """(mean, inv_std) of the 16 features: parameters by their ranges,
-    bed and coordinates by the mesh, distance by the domain size."""
+    bed, coordinates and distance by the mesh."""
     mu = np.zeros(F, np.float32)
     isd = np.zeros(F, np.float32)
     lo, hi = PARAM_RANGES[:, 0], PARAM_RANGES[:, 1]
     mu[:9] = 0.5 * (lo + hi)
     isd[:9] = 2.0 / (hi - lo)
-    for j, col in ((9, fm.tri[:, 2]), (10, fm.tri[:, 0]), (11, fm.tri[:, 1])):
+    for j, col in ((9, fm.tri[:, 2]), (10, fm.tri[:, 0]), (11, fm.tri[:, 1]),
+                   (12, fm.tri[:, 3])):
         mu[j] = col.mean()
         isd[j] = 1.0 / max(col.std(), 1e-6)
-    mu[12] = 3000.0
-    isd[12] = 1.0 / 2000.0
     return mu, isd
 
 
@@ -169,7 +237,6 @@ class Surrogate:
         self._check(st, None)
         self._h = h
         self._data = None
-        self.set_tensor_path("tcgen05")   # 1.2x the mma.sync inference at 200k x 256 rows
 
     def _check(self, st, h):
         if st != 0:
@@ -199,73 +266,179 @@ class Surrogate:
         self._check(lib().swgpu_mlp_get_params(self._h, _f32p(out)), self._h)
         return out
 
-    def gradients(self, rows, w_depth=1.0, w_arrival=1.0):
+    def gradients(self, rows, w_depth=1.0, w_arrival=1.0, w_error=1.0):
         rows = np.ascontiguousarray(rows, dtype=np.int64)
-        y = np.empty((len(rows), 2), np.float32)
+        y = np.empty((len(rows), OUT), np.float32)
         g = np.empty(lib().swgpu_mlp_num_params(), np.float32)
         loss = np.empty(1, np.float32)
         self._check(lib().swgpu_mlp_gradients(self._h, rows.ctypes.data_as(C.POINTER(C.c_int64)),
-                                              len(rows), w_depth, w_arrival, _f32p(y), _f32p(g),
-                                              _f32p(loss)), self._h)
+                                              len(rows), w_depth, w_arrival, w_error, _f32p(y),
+                                              _f32p(g), _f32p(loss)), self._h)
         return y, float(loss[0]), g
 
-    def fit(self, thetas, targets, steps=2000, batch=16384, lr=2e-3, seed=1,
-            w_depth=1.0, w_arrival=0.25):
-        """Adam training on random (scenario, triangle) rows; returns
-        {"loss", "samples_per_s", "seconds"} (device time)."""
+    def fit(self, thetas, targets, steps=4000, batch=32768, lr=1e-3, seed=1, w_depth=1.0,
+            w_arrival=0.25, w_error=0.25, chunk=250):
+        """Adam training on random (scenario, triangle) rows with a cosine
+        learning-rate decay; returns {"loss", "samples_per_s", "seconds",
+        "tflops"} (device time)."""
         self.set_data(thetas, targets)
         loss = np.empty(1, np.float32)
         ms = np.empty(1, np.float32)
-        done, total_ms, chunk = 0, 0.0, 250
+        done, total_ms = 0, 0.0
         while done < steps:
             n = min(chunk, steps - done)
-            lr_now = lr * 0.5 * (1 + np.cos(np.pi * done / steps))   # cosine decay
+            lr_now = lr * 0.5 * (1 + np.cos(np.pi * done / steps))
             self._check(lib().swgpu_mlp_train(self._h, n, batch, seed + done, float(lr_now),
-                                              w_depth, w_arrival, _f32p(loss), _f32p(ms)),
-                        self._h)
+                                              w_depth, w_arrival, w_error, _f32p(loss),
+                                              _f32p(ms)), self._h)
             total_ms += float(ms[0])
             done += n
+        flop = 3 * 2 * (F * H + 2 * H * H + H * OUT) * batch * steps   # forward + backward
         return {"loss": float(loss[0]), "samples_per_s": steps * batch / (total_ms / 1000.0),
-                "seconds": total_ms / 1000.0, "steps": steps, "batch": batch}
+                "seconds": total_ms / 1000.0, "steps": steps, "batch": batch,
+                "tflops": flop / (total_ms / 1000.0) / 1e12}
 
-    def set_tensor_path(self, path):
-        """Inference on "mma.sync" (default) or "tcgen05" tensor cores."""
-        code = {"mma.sync": 0, "tcgen05": 1}[path]
-        self._check(lib().swgpu_mlp_set_tensor_path(self._h, code), self._h)
-
-    def predict(self, thetas):
-        """(max_depth [S][N], arrival [S][N] (-1: never), device ms) for the
-        parameter vectors."""
+    def predict_raw(self, thetas):
+        """Network outputs [S][N][3] and device milliseconds."""
         import torch  # device buffer for the outputs
         self.set_data(thetas)
         S, N = len(thetas), self.fm.N
-        out = torch.empty((S * N, 2), dtype=torch.float32, device="cuda")
+        out = torch.empty((S * N, OUT), dtype=torch.float32, device="cuda")
         ms = np.empty(1, np.float32)
         self._check(lib().swgpu_mlp_predict(self._h, 0, S * N, C.c_void_p(out.data_ptr()),
                                             _f32p(ms)), self._h)
-        y = out.cpu().numpy().reshape(S, N, 2)
-        depth = np.maximum(initial_depth(self.fm, thetas) + y[..., 0] * DEPTH_SCALE, 0.0)
-        arr = np.where(y[..., 1] > 0.5 * (1.0 + NEVER), -1.0, np.clip(y[..., 1], 0, 1))
-        return depth, arr, float(ms[0])
+        return out.cpu().numpy().reshape(S, N, OUT), float(ms[0])
+
+    def predict(self, thetas):
+        """(max_depth [S][N], arrival [S][N] (-1: never), estimated absolute
+        depth error [S][N] in m, device ms)."""
+        y, ms = self.predict_raw(thetas)
+        depth = np.maximum(static_depth(self.fm, thetas) + y[..., 0] * DEPTH_SCALE, 0.0)
+        arr = np.where(y[..., 1] > 0.5 * (1.0 + NEVER), -1.0,
+                       np.clip(y[..., 1], 0, 1) * FINALTIME)
+        err = np.maximum(y[..., 2], 0.0) * DEPTH_SCALE
+        return depth, arr, err, ms
 
 
-def fallback_report(pred_depth, true_depth, solver_ms_per_scenario, infer_ms, tol=0.05,
-                    block=ALIGN):
-    """Blocks of ``block`` triangles whose max-depth error exceeds ``tol``;
-    scenarios with any such block are rerun by the solver."""
-    S, N = true_depth.shape
+# ---- the solver as fallback ----------------------------------------------------
+
+def block_index(N, block=ALIGN):
+    """Block of each triangle (blocks of ``block`` consecutive triangles of
+    the mesh's Morton order)."""
+    return np.arange(N) // block
+
+
+def _block_max(a, block=ALIGN):
+    S, N = a.shape
     nb = (N + block - 1) // block
     pad = nb * block - N
-    err = np.abs(np.asarray(pred_depth) - np.asarray(true_depth))
     if pad:
-        err = np.concatenate([err, np.zeros((S, pad), err.dtype)], axis=1)
-    berr = err.reshape(S, nb, block).max(axis=2)
-    bad = berr > tol
-    rerun = bad.any(axis=1)
-    t_fallback = infer_ms + rerun.sum() * solver_ms_per_scenario
-    t_solver = S * solver_ms_per_scenario
-    return {"blocks_over_tol_pct": 100.0 * bad.mean(), "scenarios_rerun": int(rerun.sum()),
-            "scenarios": S, "max_abs_error_m": float(err.max()),
-            "mean_abs_error_m": float(np.abs(np.asarray(pred_depth) - true_depth).mean()),
-            "time_to_answer_ms": float(t_fallback), "solver_only_ms": float(t_solver),
-            "gain": float(t_solver / t_fallback) if t_fallback > 0 else None}
+        a = np.concatenate([a, np.zeros((S, pad), a.dtype)], axis=1)
+    return a.reshape(S, nb, block).max(axis=2)
+
+
+def calibrate(err_est, err_true, tol=0.05, miss_rate=0.01, block=ALIGN):
+    """Scale k of the error estimate such that, over these (calibration)
+    scenarios, at most ``miss_rate`` of the blocks whose true maximum depth
+    error exceeds ``tol`` have k * (estimated block maximum) <= tol, i.e. go
+    unflagged.  Returns (k, stats)."""
+    est = _block_max(np.asarray(err_est, np.float64), block).ravel()
+    tru = _block_max(np.asarray(err_true, np.float64), block).ravel()
+    bad = tru > tol
+    if not bad.any():
+        return 1.0, {"bad_blocks": 0, "blocks": int(est.size)}
+    # flagged when k * est > tol: the bad blocks with the smallest estimates
+    # decide k
+    q = np.quantile(est[bad], miss_rate)
+    k = tol / max(q, 1e-9)
+    return float(k), {"bad_blocks": int(bad.sum()), "blocks": int(est.size),
+                      "flagged_frac": float((k * est > tol).mean())}
+
+
+def band_mesh(fm: FamilyMesh, ylo, yhi):
+    """The sub-mesh of triangles with centroid y in [ylo, yhi]: (mesh, vertex
+    bed, family index of each sub-mesh triangle).  Boundary edges keep their
+    family tags; the cut edges are reflective walls ("exterior")."""
+    idx = np.nonzero((fm.xy[:, 1] >= ylo) & (fm.xy[:, 1] <= yhi))[0]
+    local = -np.ones(fm.N, np.int64)
+    local[idx] = np.arange(len(idx))
+    bnd = {}
+    fam = fm.mesh.boundary
+    for (k, e), tag in fam.items():
+        if local[k] >= 0:
+            bnd[(int(local[k]), e)] = tag
+    sub = Mesh(fm.mesh.points, fm.mesh.triangles[idx], bnd)
+    fam_idx = idx[sub.permutation]
+    return sub, fm.elevation_vertex[fam_idx], fam_idx
+
+
+def band_scenarios(fm: FamilyMesh, thetas, flagged, margin=1000.0, quantum=500.0,
+                   block=ALIGN, cache=None):
+    """For each scenario with flagged blocks ([S][nblocks] bool): its band
+    (y range of the flagged blocks and the inflow segment, widened by
+    ``margin`` and rounded outward to ``quantum``) as (scenario index,
+    Scenario, family index).  Sub-meshes are cached by band."""
+    cache = {} if cache is None else cache
+    blk = block_index(fm.N, block)
+    out = []
+    for s in np.nonzero(np.asarray(flagged).any(axis=1))[0]:
+        tri = np.isin(blk, np.nonzero(flagged[s])[0])
+        y = fm.xy[tri, 1]
+        lo = min(float(y.min()), fm.inflow_y[0]) - margin
+        hi = max(float(y.max()), fm.inflow_y[1]) + margin
+        lo = max(0.0, np.floor(lo / quantum) * quantum)
+        hi = min(fm.length, np.ceil(hi / quantum) * quantum)
+        key = (lo, hi)
+        if key not in cache:
+            cache[key] = band_mesh(fm, lo, hi)
+        sub, zv, fam_idx = cache[key]
+        out.append((int(s), family_scenario(fm, thetas[s], FINALTIME, sub, zv), fam_idx))
+    return out
+
+
+def fallback(fm: FamilyMesh, thetas, depth, err_est, k, tol=0.05, margin=1000.0, batch=32,
+             block=ALIGN, precision="mixed"):
+    """The answer within ``tol``: predictions where the calibrated error
+    estimate allows, band re-solves elsewhere.  Returns (depth [S][N],
+    flagged blocks [S][nblocks], solver device ms, band triangles solved)."""
+    est = _block_max(np.asarray(err_est, np.float64), block)
+    flagged = k * est > tol
+    answer = np.array(depth, np.float32, copy=True)
+    bands = band_scenarios(fm, thetas, flagged, margin=margin, block=block)
+    blk = block_index(fm.N, block)
+    ms, tri_solved = 0.0, 0
+    for b0 in range(0, len(bands), batch):
+        part = bands[b0:b0 + batch]
+        out, t = _run([sc for _, sc, _ in part], FINALTIME, THRESHOLD, precision)
+        ms += t
+        for (s, sc, fam_idx), (hm, _ta) in zip(part, out):
+            tri_solved += sc.N
+            take = flagged[s][blk[fam_idx]]
+            answer[s, fam_idx[take]] = hm[take]
+    return answer, flagged, ms, tri_solved
+
+
+def evaluate(fm: FamilyMesh, thetas, true_depth, solver_ms, pred_depth, err_est, infer_ms, k,
+             tol=0.05, margin=1000.0, block=ALIGN):
+    """Time to an answer within ``tol`` (inference + band re-solves, device
+    time) against the solver alone on the same scenarios, and the answer's
+    error against the full solve."""
+    answer, flagged, band_ms, tri_solved = fallback(fm, thetas, pred_depth, err_est, k, tol,
+                                                    margin, block=block)
+    true_depth = np.asarray(true_depth, np.float64)
+    err_pred = _block_max(np.abs(np.asarray(pred_depth) - true_depth), block)
+    err_ans = _block_max(np.abs(answer - true_depth), block)
+    t_answer = infer_ms + band_ms
+    S = len(thetas)
+    return {"scenarios": S, "tol_m": tol,
+            "blocks_flagged_pct": 100.0 * float(flagged.mean()),
+            "scenarios_with_band_solve": int(flagged.any(axis=1).sum()),
+            "band_triangle_fraction": tri_solved / float(S * fm.N),
+            "prediction_mean_abs_error_m": float(np.abs(pred_depth - true_depth).mean()),
+            "prediction_max_abs_error_m": float(err_pred.max()),
+            "prediction_blocks_over_tol_pct": 100.0 * float((err_pred > tol).mean()),
+            "answer_max_abs_error_m": float(err_ans.max()),
+            "answer_blocks_over_tol_pct": 100.0 * float((err_ans > tol).mean()),
+            "inference_ms": float(infer_ms), "band_solve_ms": float(band_ms),
+            "time_to_answer_ms": float(t_answer), "solver_only_ms": float(solver_ms),
+            "gain": float(solver_ms / t_answer) if t_answer > 0 else None}

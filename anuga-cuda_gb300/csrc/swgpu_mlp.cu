@@ -1,23 +1,40 @@
-// swgpu_mlp.cu -- BF16 tensor-core MLP surrogate of the solver's maximum
-// depth and arrival time.
+// swgpu_mlp.cu -- BF16 surrogate network of the solver's maximum depth and
+// arrival time, on the 5th-generation tensor cores (tcgen05, TMEM).
 //
 // Rows are (scenario s, triangle k) pairs.  Each row's 16 input features
-// are assembled on the fly: the scenario's 9 parameters, the triangle's bed
-// elevation, centroid x and y, its distance to the scenario's source
-// (parameters 1 and 2), and 3 zeros; each is normalised by a per-feature
-// affine map.  The network is 16 -> 128 -> 128 -> 2 with ReLU, weights and
-// activations in BF16, every product accumulated in FP32 by
-// mma.sync.m16n8k16 (one warp = 16 rows; a layer's FP32 accumulator
-// fragments are re-packed in registers as the next layer's BF16 A
-// fragments, so activations never leave the register file in inference).
-// Training keeps FP32 master weights (Adam); a step is one fused
-// forward/backward kernel over a random batch, an FP32 weight-gradient
-// reduction over the batch and the Adam update.
+// are assembled on the fly: the scenario's 9 parameters, the triangle's
+// centroid x and y, bed elevation and distance to the inflow, and 3 zeros,
+// each normalised by a per-feature affine map.  The network is
+//   16 -> 256 -> 256 -> 256 -> 3  (ReLU after each hidden layer)
+// with weights and activations in BF16 and every product accumulated in
+// FP32; its outputs are the normalised maximum depth, the normalised
+// arrival time and an estimate of the first output's absolute error.
+//
+// Every GEMM of the forward and backward passes is the one kernel
+// tc_gemm: a CTA of 4 warps computes a 128 x N tile (N = 256 or 16) of
+// A (M x K) times B (N x K)^T, both operands K-major in global memory.
+// Chunks of 64 along K are staged by cp.async into shared memory in the
+// canonical K-major no-swizzle layout (8-row x 16-byte core matrices, 128
+// bytes apart along K, (K/8)*128 bytes apart along M/N), double-buffered;
+// one thread issues the chunk's tcgen05.mma (kind::f16, M = 128) into an
+// FP32 accumulator in tensor memory and commits it to the stage's
+// mbarrier, which frees the stage for the chunk after next.  The epilogue
+// reads each warp's 32 TMEM lanes (its 32 rows) with tcgen05.ld and either
+//  * adds the bias, applies ReLU and stores BF16 activations (a hidden
+//    layer of the forward pass),
+//  * multiplies by the ReLU mask of the previous activations and stores
+//    BF16 gradients (the backward pass through a layer), or
+//  * adds the FP32 partial weight gradient of its slice of the batch into
+//    the gradient vector (split over the batch, K = rows).
+// Activations and gradients are stored row-major (rows x features) for the
+// next layer's A operand and, in training, also feature-major (features x
+// rows) for the weight gradients, whose K is the batch.  The 256 -> 3
+// output layer and its gradient run on the CUDA cores (head kernels).
+// Training keeps FP32 master weights updated by Adam.
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cstdarg>
-
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -27,245 +44,149 @@
 
 namespace {
 
-constexpr int kF = 16;      // input features (13 used)
-constexpr int kH = 128;     // hidden units per layer
-constexpr int kOut = 2;     // outputs: max depth, arrival time (normalised)
-constexpr int kParams = 9;  // scenario parameters
-constexpr int kS1 = 24;     // smem row strides (elements) with padding against bank conflicts
-constexpr int kS2 = 136;
-constexpr int kWarps = 8;   // warps per block, 16 rows each
-constexpr int kRowsPerBlock = 16 * kWarps;
+constexpr int kF = 16;       // input features (13 used)
+constexpr int kH = 256;      // hidden units per layer
+constexpr int kOut = 3;      // outputs: depth, arrival time, depth-error estimate
+constexpr int kTargets = 2;  // targets per row: depth, arrival time
+constexpr int kParams = 9;   // scenario parameters
+constexpr int kTri = 4;      // per-triangle table: x, y, z, distance to the inflow
 
-// flat FP32 parameter vector: W1 [16][128] (in-major), b1, W2 [128][128],
-// b2, W3 [128][2], b3
-constexpr int kOffW1 = 0;
-constexpr int kOffB1 = kOffW1 + kF * kH;
-constexpr int kOffW2 = kOffB1 + kH;
-constexpr int kOffB2 = kOffW2 + kH * kH;
-constexpr int kOffW3 = kOffB2 + kH;
-constexpr int kOffB3 = kOffW3 + kH * kOut;
-constexpr int kNumParams = kOffB3 + kOut;
+// flat FP32 parameter vector, weights in-major ([in][out]):
+// W1 [16][256], b1, W2 [256][256], b2, W3 [256][256], b3, W4 [256][3], b4
+constexpr long kOffW1 = 0;
+constexpr long kOffB1 = kOffW1 + kF * kH;
+constexpr long kOffW2 = kOffB1 + kH;
+constexpr long kOffB2 = kOffW2 + kH * kH;
+constexpr long kOffW3 = kOffB2 + kH;
+constexpr long kOffB3 = kOffW3 + kH * kH;
+constexpr long kOffW4 = kOffB3 + kH;
+constexpr long kOffB4 = kOffW4 + kH * kOut;
+constexpr long kNumParams = kOffB4 + kOut;
 
-// BF16 weight images in the layouts the mma B fragments read
+// BF16 weight images in the layouts the GEMMs read as their B operand
+// (N x K, K contiguous): forward layers need W^T ([out][in]), the backward
+// pass through a layer needs W itself ([in][out]).
 struct BfWeights {
-    __nv_bfloat16 w1t[kH * kS1];  // [out][in]
-    __nv_bfloat16 w2t[kH * kS2];  // [out][in]
-    __nv_bfloat16 w2[kH * kS2];   // [in][out] (backward)
-    __nv_bfloat16 w3t[8 * kS2];   // [out (2 used)][in]
-    __nv_bfloat16 w3[kH * 8];     // [in][out] (backward, 2 used)
-    float b1[kH], b2[kH], b3[8];
+    __nv_bfloat16 wt1[kH * kF];   // [out][in]
+    __nv_bfloat16 wt2[kH * kH];
+    __nv_bfloat16 wt3[kH * kH];
+    __nv_bfloat16 w2[kH * kH];    // [in][out]
+    __nv_bfloat16 w3[kH * kH];
+    __nv_bfloat16 w4[kH * kOut];  // [in][out] (head, CUDA cores)
 };
 
-__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
-}
-__device__ __forceinline__ float2 unpack2(uint32_t u) {
-    __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162 *>(&u);
-    return __bfloat1622float2(v);
-}
-__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16 *p) {
-    return *reinterpret_cast<const uint32_t *>(p);
-}
-// D += A(16x16, row) * B(16x8, col), BF16 in, FP32 accumulate
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
-                                         uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-        "{%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
+// ---- features --------------------------------------------------------------
 
 struct FeatureTables {
     const float *scen;   // [S][9]
-    const float *tri;    // [N][3]: x, y, z
+    const float *tri;    // [N][4]: x, y, z, distance to the inflow
     const float *mu;     // [16]
     const float *isd;    // [16]
     long long N;
 };
 
-__device__ __forceinline__ float raw_feature(int c, const float *th, float x, float y, float z) {
+__device__ __forceinline__ float raw_feature(int c, const float *th, const float *tr) {
     if (c < kParams) return th[c];
-    if (c == 9) return z;
-    if (c == 10) return x;
-    if (c == 11) return y;
-    if (c == 12) {
-        const float dx = x - th[1], dy = y - th[2];
-        return sqrtf(dx * dx + dy * dy);
-    }
+    if (c == 9) return tr[2];   // bed
+    if (c == 10) return tr[0];  // x
+    if (c == 11) return tr[1];  // y
+    if (c == 12) return tr[3];  // distance to the inflow
     return 0.0f;
 }
 
-// The A fragment of one warp's 16 rows: row g and g+8 of the tile (rows
-// r0 + g, r0 + g + 8), columns 2t, 2t+1, 2t+8, 2t+9 (g = lane/4, t = lane%4).
-__device__ __forceinline__ void load_features(const FeatureTables &F, long long row_a,
-                                              long long row_b, bool va, bool vb,
-                                              uint32_t (&a)[4]) {
-    const int lane = threadIdx.x & 31, t = lane & 3;
-    float v[2][4];
-    const long long rows[2] = {row_a, row_b};
-    const bool valid[2] = {va, vb};
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int cols[4] = {2 * t, 2 * t + 1, 2 * t + 8, 2 * t + 9};
-        if (!valid[h]) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) v[h][j] = 0.0f;
-            continue;
-        }
-        const long long s = rows[h] / F.N, k = rows[h] - s * F.N;
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Row of batch position r: given (rows), drawn uniformly from all (scenario,
+// triangle) pairs (seeded), or row0 + r (inference).
+__device__ __forceinline__ long long batch_row(const long long *rows, unsigned long long seed,
+                                               long long r, long long total, long long row0) {
+    if (rows) return rows[r];
+    if (total > 0)
+        return (long long)(mix64(seed ^ (unsigned long long)r * 0xD1B54A32D192ED03ull) %
+                           (unsigned long long)total);
+    return row0 + r;
+}
+
+// Normalised BF16 features of batch rows [0, nrows): row-major xr [Bp][16]
+// and (training) feature-major xc [16][Bp]; rows nrows..Bp-1 are zero.
+// Also records each batch row's data row (training targets).
+__global__ void __launch_bounds__(256) mlp_features(FeatureTables F, const long long *rows,
+                                                    unsigned long long seed, long long total,
+                                                    long long row0, long long nrows, long long Bp,
+                                                    __nv_bfloat16 *__restrict__ xr,
+                                                    __nv_bfloat16 *__restrict__ xc,
+                                                    long long *__restrict__ row_of) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= Bp) return;
+    float v[kF];
+    if (r < nrows) {
+        const long long q = batch_row(rows, seed, r, total, row0);
+        if (row_of) row_of[r] = q;
+        const long long s = q / F.N, k = q - s * F.N;
         const float *th = F.scen + s * kParams;
-        const float x = F.tri[3 * k], y = F.tri[3 * k + 1], z = F.tri[3 * k + 2];
+        const float *tr = F.tri + k * kTri;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int c = cols[j];
-            v[h][j] = (raw_feature(c, th, x, y, z) - F.mu[c]) * F.isd[c];
-        }
+        for (int c = 0; c < kF; c++) v[c] = (raw_feature(c, th, tr) - F.mu[c]) * F.isd[c];
+    } else {
+#pragma unroll
+        for (int c = 0; c < kF; c++) v[c] = 0.0f;
     }
-    a[0] = pack2(v[0][0], v[0][1]);
-    a[1] = pack2(v[1][0], v[1][1]);
-    a[2] = pack2(v[0][2], v[0][3]);
-    a[3] = pack2(v[1][2], v[1][3]);
-}
-
-// One hidden layer over a warp's 16 rows: acc[j] = bias + A x W^T for the
-// 16 n-tiles of 8 units; then ReLU and re-pack as 8 A fragments (k-steps).
-template <int KSTEPS, int STRIDE>
-__device__ __forceinline__ void hidden_layer(const uint32_t (*a)[4], const __nv_bfloat16 *wt,
-                                             const float *bias, uint32_t (&out)[8][4]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __align__(16) __nv_bfloat16 b[kF];
 #pragma unroll
-    for (int jj = 0; jj < 8; jj++) {  // pairs of n-tiles -> one k-step of the next layer
-        float acc[2][4];
+    for (int c = 0; c < kF; c++) b[c] = __float2bfloat16(v[c]);
+    int4 *dst = reinterpret_cast<int4 *>(xr + r * kF);
+    dst[0] = reinterpret_cast<const int4 *>(b)[0];
+    dst[1] = reinterpret_cast<const int4 *>(b)[1];
+    if (xc) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int j = 2 * jj + h;
-            const float bl = bias[8 * j + 2 * t], bh = bias[8 * j + 2 * t + 1];
-            acc[h][0] = bl;
-            acc[h][1] = bh;
-            acc[h][2] = bl;
-            acc[h][3] = bh;
-            const __nv_bfloat16 *col = wt + (8 * j + g) * STRIDE;
-#pragma unroll
-            for (int kk = 0; kk < KSTEPS; kk++)
-                mma16816(acc[h], a[kk], lds32(col + 16 * kk + 2 * t),
-                         lds32(col + 16 * kk + 8 + 2 * t));
-        }
-        out[jj][0] = pack2(fmaxf(acc[0][0], 0.f), fmaxf(acc[0][1], 0.f));
-        out[jj][1] = pack2(fmaxf(acc[0][2], 0.f), fmaxf(acc[0][3], 0.f));
-        out[jj][2] = pack2(fmaxf(acc[1][0], 0.f), fmaxf(acc[1][1], 0.f));
-        out[jj][3] = pack2(fmaxf(acc[1][2], 0.f), fmaxf(acc[1][3], 0.f));
+        for (int c = 0; c < kF; c++) xc[c * Bp + r] = b[c];
     }
 }
 
-// Output layer: the one n-tile whose columns 0 and 1 are the outputs.
-__device__ __forceinline__ void output_layer(const uint32_t (&a)[8][4], const BfWeights &W,
-                                             float (&y)[4]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    y[0] = y[2] = W.b3[2 * t];
-    y[1] = y[3] = W.b3[2 * t + 1];
-    const __nv_bfloat16 *col = W.w3t + g * kS2;
-#pragma unroll
-    for (int kk = 0; kk < 8; kk++)
-        mma16816(y, a[kk], lds32(col + 16 * kk + 2 * t), lds32(col + 16 * kk + 8 + 2 * t));
+// ---- tcgen05 GEMM ----------------------------------------------------------
+
+constexpr int kTileM = 128;  // rows per CTA (TMEM lanes)
+constexpr int kChunkK = 64;  // K per stage
+constexpr int kGemmThreads = 128;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
 }
 
-__device__ void load_weights(BfWeights &dst, const BfWeights *src) {
-    const int n = (int)(sizeof(BfWeights) / 16);
-    const int4 *s = reinterpret_cast<const int4 *>(src);
-    int4 *d = reinterpret_cast<int4 *>(&dst);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
-    __syncthreads();
-}
-
-// ---- inference -----------------------------------------------------------
-__global__ void __launch_bounds__(32 * kWarps) mlp_predict(FeatureTables F, const BfWeights *gw,
-                                                           long long row0, long long nrows,
-                                                           float *__restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    BfWeights &W = *reinterpret_cast<BfWeights *>(smem);
-    load_weights(W, gw);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    for (long long base = (long long)blockIdx.x * kRowsPerBlock; base < nrows;
-         base += (long long)gridDim.x * kRowsPerBlock) {
-        const long long ra = base + 16 * warp + g, rb = ra + 8;
-        uint32_t x[1][4];
-        load_features(F, row0 + ra, row0 + rb, ra < nrows, rb < nrows, x[0]);
-        uint32_t a1[8][4], a2[8][4];
-        hidden_layer<1, kS1>(x, W.w1t, W.b1, a1);
-        hidden_layer<8, kS2>(a1, W.w2t, W.b2, a2);
-        float y[4];
-        output_layer(a2, W, y);
-        if (t == 0) {
-            if (ra < nrows) {
-                out[2 * ra] = y[0];
-                out[2 * ra + 1] = y[1];
-            }
-            if (rb < nrows) {
-                out[2 * rb] = y[2];
-                out[2 * rb + 1] = y[3];
-            }
-        }
-    }
-}
-
-// ---- inference on the 5th-generation tensor cores (tcgen05, TMEM) --------
-//
-// A CTA of 4 warps takes tiles of 128 rows.  Layer 1 (K = 16) and layer 2
-// (K = 128) are each one 128 x 128 tcgen05.mma chain issued by one thread:
-// A (activations) and B (weights, N x K) in shared memory in the canonical
-// K-major layout without swizzle (8-row x 16-byte core matrices, adjacent
-// along K 128 bytes apart, along M/N (K/8)*128 bytes apart), the FP32
-// accumulators in tensor memory (256 columns: layer 1 in 0..127, layer 2 in
-// 128..255).  Completion is signalled through tcgen05.commit on an
-// mbarrier; warp w then reads TMEM lanes 32w..32w+31 (its rows) with
-// tcgen05.ld, applies bias and ReLU, and writes the next layer's A tile, or
-// for layer 2 evaluates the 128 -> 2 output layer on the CUDA cores.
-
-constexpr int kTcRows = 128;
-
-struct __align__(1024) TcSmem {
-    __nv_bfloat16 a1[kTcRows * kF];   // layer-1 A: 128 x 16
-    __nv_bfloat16 b1[kH * kF];        // W1 as N x K: 128 x 16
-    __nv_bfloat16 a2[kTcRows * kH];   // layer-2 A: 128 x 128
-    __nv_bfloat16 b2[kH * kH];        // W2 as N x K: 128 x 128
-    float w3[kH * 2], bias1[kH], bias2[kH], bias3[2];
-    unsigned long long bar;
-    unsigned tmem_base;
-};
-
-// Byte offset of element (r, k) of an R x K K-major tile in the canonical
-// no-swizzle layout.
-__host__ __device__ __forceinline__ unsigned canon_offset(int r, int k, int K) {
-    return (unsigned)((r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
-__device__ __forceinline__ unsigned long long smem_desc(const void *p, unsigned lbo,
+// Shared-memory matrix descriptor: start, leading-dimension byte offset
+// (between core matrices along K), stride byte offset (between 8-row groups
+// along M/N), descriptor version 1 (bit 46), no swizzle.
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr, unsigned lbo,
                                                         unsigned sbo) {
-    const unsigned addr = (unsigned)__cvta_generic_to_shared(p);
     return (unsigned long long)((addr >> 4) & 0x3FFFu) |
            ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
            ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
 // kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both
-// K-major, N = 128, M = 128.
-constexpr unsigned kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) |
-                              ((128u >> 4) << 24);
+// K-major, M = 128, N given.
+__host__ __device__ constexpr unsigned tc_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) |
+           ((unsigned)(kTileM >> 4) << 24);
+}
 
 __device__ __forceinline__ void tc_mma(unsigned d_tmem, unsigned long long a,
-                                       unsigned long long b, bool accumulate) {
+                                       unsigned long long b, unsigned idesc, bool accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(kTcIdesc), "r"((unsigned)accumulate)
+        "l"(a), "l"(b), "r"(idesc), "r"((unsigned)accumulate)
         : "memory");
 }
 __device__ __forceinline__ void tc_commit(unsigned long long *bar) {
     asm volatile(
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            (unsigned)__cvta_generic_to_shared(bar))
+            smem_u32(bar))
         : "memory");
 }
 __device__ __forceinline__ void tc_fence_after() {
@@ -294,11 +215,23 @@ __device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
 #pragma unroll
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld16(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+        "%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
 
-__device__ __forceinline__ void mbar_init_tc(unsigned long long *bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
-                     (unsigned)__cvta_generic_to_shared(bar))
-                 : "memory");
+__device__ __forceinline__ void mbar_init(unsigned long long *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 __device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned parity) {
@@ -307,454 +240,384 @@ __device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned pari
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"((unsigned)__cvta_generic_to_shared(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     return ok != 0;
 }
 constexpr int kTcWaitLimit = 1 << 22;
-// bounded wait for the MMA chain; false after kTcWaitLimit polls
-__device__ __forceinline__ bool tc_wait(unsigned long long *bar, unsigned parity) {
-    for (int i = 0; i < kTcWaitLimit; i++)
-        if (mbar_test(bar, parity)) return true;
-    return false;
+// Bounded wait of the whole CTA for an MMA commit: every thread polls at
+// most kTcWaitLimit times; true when all saw the phase complete.
+__device__ __forceinline__ bool cta_wait(unsigned long long *bar, unsigned parity) {
+    bool ok = false;
+    for (int i = 0; i < kTcWaitLimit && !ok; i++) ok = mbar_test(bar, parity);
+    return __syncthreads_and(ok) != 0;
 }
 
-__global__ void __launch_bounds__(128, 1) mlp_predict_tc(FeatureTables F, const float *params,
-                                                         long long row0, long long nrows,
-                                                         float *__restrict__ out,
-                                                         int *__restrict__ status) {
+// 16-byte asynchronous copy global -> shared; src_bytes 0 fills zeros.
+__device__ __forceinline__ void cp_async16(unsigned dst, const void *src, unsigned src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
+                 "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Stages rows [r0, r0 + R) x k-range [k0, k0 + kc) of a K-major matrix
+// (row stride ld elements, nvalid valid rows) into the canonical layout at
+// smem address dst.  Vector v (8 elements) goes to byte 16 v: the 8 lanes
+// of a group take 8 consecutive rows at one k (a 128-byte core matrix),
+// consecutive groups the next k, so a warp stores 512 contiguous bytes and
+// reads 64 contiguous bytes of each of 8 rows.
+__device__ __forceinline__ void stage_operand(unsigned dst, const __nv_bfloat16 *src, long ld,
+                                              long long r0, long long nvalid, int R, long k0,
+                                              int kc) {
+    const int kvn = kc >> 3;       // 16-byte vectors per row in the chunk
+    const int nvec = R * kvn;
+    for (int v = threadIdx.x; v < nvec; v += kGemmThreads) {
+        const int r = (v & 7) + 8 * (v / (8 * kvn));
+        const int kv = (v >> 3) % kvn;
+        const long long row = r0 + r;
+        const bool in = row < nvalid;
+        const __nv_bfloat16 *p = in ? src + row * ld + k0 + 8 * kv : src;
+        cp_async16(dst + 16u * (unsigned)v, p, in ? 16u : 0u);
+    }
+}
+
+enum { kEpiHidden = 0, kEpiDgrad = 1, kEpiWgrad = 2, kEpiWgradT = 3 };
+
+struct GemmArgs {
+    const __nv_bfloat16 *A;  // M x K, K contiguous, row stride lda
+    long lda;
+    const __nv_bfloat16 *B;  // N x K, K contiguous, row stride ldb
+    long ldb;
+    long long M;             // valid rows of A (and of the output)
+    long K;                  // K of the whole product (a multiple of 16)
+    long k_per_split;        // K range of one blockIdx.y (a multiple of 64, or K)
+    // epilogue
+    const float *bias;               // hidden: [N]
+    const __nv_bfloat16 *mask;       // dgrad: previous activations [M][N] row-major
+    __nv_bfloat16 *out_row;          // hidden/dgrad: [M][N]
+    __nv_bfloat16 *out_col;          // hidden/dgrad: [N][ldc] (may be null)
+    long ldc;
+    float *grad;                     // wgrad: [M][N] (or [N][M] transposed)
+    int *status;
+};
+
+template <int N>
+struct __align__(1024) GemmSmem {
+    __nv_bfloat16 a[2][kTileM * kChunkK];
+    __nv_bfloat16 b[2][N * kChunkK];
+    unsigned long long bar[2];
+    unsigned tmem_base;
+};
+
+template <int N>
+__host__ __device__ constexpr int tmem_cols() {
+    return N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+}
+
+// The epilogue of one 32-column slice c0 .. c0+31 (or 16 for N = 16) of
+// this thread's row.
+template <int N, int EPI, int W>
+__device__ __forceinline__ void gemm_epilogue(const GemmArgs &g, long long row, int c0,
+                                              const float (&v)[W]) {
+    if (row >= g.M) return;
+    if (EPI == kEpiWgrad) {
+#pragma unroll
+        for (int j = 0; j < W; j++) atomicAdd(&g.grad[row * N + c0 + j], v[j]);
+        return;
+    }
+    if (EPI == kEpiWgradT) {
+#pragma unroll
+        for (int j = 0; j < W; j++) atomicAdd(&g.grad[(long long)(c0 + j) * g.M + row], v[j]);
+        return;
+    }
+    __align__(16) __nv_bfloat16 o[W];
+    if (EPI == kEpiHidden) {
+#pragma unroll
+        for (int j = 0; j < W; j++) o[j] = __float2bfloat16(fmaxf(v[j] + g.bias[c0 + j], 0.0f));
+    } else {  // dgrad: the ReLU mask of the activations this layer read
+        __align__(16) __nv_bfloat16 pm[W];
+        const int4 *src = reinterpret_cast<const int4 *>(g.mask + row * N + c0);
+#pragma unroll
+        for (int q = 0; q < W / 8; q++) reinterpret_cast<int4 *>(pm)[q] = src[q];
+#pragma unroll
+        for (int j = 0; j < W; j++)
+            o[j] = __float2bfloat16(__bfloat162float(pm[j]) > 0.0f ? v[j] : 0.0f);
+    }
+    int4 *dst = reinterpret_cast<int4 *>(g.out_row + row * N + c0);
+#pragma unroll
+    for (int q = 0; q < W / 8; q++) dst[q] = reinterpret_cast<const int4 *>(o)[q];
+    if (g.out_col) {
+#pragma unroll
+        for (int j = 0; j < W; j++) g.out_col[(long long)(c0 + j) * g.ldc + row] = o[j];
+    }
+}
+
+// C (128 x N tile) = A (tile rows) x B^T over this CTA's K range, then the
+// epilogue.  blockIdx.x: row tile; blockIdx.y: K split (weight gradients).
+template <int N, int EPI>
+__global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm(GemmArgs g) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte aligned view of the dynamic shared memory
-    TcSmem &T = *reinterpret_cast<TcSmem *>(
-        smem_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 1023u)) & 1023u));
+    GemmSmem<N> &S = *reinterpret_cast<GemmSmem<N> *>(
+        smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // weights into the canonical layouts (BF16) and FP32 biases
-    for (int e = tid; e < kH * kF; e += 128) {
-        const int n = e / kF, k = e % kF;  // W1 [in k][out n]
-        *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(T.b1) +
-                                           canon_offset(n, k, kF)) =
-            __float2bfloat16(params[kOffW1 + k * kH + n]);
-    }
-    for (int e = tid; e < kH * kH; e += 128) {
-        const int n = e / kH, k = e % kH;  // W2 [in k][out n]
-        *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(T.b2) +
-                                           canon_offset(n, k, kH)) =
-            __float2bfloat16(params[kOffW2 + k * kH + n]);
-    }
-    for (int e = tid; e < kH * 2; e += 128)  // W3 rounded like the other weights
-        T.w3[e] = __bfloat162float(__float2bfloat16(params[kOffW3 + e]));
-    for (int e = tid; e < kH; e += 128) {
-        T.bias1[e] = params[kOffB1 + e];
-        T.bias2[e] = params[kOffB2 + e];
-    }
-    if (tid < 2) T.bias3[tid] = params[kOffB3 + tid];
+    const long long m0 = (long long)blockIdx.x * kTileM;
+    const long kb = (long)blockIdx.y * g.k_per_split;
+    const long ke = g.K < kb + g.k_per_split ? g.K : kb + g.k_per_split;
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-                         (unsigned)__cvta_generic_to_shared(&T.tmem_base))
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&S.tmem_base)),
+                     "n"(tmem_cols<N>())
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0) mbar_init_tc(&T.bar);
+    if (tid == 0) {
+        mbar_init(&S.bar[0]);
+        mbar_init(&S.bar[1]);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const unsigned tmem = T.tmem_base;
-    const unsigned d1 = tmem, d2 = tmem + 128u;              // column offsets
-    const unsigned lane_base = (unsigned)(32 * warp) << 16;  // this warp's TMEM lanes
-    unsigned parity = 0u;
+    const unsigned tmem = S.tmem_base;
+    const int kc = g.K < kChunkK ? (int)g.K : kChunkK;  // 64, or 16 for K = 16
+    const int nk = (int)((ke - kb + kc - 1) / kc);
+    constexpr unsigned idesc = tc_idesc(N);
+    auto issue = [&](int c) {
+        const int s = c & 1;
+        const long k0 = kb + (long)c * kc;
+        stage_operand(smem_u32(S.a[s]), g.A, g.lda, m0, g.M, kTileM, k0, kc);
+        stage_operand(smem_u32(S.b[s]), g.B, g.ldb, 0, N, N, k0, kc);
+        cp_async_commit();
+    };
     bool ok = true;
-    for (long long base = (long long)blockIdx.x * kTcRows; base < nrows && ok;
-         base += (long long)gridDim.x * kTcRows) {
-        const long long r = base + tid;  // this thread's row
-        const bool valid = r < nrows;
-        // ---- layer-1 A: the row's 16 normalised features
-        {
-            float v[kF];
-            if (valid) {
-                const long long q = row0 + r;
-                const long long sidx = q / F.N, k = q - sidx * F.N;
-                const float *th = F.scen + sidx * kParams;
-                const float x = F.tri[3 * k], y = F.tri[3 * k + 1], z = F.tri[3 * k + 2];
-#pragma unroll
-                for (int c = 0; c < kF; c++)
-                    v[c] = (raw_feature(c, th, x, y, z) - F.mu[c]) * F.isd[c];
-            } else {
-#pragma unroll
-                for (int c = 0; c < kF; c++) v[c] = 0.f;
-            }
-#pragma unroll
-            for (int c = 0; c < kF; c += 2)
-                *reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(T.a1) +
-                                              canon_offset(tid, c, kF)) = pack2(v[c], v[c + 1]);
+    if (nk > 0) issue(0);
+    for (int c = 0; c < nk && ok; c++) {
+        if (c + 1 < nk) {
+            // stage (c+1)&1 was read by the MMAs of chunk c-1
+            if (c >= 1) ok = cta_wait(&S.bar[(c - 1) & 1], ((c - 1) >> 1) & 1);
+            if (!ok) break;
+            issue(c + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
-        proxy_fence();
+        proxy_fence();  // the copies into shared memory, before the tensor core reads
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
-            // K = 16: one MMA
-            tc_mma(d1, smem_desc(T.a1, 128, (kF / 8) * 128), smem_desc(T.b1, 128, (kF / 8) * 128),
-                   false);
-            tc_commit(&T.bar);
+            const int s = c & 1;
+            const unsigned sbo = (unsigned)(kc / 8) * 128u;
+            const unsigned a0 = smem_u32(S.a[s]), b0 = smem_u32(S.b[s]);
+            for (int kk = 0; kk < kc / 16; kk++)
+                tc_mma(tmem, smem_desc(a0 + 256u * kk, 128, sbo),
+                       smem_desc(b0 + 256u * kk, 128, sbo), idesc, c > 0 || kk > 0);
+            tc_commit(&S.bar[s]);
         }
-        // every thread votes, so that the whole block leaves together on a timeout
-        if (!__syncthreads_and(tc_wait(&T.bar, parity))) {
-            ok = false;
-            if (tid == 0) atomicExch(status, SWGPU_ETIMEOUT);
-            break;
-        }
-        parity ^= 1u;
-        tc_fence_after();
-        // ---- layer-1 epilogue: bias, ReLU, BF16 into layer-2 A
-#pragma unroll
-        for (int ch = 0; ch < 4; ch++) {
-            float v[32];
-            tc_ld32(d1 + lane_base + 32u * ch, v);
-#pragma unroll
-            for (int c = 0; c < 32; c += 2) {
-                const int col = 32 * ch + c;
-                const float a = fmaxf(v[c] + T.bias1[col], 0.f);
-                const float b = fmaxf(v[c + 1] + T.bias1[col + 1], 0.f);
-                *reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(T.a2) +
-                                              canon_offset(tid, col, kH)) = pack2(a, b);
-            }
-        }
-        proxy_fence();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if (tid == 0) {
-#pragma unroll
-            for (int kk = 0; kk < kH / 16; kk++)  // K = 128 in 8 steps of 16
-                tc_mma(d2,
-                       smem_desc(reinterpret_cast<unsigned char *>(T.a2) + kk * 256, 128,
-                                 (kH / 8) * 128),
-                       smem_desc(reinterpret_cast<unsigned char *>(T.b2) + kk * 256, 128,
-                                 (kH / 8) * 128),
-                       kk > 0);
-            tc_commit(&T.bar);
-        }
-        if (!__syncthreads_and(tc_wait(&T.bar, parity))) {
-            ok = false;
-            if (tid == 0) atomicExch(status, SWGPU_ETIMEOUT);
-            break;
-        }
-        parity ^= 1u;
-        tc_fence_after();
-        // ---- layer-2 epilogue and the output layer on the CUDA cores
-        float y0 = T.bias3[0], y1 = T.bias3[1];
-#pragma unroll
-        for (int ch = 0; ch < 4; ch++) {
-            float v[32];
-            tc_ld32(d2 + lane_base + 32u * ch, v);
-#pragma unroll
-            for (int c = 0; c < 32; c++) {
-                const int col = 32 * ch + c;
-                // the activation is rounded to BF16 like the mma.sync path's
-                const float a = __bfloat162float(__float2bfloat16(fmaxf(v[c] + T.bias2[col], 0.f)));
-                y0 += a * T.w3[2 * col];
-                y1 += a * T.w3[2 * col + 1];
-            }
-        }
-        if (valid) {
-            out[2 * r] = y0;
-            out[2 * r + 1] = y1;
-        }
-        tc_fence_before();
-        __syncthreads();  // TMEM and the A tiles are reused by the next tile
-        tc_fence_after();
     }
+    if (ok && nk > 0) ok = cta_wait(&S.bar[(nk - 1) & 1], ((nk - 1) >> 1) & 1);
+    if (!ok) {
+        // status first; then let copies land (cp.async completes on its own)
+        // and give the MMAs in flight one more bounded wait before the
+        // columns are freed
+        if (tid == 0) atomicExch(g.status, SWGPU_ETIMEOUT);
+        cp_async_wait<0>();
+        if (nk > 0) cta_wait(&S.bar[(nk - 1) & 1], ((nk - 1) >> 1) & 1);
+    } else {
+        tc_fence_after();
+        const long long row = m0 + 32 * warp + lane;
+        const unsigned lane_addr = tmem + ((unsigned)(32 * warp) << 16);
+        if (nk == 0) {
+            // an empty K range (a split past the end): nothing to add
+        } else if (N >= 32) {
+#pragma unroll 1
+            for (int c0 = 0; c0 < N; c0 += 32) {
+                float v[32];
+                tc_ld32(lane_addr + c0, v);
+                gemm_epilogue<N, EPI, 32>(g, row, c0, v);
+            }
+        } else {
+            float v[16];
+            tc_ld16(lane_addr, v);
+            gemm_epilogue<N, EPI, 16>(g, row, 0, v);
+        }
+    }
+    tc_fence_before();
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "n"(tmem_cols<N>())
                      : "memory");
 }
 
-// ---- training ------------------------------------------------------------
-__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
-    z += 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
+// ---- output layer (CUDA cores) --------------------------------------------
 
-// Row of batch position r: either given, or drawn uniformly from all
-// (scenario, triangle) pairs of the training set.
-__device__ __forceinline__ long long batch_row(const long long *rows, unsigned long long seed,
-                                               long long r, long long total) {
-    if (rows) return rows[r];
-    return (long long)(mix64(seed ^ (unsigned long long)r * 0xD1B54A32D192ED03ull) %
-                       (unsigned long long)total);
-}
+constexpr int kHeadRows = 32;  // rows per block: one warp per row, 8 warps
 
-struct BatchScratch {
-    __nv_bfloat16 *x;   // [B][16]
-    __nv_bfloat16 *a1;  // [B][128]
-    __nv_bfloat16 *a2;  // [B][128]
-    float *dz1;         // [B][128]
-    float *dz2;         // [B][128]
-    float *dy;          // [B][2]
-    float *y;           // [B][2] outputs
-};
-
-// Forward and backward of a batch: loss = mean over rows and outputs of
-// wt_o (y_o - target_o)^2.  Stores the inputs, activations and the
-// gradients with respect to each layer's pre-activations for the weight
-// gradient kernel; accumulates the loss.
-__global__ void __launch_bounds__(32 * kWarps)
-    mlp_forward_backward(FeatureTables F, const BfWeights *gw, const float *__restrict__ targets,
-                         const long long *rows, unsigned long long seed, long long batch,
-                         long long total, float w_depth, float w_arrival, BatchScratch B,
-                         float *loss) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    BfWeights &W = *reinterpret_cast<BfWeights *>(smem);
-    load_weights(W, gw);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    float my_loss = 0.0f;
-    const float inv_b = 1.0f / (float)batch;
-    for (long long base = (long long)blockIdx.x * kRowsPerBlock; base < batch;
-         base += (long long)gridDim.x * kRowsPerBlock) {
-        const long long ra = base + 16 * warp + g, rb = ra + 8;
-        const bool va = ra < batch, vb = rb < batch;
-        const long long qa = va ? batch_row(rows, seed, ra, total) : 0;
-        const long long qb = vb ? batch_row(rows, seed, rb, total) : 0;
-        uint32_t x[1][4];
-        load_features(F, qa, qb, va, vb, x[0]);
-        uint32_t a1[8][4], a2[8][4];
-        hidden_layer<1, kS1>(x, W.w1t, W.b1, a1);
-        hidden_layer<8, kS2>(a1, W.w2t, W.b2, a2);
-        float y[4];
-        output_layer(a2, W, y);
-        // dL/dy for outputs 0 and 1 of rows a and b (held by t == 0)
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        if (t == 0) {
-            const float wts[2] = {w_depth, w_arrival};
-            if (va) {
+// y = H3 W4 + b4 for each row; the 8 columns of lane l are 8l .. 8l+7.
+__device__ __forceinline__ void head_forward(const __nv_bfloat16 *h, const BfWeights *W,
+                                             const float *b4, float (&hv)[8], float (&y)[kOut]) {
+    const int lane = threadIdx.x & 31;
+    __align__(16) __nv_bfloat16 hb[8];
+    *reinterpret_cast<int4 *>(hb) = *reinterpret_cast<const int4 *>(h + 8 * lane);
+    float acc[kOut] = {0.f, 0.f, 0.f};
 #pragma unroll
-                for (int o = 0; o < 2; o++) {
-                    const float e = y[o] - targets[2 * qa + o];
-                    d[o] = 2.0f * wts[o] * e * inv_b;
-                    my_loss += wts[o] * e * e * inv_b;
-                    B.dy[2 * ra + o] = d[o];
-                    B.y[2 * ra + o] = y[o];
-                }
-            }
-            if (vb) {
+    for (int j = 0; j < 8; j++) {
+        hv[j] = __bfloat162float(hb[j]);
 #pragma unroll
-                for (int o = 0; o < 2; o++) {
-                    const float e = y[2 + o] - targets[2 * qb + o];
-                    d[2 + o] = 2.0f * wts[o] * e * inv_b;
-                    my_loss += wts[o] * e * e * inv_b;
-                    B.dy[2 * rb + o] = d[2 + o];
-                    B.y[2 * rb + o] = y[2 + o];
-                }
-            }
-        }
-        // broadcast the group's dy to its 4 threads
-        const int src = lane & ~3;
-#pragma unroll
-        for (int i = 0; i < 4; i++) d[i] = __shfl_sync(0xffffffffu, d[i], src);
-        // dz2 = (dy W3^T) * relu'(z2), in the C layout of layer 2; re-packed
-        // as A fragments for dz2 W2^T
-        uint32_t g2[8][4];
-#pragma unroll
-        for (int jj = 0; jj < 8; jj++) {
-            float dz[2][4];
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int j = 2 * jj + h;
-                const int u0 = 8 * j + 2 * t, u1 = u0 + 1;
-                const float2 w30 = __bfloat1622float2(
-                    *reinterpret_cast<const __nv_bfloat162 *>(&W.w3[u0 * 8]));
-                const float2 w31 = __bfloat1622float2(
-                    *reinterpret_cast<const __nv_bfloat162 *>(&W.w3[u1 * 8]));
-                const float2 pa = unpack2(a2[jj][h == 0 ? 0 : 2]);  // row a, units u0,u1
-                const float2 pb = unpack2(a2[jj][h == 0 ? 1 : 3]);  // row b
-                dz[h][0] = pa.x > 0.f ? d[0] * w30.x + d[1] * w30.y : 0.f;
-                dz[h][1] = pa.y > 0.f ? d[0] * w31.x + d[1] * w31.y : 0.f;
-                dz[h][2] = pb.x > 0.f ? d[2] * w30.x + d[3] * w30.y : 0.f;
-                dz[h][3] = pb.y > 0.f ? d[2] * w31.x + d[3] * w31.y : 0.f;
-                if (va) {
-                    B.dz2[ra * kH + u0] = dz[h][0];
-                    B.dz2[ra * kH + u1] = dz[h][1];
-                }
-                if (vb) {
-                    B.dz2[rb * kH + u0] = dz[h][2];
-                    B.dz2[rb * kH + u1] = dz[h][3];
-                }
-            }
-            g2[jj][0] = pack2(dz[0][0], dz[0][1]);
-            g2[jj][1] = pack2(dz[0][2], dz[0][3]);
-            g2[jj][2] = pack2(dz[1][0], dz[1][1]);
-            g2[jj][3] = pack2(dz[1][2], dz[1][3]);
-        }
-        // dz1 = (dz2 W2^T) * relu'(z1)
-#pragma unroll
-        for (int jj = 0; jj < 8; jj++) {
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int j = 2 * jj + h;
-                float acc[4] = {0.f, 0.f, 0.f, 0.f};
-                const __nv_bfloat16 *col = W.w2 + (8 * j + g) * kS2;
-#pragma unroll
-                for (int kk = 0; kk < 8; kk++)
-                    mma16816(acc, g2[kk], lds32(col + 16 * kk + 2 * t),
-                             lds32(col + 16 * kk + 8 + 2 * t));
-                const int u0 = 8 * j + 2 * t, u1 = u0 + 1;
-                const float2 pa = unpack2(a1[jj][h == 0 ? 0 : 2]);
-                const float2 pb = unpack2(a1[jj][h == 0 ? 1 : 3]);
-                if (va) {
-                    B.dz1[ra * kH + u0] = pa.x > 0.f ? acc[0] : 0.f;
-                    B.dz1[ra * kH + u1] = pa.y > 0.f ? acc[1] : 0.f;
-                }
-                if (vb) {
-                    B.dz1[rb * kH + u0] = pb.x > 0.f ? acc[2] : 0.f;
-                    B.dz1[rb * kH + u1] = pb.y > 0.f ? acc[3] : 0.f;
-                }
-            }
-        }
-        // inputs and activations of the rows for the weight gradients
-#pragma unroll
-        for (int jj = 0; jj < 8; jj++) {
-            const int u0 = 16 * jj + 2 * t;
-            if (va) {
-                *reinterpret_cast<uint32_t *>(&B.a1[ra * kH + u0]) = a1[jj][0];
-                *reinterpret_cast<uint32_t *>(&B.a1[ra * kH + u0 + 8]) = a1[jj][2];
-                *reinterpret_cast<uint32_t *>(&B.a2[ra * kH + u0]) = a2[jj][0];
-                *reinterpret_cast<uint32_t *>(&B.a2[ra * kH + u0 + 8]) = a2[jj][2];
-            }
-            if (vb) {
-                *reinterpret_cast<uint32_t *>(&B.a1[rb * kH + u0]) = a1[jj][1];
-                *reinterpret_cast<uint32_t *>(&B.a1[rb * kH + u0 + 8]) = a1[jj][3];
-                *reinterpret_cast<uint32_t *>(&B.a2[rb * kH + u0]) = a2[jj][1];
-                *reinterpret_cast<uint32_t *>(&B.a2[rb * kH + u0 + 8]) = a2[jj][3];
-            }
-        }
-        if (va) {
-            *reinterpret_cast<uint32_t *>(&B.x[ra * kF + 2 * t]) = x[0][0];
-            *reinterpret_cast<uint32_t *>(&B.x[ra * kF + 2 * t + 8]) = x[0][2];
-        }
-        if (vb) {
-            *reinterpret_cast<uint32_t *>(&B.x[rb * kF + 2 * t]) = x[0][1];
-            *reinterpret_cast<uint32_t *>(&B.x[rb * kF + 2 * t + 8]) = x[0][3];
-        }
+        for (int o = 0; o < kOut; o++)
+            acc[o] = fmaf(hv[j], __bfloat162float(W->w4[(8 * lane + j) * kOut + o]), acc[o]);
     }
-    for (int o = 16; o > 0; o >>= 1) my_loss += __shfl_xor_sync(0xffffffffu, my_loss, o);
-    if (lane == 0) atomicAdd(loss, my_loss);
+#pragma unroll
+    for (int o = 0; o < kOut; o++) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) acc[o] += __shfl_xor_sync(0xffffffffu, acc[o], d);
+        y[o] = acc[o] + b4[o];
+    }
 }
 
-// Weight gradients: grad[i][o] += sum over a chunk of rows of
-// in[r][i] * dz[r][o] (FP32), one block per (layer tile, row chunk).
-constexpr int kChunk = 256;
-__global__ void __launch_bounds__(256) mlp_weight_grads(BatchScratch B, long long batch,
-                                                        float *__restrict__ grad) {
-    __shared__ float sin_[32][kH + 1];
-    __shared__ float sdz[32][kH + 1];
-    // blockIdx.y: 0 -> W2 (128 x 128), 1 -> W1 (16 x 128), 2 -> W3 (128 x 2),
-    // 3 -> biases b1, b2, b3
-    const int layer = blockIdx.y;
-    const long long r0 = (long long)blockIdx.x * kChunk;
-    const long long r1 = r0 + kChunk < batch ? r0 + kChunk : batch;
-    const int tid = threadIdx.x;
-    // each thread owns 64 (i, o) entries of a 128 x 128 tile: i = tid / 2,
-    // o = (tid % 2) * 64 + c
-    float acc[64];
+__global__ void __launch_bounds__(256) mlp_head_predict(const __nv_bfloat16 *__restrict__ h3,
+                                                        const BfWeights *W, const float *params,
+                                                        long long nrows, float *__restrict__ out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long r = (long long)blockIdx.x * 8 + warp;
+    if (r >= nrows) return;
+    float hv[8], y[kOut];
+    head_forward(h3 + r * kH, W, params + kOffB4, hv, y);
+    if (lane < kOut) out[r * kOut + lane] = y[lane];
+}
+
+// Training head: outputs, loss, dL/dy and the gradient into layer 3,
+// dz3 = (dy W4^T) * relu'(h3), stored row-major and feature-major; the
+// output layer's own gradients (W4, b4) are summed per block.  loss =
+// mean over rows of w_d (y0 - t0)^2 + w_a (y1 - t1)^2 + w_e (y2 - |y0 - t0|)^2,
+// the error estimate's target |y0 - t0| taken as a constant.
+__global__ void __launch_bounds__(256) mlp_head_train(
+    const __nv_bfloat16 *__restrict__ h3, const BfWeights *W, const float *params,
+    const float *__restrict__ targets, const long long *__restrict__ row_of, long long nrows,
+    long long Bp, float w_d, float w_a, float w_e, float *__restrict__ y_out,
+    __nv_bfloat16 *__restrict__ dz_row, __nv_bfloat16 *__restrict__ dz_col,
+    float *__restrict__ grad, float *__restrict__ loss) {
+    // rows padded by 16 bytes: the feature-major pass reads down a column
+    __shared__ __align__(16) __nv_bfloat16 tile[kHeadRows][kH + 8];
+    __shared__ float gw4[kH * kOut];
+    __shared__ float gb4[kOut];
+    __shared__ float lsum;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kH * kOut; i += blockDim.x) gw4[i] = 0.f;
+    if (threadIdx.x < kOut) gb4[threadIdx.x] = 0.f;
+    if (threadIdx.x == 0) lsum = 0.f;
+    __syncthreads();
+    const float inv_b = 1.0f / (float)nrows;
+    const long long rb = (long long)blockIdx.x * kHeadRows;
+    for (int i = warp; i < kHeadRows; i += 8) {
+        const long long r = rb + i;
+        __align__(16) __nv_bfloat16 dz[8];
+        if (r < nrows) {
+            float hv[8], y[kOut];
+            head_forward(h3 + r * kH, W, params + kOffB4, hv, y);
+            const float *t = targets + row_of[r] * kTargets;
+            const float e0 = y[0] - t[0], e1 = y[1] - t[1];
+            const float e2 = y[2] - fabsf(e0);
+            const float d0 = 2.f * w_d * e0 * inv_b, d1 = 2.f * w_a * e1 * inv_b,
+                        d2 = 2.f * w_e * e2 * inv_b;
+            if (lane == 0) {
+                y_out[r * kOut] = y[0];
+                y_out[r * kOut + 1] = y[1];
+                y_out[r * kOut + 2] = y[2];
+                atomicAdd(&lsum, (w_d * e0 * e0 + w_a * e1 * e1 + w_e * e2 * e2) * inv_b);
+                atomicAdd(&gb4[0], d0);
+                atomicAdd(&gb4[1], d1);
+                atomicAdd(&gb4[2], d2);
+            }
 #pragma unroll
-    for (int c = 0; c < 64; c++) acc[c] = 0.f;
-    const int ni = layer == 1 ? kF : kH;
-    const int no = layer == 2 ? kOut : kH;
-    for (long long rb = r0; rb < r1; rb += 32) {
-        const int nr = (int)(r1 - rb < 32 ? r1 - rb : 32);
-        for (int e = tid; e < 32 * kH; e += 256) {
-            const int rr = e / kH, c = e % kH;
-            float vin = 0.f, vdz = 0.f;
-            if (rr < nr) {
-                const long long r = rb + rr;
-                if (layer == 0) {
-                    vin = __bfloat162float(B.a1[r * kH + c]);
-                    vdz = B.dz2[r * kH + c];
-                } else if (layer == 1) {
-                    vin = c < kF ? __bfloat162float(B.x[r * kF + c]) : 0.f;
-                    vdz = B.dz1[r * kH + c];
-                } else if (layer == 2) {
-                    vin = __bfloat162float(B.a2[r * kH + c]);
-                    vdz = c < kOut ? B.dy[r * kOut + c] : 0.f;
-                } else {
-                    vin = B.dz1[r * kH + c];   // bias rows: b1 from dz1, b2 from dz2,
-                    vdz = B.dz2[r * kH + c];   // b3 from dy
-                }
+            for (int j = 0; j < 8; j++) {
+                const int c = 8 * lane + j;
+                const float w0 = __bfloat162float(W->w4[c * kOut]);
+                const float w1 = __bfloat162float(W->w4[c * kOut + 1]);
+                const float w2 = __bfloat162float(W->w4[c * kOut + 2]);
+                const float g = fmaf(d0, w0, fmaf(d1, w1, d2 * w2));
+                dz[j] = __float2bfloat16(hv[j] > 0.f ? g : 0.f);
+                atomicAdd(&gw4[c * kOut], hv[j] * d0);
+                atomicAdd(&gw4[c * kOut + 1], hv[j] * d1);
+                atomicAdd(&gw4[c * kOut + 2], hv[j] * d2);
             }
-            sin_[rr][c] = vin;
-            sdz[rr][c] = vdz;
-        }
-        __syncthreads();
-        if (layer < 3) {
-            const int i = tid >> 1, ob = (tid & 1) * 64;
-            if (i < ni) {
-                for (int rr = 0; rr < nr; rr++) {
-                    const float a = sin_[rr][i];
+        } else {
 #pragma unroll
-                    for (int c = 0; c < 64; c++) acc[c] += a * sdz[rr][ob + c];
-                }
-            }
-        } else if (tid < kH) {
-            for (int rr = 0; rr < nr; rr++) {
-                acc[0] += sin_[rr][tid];
-                acc[1] += sdz[rr][tid];
-            }
-            if (tid < kOut)
-                for (int rr = 0; rr < nr; rr++) acc[2] += B.dy[(rb + rr) * kOut + tid];
+            for (int j = 0; j < 8; j++) dz[j] = __float2bfloat16(0.f);
         }
+        *reinterpret_cast<int4 *>(&tile[i][8 * lane]) = *reinterpret_cast<const int4 *>(dz);
+    }
+    __syncthreads();
+    // row-major rows of the block (rows up to Bp: the padding is zero)
+    for (int v = threadIdx.x; v < kHeadRows * (kH / 8); v += blockDim.x) {
+        const int i = v / (kH / 8), q = v % (kH / 8);
+        const long long r = rb + i;
+        if (r < Bp)
+            reinterpret_cast<int4 *>(dz_row + r * kH)[q] =
+                reinterpret_cast<const int4 *>(&tile[i][0])[q];
+    }
+    // feature-major: 32 consecutive rows of each feature
+    for (int v = threadIdx.x; v < kH * kHeadRows; v += blockDim.x) {
+        const int c = v / kHeadRows, i = v % kHeadRows;
+        const long long r = rb + i;
+        if (r < Bp) dz_col[(long long)c * Bp + r] = tile[i][c];
+    }
+    for (int i = threadIdx.x; i < kH * kOut; i += blockDim.x)
+        atomicAdd(&grad[kOffW4 + i], gw4[i]);
+    if (threadIdx.x < kOut) atomicAdd(&grad[kOffB4 + threadIdx.x], gb4[threadIdx.x]);
+    if (threadIdx.x == 0) atomicAdd(loss, lsum);
+}
+
+// Bias gradients: sum over the batch of each feature-major gradient row.
+__global__ void __launch_bounds__(256) mlp_bias_grad(const __nv_bfloat16 *__restrict__ dz_col,
+                                                     long long Bp, int nfeat,
+                                                     float *__restrict__ gb) {
+    const int f = blockIdx.x;
+    if (f >= nfeat) return;
+    float s = 0.f;
+    const __nv_bfloat16 *p = dz_col + (long long)f * Bp;
+    for (long long r = threadIdx.x; r < Bp; r += blockDim.x) s += __bfloat162float(p[r]);
+    __shared__ float sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int t = 128; t > 0; t >>= 1) {
+        if ((int)threadIdx.x < t) sh[threadIdx.x] += sh[threadIdx.x + t];
         __syncthreads();
     }
-    if (layer < 3) {
-        const int i = tid >> 1, ob = (tid & 1) * 64;
-        if (i >= ni) return;
-        float *gw = grad + (layer == 0 ? kOffW2 : layer == 1 ? kOffW1 : kOffW3);
-        for (int c = 0; c < 64; c++) {
-            const int o = ob + c;
-            if (o < no) atomicAdd(&gw[i * no + o], acc[c]);
-        }
-    } else if (tid < kH) {
-        atomicAdd(&grad[kOffB1 + tid], acc[0]);
-        atomicAdd(&grad[kOffB2 + tid], acc[1]);
-        if (tid < kOut) atomicAdd(&grad[kOffB3 + tid], acc[2]);
-    }
+    if (threadIdx.x == 0) gb[f] += sh[0];
 }
 
-// BF16 images of the FP32 parameters.
+// ---- weights ----------------------------------------------------------------
+
 __global__ void mlp_pack_weights(const float *__restrict__ p, BfWeights *W) {
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const __nv_bfloat16 zero = __float2bfloat16(0.f);
-    if (tid < kH * kS1) {
-        const int o = tid / kS1, i = tid % kS1;
-        W->w1t[tid] = i < kF ? __float2bfloat16(p[kOffW1 + i * kH + o]) : zero;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kH * kH) {
+        const int in = i / kH, out = i % kH;
+        const __nv_bfloat16 a = __float2bfloat16(p[kOffW2 + i]);
+        const __nv_bfloat16 b = __float2bfloat16(p[kOffW3 + i]);
+        W->w2[i] = a;
+        W->w3[i] = b;
+        W->wt2[out * kH + in] = a;
+        W->wt3[out * kH + in] = b;
     }
-    if (tid < kH * kS2) {
-        const int r = tid / kS2, c = tid % kS2;
-        W->w2t[tid] = c < kH ? __float2bfloat16(p[kOffW2 + c * kH + r]) : zero;
-        W->w2[tid] = c < kH ? __float2bfloat16(p[kOffW2 + r * kH + c]) : zero;
+    if (i < kF * kH) {
+        const int in = i / kH, out = i % kH;
+        W->wt1[out * kF + in] = __float2bfloat16(p[kOffW1 + i]);
     }
-    if (tid < 8 * kS2) {
-        const int o = tid / kS2, i = tid % kS2;
-        W->w3t[tid] = (o < kOut && i < kH) ? __float2bfloat16(p[kOffW3 + i * kOut + o]) : zero;
-    }
-    if (tid < kH * 8) {
-        const int i = tid / 8, o = tid % 8;
-        W->w3[tid] = o < kOut ? __float2bfloat16(p[kOffW3 + i * kOut + o]) : zero;
-    }
-    if (tid < kH) {
-        W->b1[tid] = p[kOffB1 + tid];
-        W->b2[tid] = p[kOffB2 + tid];
-    }
-    if (tid < 8) W->b3[tid] = tid < kOut ? p[kOffB3 + tid] : 0.f;
+    if (i < kH * kOut) W->w4[i] = __float2bfloat16(p[kOffW4 + i]);
 }
 
-// Adam on the FP32 master parameters.
 __global__ void mlp_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
-                         float *__restrict__ v, int n, float lr, float b1, float b2, float eps,
+                         float *__restrict__ v, long n, float lr, float b1, float b2, float eps,
                          float c1, float c2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -764,23 +627,36 @@ __global__ void mlp_adam(float *__restrict__ p, const float *__restrict__ g, flo
     p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
 }
 
+// ---- host side ----------------------------------------------------------------
+
+struct Buffers {  // one batch of rows (training) or one chunk (inference)
+    long long cap = 0;  // rows (a multiple of kTileM)
+    bool train = false;
+    __nv_bfloat16 *xr = nullptr, *xc = nullptr;
+    __nv_bfloat16 *h1 = nullptr, *h2 = nullptr, *h3 = nullptr;     // row-major
+    __nv_bfloat16 *h1c = nullptr, *h2c = nullptr;                  // feature-major
+    __nv_bfloat16 *d3 = nullptr, *d2 = nullptr, *d3c = nullptr, *d2c = nullptr, *d1c = nullptr;
+    long long *row_of = nullptr;
+    float *y = nullptr;
+};
+
 struct Mlp {
     int device = 0;
+    int sms = 1;
     cudaStream_t stream = nullptr;
     float *params = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
     BfWeights *w = nullptr;
     float *mu = nullptr, *isd = nullptr;
     float *scen = nullptr, *tri = nullptr, *targets = nullptr;
     long long S = 0, N = 0;
-    BatchScratch scratch{};
-    long long scratch_rows = 0;
+    Buffers buf;
     long long *rows = nullptr;
     long long rows_cap = 0;
     float *loss = nullptr;
-    int *status = nullptr;   // device-side failure of the tensor-core kernel
-    int tensor_path = 0;     // 0: mma.sync, 1: tcgen05 (inference)
+    int *status = nullptr;   // device-side failure of a tensor-core kernel
+    bool unusable = false;   // a kernel reported SWGPU_ETIMEOUT
     long long adam_t = 0;
-    std::vector<void *> allocs;
+    std::vector<void *> allocs, data_allocs, buf_allocs;
     std::string err;
 };
 
@@ -805,58 +681,178 @@ int mfail(Mlp *m, int code, const char *fmt, ...) {
     } while (0)
 
 template <typename T>
-int malloc_dev(Mlp *m, T **p, size_t count) {
+int malloc_dev(Mlp *m, T **p, size_t count, std::vector<void *> *owner = nullptr) {
     void *q = nullptr;
     cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
     if (e != cudaSuccess)
         return mfail(m, SWGPU_ENOMEM, "cudaMalloc %zu bytes: %s", count * sizeof(T),
                      cudaGetErrorString(e));
-    m->allocs.push_back(q);
+    (owner ? *owner : m->allocs).push_back(q);
     *p = static_cast<T *>(q);
     return SWGPU_OK;
 }
 
-int ensure_scratch(Mlp *m, long long batch) {
-    if (batch <= m->scratch_rows) return SWGPU_OK;
+void free_list(std::vector<void *> &v) {
+    for (void *p : v) cudaFree(p);
+    v.clear();
+}
+
+// Row buffers for `rows` rows (rounded up to the tile), reallocated only
+// when they grow or when training needs the feature-major copies.
+int ensure_buffers(Mlp *m, long long rows, bool train, std::vector<void *> &owned) {
+    const long long cap = (rows + kTileM - 1) / kTileM * kTileM;
+    Buffers &B = m->buf;
+    if (cap <= B.cap && (B.train || !train)) return SWGPU_OK;
+    MCK(cudaStreamSynchronize(m->stream));
+    free_list(owned);
+    B = Buffers{};
     int rc;
-    BatchScratch &B = m->scratch;
-    if ((rc = malloc_dev(m, &B.x, (size_t)batch * kF))) return rc;
-    if ((rc = malloc_dev(m, &B.a1, (size_t)batch * kH))) return rc;
-    if ((rc = malloc_dev(m, &B.a2, (size_t)batch * kH))) return rc;
-    if ((rc = malloc_dev(m, &B.dz1, (size_t)batch * kH))) return rc;
-    if ((rc = malloc_dev(m, &B.dz2, (size_t)batch * kH))) return rc;
-    if ((rc = malloc_dev(m, &B.dy, (size_t)batch * kOut))) return rc;
-    if ((rc = malloc_dev(m, &B.y, (size_t)batch * kOut))) return rc;
-    m->scratch_rows = batch;
+    const size_t hr = (size_t)cap * kH;
+    if ((rc = malloc_dev(m, &B.xr, (size_t)cap * kF, &owned)) ||
+        (rc = malloc_dev(m, &B.h1, hr, &owned)) || (rc = malloc_dev(m, &B.h2, hr, &owned)) ||
+        (rc = malloc_dev(m, &B.h3, hr, &owned)) || (rc = malloc_dev(m, &B.y, (size_t)cap * kOut, &owned)))
+        return rc;
+    if (train) {
+        if ((rc = malloc_dev(m, &B.xc, (size_t)cap * kF, &owned)) ||
+            (rc = malloc_dev(m, &B.h1c, hr, &owned)) || (rc = malloc_dev(m, &B.h2c, hr, &owned)) ||
+            (rc = malloc_dev(m, &B.d3, hr, &owned)) || (rc = malloc_dev(m, &B.d2, hr, &owned)) ||
+            (rc = malloc_dev(m, &B.d3c, hr, &owned)) || (rc = malloc_dev(m, &B.d2c, hr, &owned)) ||
+            (rc = malloc_dev(m, &B.d1c, hr, &owned)) ||
+            (rc = malloc_dev(m, &B.row_of, (size_t)cap, &owned)))
+            return rc;
+    }
+    B.cap = cap;
+    B.train = train;
     return SWGPU_OK;
 }
 
-int sm_count() {
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 1;
+template <int N, int EPI>
+int launch_gemm(Mlp *m, const GemmArgs &g, int splits) {
+    const unsigned grid_x = (unsigned)((g.M + kTileM - 1) / kTileM);
+    const size_t smem = sizeof(GemmSmem<N>) + 1024;
+    tc_gemm<N, EPI><<<dim3(grid_x, (unsigned)splits), kGemmThreads, smem, m->stream>>>(g);
+    MCK(cudaGetLastError());
+    return SWGPU_OK;
+}
+
+template <int N, int EPI>
+cudaError_t gemm_attr() {
+    return cudaFuncSetAttribute(tc_gemm<N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(GemmSmem<N>) + 1024));
 }
 
 FeatureTables tables(const Mlp *m) {
     return FeatureTables{m->scen, m->tri, m->mu, m->isd, m->N};
 }
 
-// forward + backward + weight gradients of one batch into m->grad
-int batch_gradients(Mlp *m, const long long *d_rows, unsigned long long seed, long long batch,
-                    long long total, float w_depth, float w_arrival) {
-    int rc = ensure_scratch(m, batch);
+GemmArgs gemm_args(Mlp *m, const __nv_bfloat16 *A, long lda, const __nv_bfloat16 *B, long ldb,
+                   long long M, long K) {
+    GemmArgs g{};
+    g.A = A;
+    g.lda = lda;
+    g.B = B;
+    g.ldb = ldb;
+    g.M = M;
+    g.K = K;
+    g.k_per_split = K;
+    g.status = m->status;
+    return g;
+}
+
+// Forward pass of Bp rows already in buf.xr (feature-major copies when train).
+int forward(Mlp *m, long long Bp, bool train) {
+    Buffers &B = m->buf;
+    const BfWeights *W = m->w;
+    int rc;
+    GemmArgs g = gemm_args(m, B.xr, kF, W->wt1, kF, Bp, kF);
+    g.bias = m->params + kOffB1;
+    g.out_row = B.h1;
+    g.out_col = train ? B.h1c : nullptr;
+    g.ldc = Bp;
+    if ((rc = launch_gemm<kH, kEpiHidden>(m, g, 1))) return rc;
+    g = gemm_args(m, B.h1, kH, W->wt2, kH, Bp, kH);
+    g.bias = m->params + kOffB2;
+    g.out_row = B.h2;
+    g.out_col = train ? B.h2c : nullptr;
+    g.ldc = Bp;
+    if ((rc = launch_gemm<kH, kEpiHidden>(m, g, 1))) return rc;
+    g = gemm_args(m, B.h2, kH, W->wt3, kH, Bp, kH);
+    g.bias = m->params + kOffB3;
+    g.out_row = B.h3;
+    g.out_col = nullptr;
+    if ((rc = launch_gemm<kH, kEpiHidden>(m, g, 1))) return rc;
+    return SWGPU_OK;
+}
+
+// Batch rows per K split of the weight-gradient GEMMs.
+constexpr long kWgradRows = 1024;
+
+// Forward, backward and the gradient vector of nrows rows (Bp padded).
+int batch_gradients(Mlp *m, const long long *d_rows, unsigned long long seed, long long nrows,
+                    float w_d, float w_a, float w_e) {
+    const long long Bp = (nrows + kTileM - 1) / kTileM * kTileM;
+    int rc = ensure_buffers(m, nrows, true, m->buf_allocs);
     if (rc) return rc;
+    Buffers &B = m->buf;
+    const BfWeights *W = m->w;
     MCK(cudaMemsetAsync(m->grad, 0, sizeof(float) * kNumParams, m->stream));
     MCK(cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream));
-    const long long tiles = (batch + kRowsPerBlock - 1) / kRowsPerBlock;
-    const int grid = (int)std::min<long long>(tiles, 4LL * sm_count());
-    mlp_forward_backward<<<grid, 32 * kWarps, sizeof(BfWeights), m->stream>>>(
-        tables(m), m->w, m->targets, d_rows, seed, batch, total, w_depth, w_arrival, m->scratch,
-        m->loss);
-    const dim3 g2((unsigned)((batch + kChunk - 1) / kChunk), 4);
-    mlp_weight_grads<<<g2, 256, 0, m->stream>>>(m->scratch, batch, m->grad);
+    mlp_features<<<(unsigned)((Bp + 255) / 256), 256, 0, m->stream>>>(
+        tables(m), d_rows, seed, d_rows ? 0 : m->S * m->N, 0, nrows, Bp, B.xr, B.xc, B.row_of);
+    if ((rc = forward(m, Bp, true))) return rc;
+    mlp_head_train<<<(unsigned)((Bp + kHeadRows - 1) / kHeadRows), 256, 0, m->stream>>>(
+        B.h3, W, m->params, m->targets, B.row_of, nrows, Bp, w_d, w_a, w_e, B.y, B.d3, B.d3c,
+        m->grad, m->loss);
     MCK(cudaGetLastError());
+    const int splits = (int)((Bp + kWgradRows - 1) / kWgradRows);
+    // layer 3: gW3 = H2^T dZ3 (in x out), gb3; dZ2 = (dZ3 W3^T) * relu'(H2)
+    GemmArgs g = gemm_args(m, B.h2c, Bp, B.d3c, Bp, kH, Bp);
+    g.k_per_split = kWgradRows;
+    g.grad = m->grad + kOffW3;
+    if ((rc = launch_gemm<kH, kEpiWgrad>(m, g, splits))) return rc;
+    mlp_bias_grad<<<kH, 256, 0, m->stream>>>(B.d3c, Bp, kH, m->grad + kOffB3);
+    g = gemm_args(m, B.d3, kH, W->w3, kH, Bp, kH);
+    g.mask = B.h2;
+    g.out_row = B.d2;
+    g.out_col = B.d2c;
+    g.ldc = Bp;
+    if ((rc = launch_gemm<kH, kEpiDgrad>(m, g, 1))) return rc;
+    // layer 2: gW2 = H1^T dZ2, gb2; dZ1 = (dZ2 W2^T) * relu'(H1)
+    g = gemm_args(m, B.h1c, Bp, B.d2c, Bp, kH, Bp);
+    g.k_per_split = kWgradRows;
+    g.grad = m->grad + kOffW2;
+    if ((rc = launch_gemm<kH, kEpiWgrad>(m, g, splits))) return rc;
+    mlp_bias_grad<<<kH, 256, 0, m->stream>>>(B.d2c, Bp, kH, m->grad + kOffB2);
+    g = gemm_args(m, B.d2, kH, W->w2, kH, Bp, kH);
+    g.mask = B.h1;
+    g.out_row = B.d3;  // dZ1 row-major is not needed again: B.d3 is free
+    g.out_col = B.d1c;
+    g.ldc = Bp;
+    if ((rc = launch_gemm<kH, kEpiDgrad>(m, g, 1))) return rc;
+    // layer 1: gW1^T = dZ1^T X (out x in), stored transposed into W1 [in][out]; gb1
+    g = gemm_args(m, B.d1c, Bp, B.xc, Bp, kH, Bp);
+    g.k_per_split = kWgradRows;
+    g.grad = m->grad + kOffW1;
+    if ((rc = launch_gemm<kF, kEpiWgradT>(m, g, splits))) return rc;
+    mlp_bias_grad<<<kH, 256, 0, m->stream>>>(B.d1c, Bp, kH, m->grad + kOffB1);
+    MCK(cudaGetLastError());
+    return SWGPU_OK;
+}
+
+int read_status(Mlp *m, const char *what) {
+    int st = 0;
+    MCK(cudaMemcpy(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) {
+        if (st == SWGPU_ETIMEOUT) m->unusable = true;
+        return mfail(m, st, "%s: a tensor-core wait ran out; destroy the handle", what);
+    }
+    return SWGPU_OK;
+}
+
+int usable(Mlp *m, const char *what) {
+    if (m && m->unusable)
+        return mfail(m, SWGPU_ETIMEOUT,
+                     "%s: handle unusable after a tensor-core wait ran out; destroy it", what);
     return SWGPU_OK;
 }
 
@@ -872,17 +868,13 @@ int swgpu_mlp_create(const float *params, const float *feature_mean,
     Mlp *m = new Mlp();
     int rc = SWGPU_OK;
     cudaError_t e = cudaGetDevice(&m->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(BfWeights));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(mlp_predict_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(TcSmem) + 1024);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(mlp_forward_backward,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(BfWeights));
+    if (e == cudaSuccess) e = gemm_attr<kH, kEpiHidden>();
+    if (e == cudaSuccess) e = gemm_attr<kH, kEpiDgrad>();
+    if (e == cudaSuccess) e = gemm_attr<kH, kEpiWgrad>();
+    if (e == cudaSuccess) e = gemm_attr<kF, kEpiWgradT>();
     if (e != cudaSuccess) {
         rc = mfail(m, SWGPU_ECUDA, "swgpu_mlp_create: %s", cudaGetErrorString(e));
         delete m;
@@ -893,22 +885,26 @@ int swgpu_mlp_create(const float *params, const float *feature_mean,
         (rc = malloc_dev(m, &m->adam_v, kNumParams)) || (rc = malloc_dev(m, &m->w, 1)) ||
         (rc = malloc_dev(m, &m->mu, kF)) || (rc = malloc_dev(m, &m->isd, kF)) ||
         (rc = malloc_dev(m, &m->loss, 1)) || (rc = malloc_dev(m, &m->status, 1))) {
-        for (void *p : m->allocs) cudaFree(p);
+        free_list(m->allocs);
         delete m;
         return rc;
     }
-    cudaMemcpy(m->params, params, sizeof(float) * kNumParams, cudaMemcpyHostToDevice);
-    cudaMemcpy(m->mu, feature_mean, sizeof(float) * kF, cudaMemcpyHostToDevice);
-    cudaMemcpy(m->isd, feature_inv_std, sizeof(float) * kF, cudaMemcpyHostToDevice);
-    cudaMemset(m->adam_m, 0, sizeof(float) * kNumParams);
-    cudaMemset(m->adam_v, 0, sizeof(float) * kNumParams);
-    cudaMemset(m->status, 0, sizeof(int));
-    mlp_pack_weights<<<(kH * kS2 + 255) / 256, 256, 0, m->stream>>>(m->params, m->w);
-    e = cudaStreamSynchronize(m->stream);
+    e = cudaMemcpy(m->params, params, sizeof(float) * kNumParams, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(m->mu, feature_mean, sizeof(float) * kF, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(m->isd, feature_inv_std, sizeof(float) * kF, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(m->adam_m, 0, sizeof(float) * kNumParams);
+    if (e == cudaSuccess) e = cudaMemset(m->adam_v, 0, sizeof(float) * kNumParams);
+    if (e == cudaSuccess) e = cudaMemset(m->status, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        mlp_pack_weights<<<(kH * kH + 255) / 256, 256, 0, m->stream>>>(m->params, m->w);
+        e = cudaStreamSynchronize(m->stream);
+    }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
         rc = mfail(m, SWGPU_ECUDA, "swgpu_mlp_create: %s", cudaGetErrorString(e));
-        for (void *p : m->allocs) cudaFree(p);
+        free_list(m->allocs);
         delete m;
         return rc;
     }
@@ -920,7 +916,9 @@ int swgpu_mlp_destroy(void *handle) {
     Mlp *m = static_cast<Mlp *>(handle);
     if (!m) return SWGPU_OK;
     if (m->stream) cudaStreamSynchronize(m->stream);
-    for (void *p : m->allocs) cudaFree(p);
+    free_list(m->data_allocs);
+    free_list(m->buf_allocs);
+    free_list(m->allocs);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
     return SWGPU_OK;
@@ -931,23 +929,28 @@ const char *swgpu_mlp_last_error(void *handle) {
     return m ? m->err.c_str() : g_mlp_error.c_str();
 }
 
-int swgpu_mlp_set_data(void *handle, const float *tri_xyz, int64_t ntri, const float *scen,
+int swgpu_mlp_set_data(void *handle, const float *tri, int64_t ntri, const float *scen,
                        int64_t nscen, const float *targets) {
     Mlp *m = static_cast<Mlp *>(handle);
-    if (!m || !tri_xyz || !scen || ntri <= 0 || nscen <= 0)
+    if (!m || !tri || !scen || ntri <= 0 || nscen <= 0)
         return mfail(m, SWGPU_EINVAL, "swgpu_mlp_set_data: bad argument");
+    if (int rc = usable(m, "swgpu_mlp_set_data")) return rc;
     if ((long long)ntri * nscen >= (1LL << 40))
         return mfail(m, SWGPU_EINVAL, "swgpu_mlp_set_data: too many rows");
+    MCK(cudaStreamSynchronize(m->stream));
+    free_list(m->data_allocs);
+    m->tri = m->scen = m->targets = nullptr;
+    m->N = m->S = 0;
     int rc;
-    if ((rc = malloc_dev(m, &m->tri, (size_t)ntri * 3)) ||
-        (rc = malloc_dev(m, &m->scen, (size_t)nscen * kParams)))
+    if ((rc = malloc_dev(m, &m->tri, (size_t)ntri * kTri, &m->data_allocs)) ||
+        (rc = malloc_dev(m, &m->scen, (size_t)nscen * kParams, &m->data_allocs)))
         return rc;
-    MCK(cudaMemcpy(m->tri, tri_xyz, sizeof(float) * 3 * ntri, cudaMemcpyHostToDevice));
+    MCK(cudaMemcpy(m->tri, tri, sizeof(float) * kTri * ntri, cudaMemcpyHostToDevice));
     MCK(cudaMemcpy(m->scen, scen, sizeof(float) * kParams * nscen, cudaMemcpyHostToDevice));
-    m->targets = nullptr;
     if (targets) {
-        if ((rc = malloc_dev(m, &m->targets, (size_t)ntri * nscen * kOut))) return rc;
-        MCK(cudaMemcpy(m->targets, targets, sizeof(float) * kOut * ntri * nscen,
+        if ((rc = malloc_dev(m, &m->targets, (size_t)ntri * nscen * kTargets, &m->data_allocs)))
+            return rc;
+        MCK(cudaMemcpy(m->targets, targets, sizeof(float) * kTargets * ntri * nscen,
                        cudaMemcpyHostToDevice));
     }
     m->N = ntri;
@@ -960,43 +963,47 @@ int swgpu_mlp_predict(void *handle, int64_t row0, int64_t nrows, float *out_devi
     Mlp *m = static_cast<Mlp *>(handle);
     if (!m || !out_device || nrows <= 0 || row0 < 0 || row0 + nrows > m->S * m->N)
         return mfail(m, SWGPU_EINVAL, "swgpu_mlp_predict: bad rows");
+    if (int rc = usable(m, "swgpu_mlp_predict")) return rc;
+    // chunks of up to 2^21 rows through row buffers (1 GB per activation)
+    const long long chunk = std::min<long long>(nrows, 1LL << 21);
+    int rc = ensure_buffers(m, chunk, false, m->buf_allocs);
+    if (rc) return rc;
     cudaEvent_t a, b;
     MCK(cudaEventCreate(&a));
     MCK(cudaEventCreate(&b));
     MCK(cudaEventRecord(a, m->stream));
-    if (m->tensor_path == 1) {
-        // two CTAs per SM: each holds 256 TMEM columns of the SM's 512
-        const long long tiles = (nrows + kTcRows - 1) / kTcRows;
-        const int grid = (int)std::min<long long>(tiles, 2LL * sm_count());
-        mlp_predict_tc<<<grid, 128, sizeof(TcSmem) + 1024, m->stream>>>(
-            tables(m), m->params, row0, nrows, out_device, m->status);
-    } else {
-        const long long tiles = (nrows + kRowsPerBlock - 1) / kRowsPerBlock;
-        const int grid = (int)std::min<long long>(tiles, 4LL * sm_count());
-        mlp_predict<<<grid, 32 * kWarps, sizeof(BfWeights), m->stream>>>(tables(m), m->w, row0,
-                                                                          nrows, out_device);
+    for (long long r0 = 0; r0 < nrows; r0 += chunk) {
+        const long long n = std::min(chunk, nrows - r0);
+        const long long Bp = (n + kTileM - 1) / kTileM * kTileM;
+        mlp_features<<<(unsigned)((Bp + 255) / 256), 256, 0, m->stream>>>(
+            tables(m), nullptr, 0, 0, row0 + r0, n, Bp, m->buf.xr, nullptr, nullptr);
+        if ((rc = forward(m, Bp, false))) return rc;
+        mlp_head_predict<<<(unsigned)((n + 7) / 8), 256, 0, m->stream>>>(
+            m->buf.h3, m->w, m->params, n, out_device + r0 * kOut);
+        MCK(cudaGetLastError());
     }
-    MCK(cudaGetLastError());
     MCK(cudaEventRecord(b, m->stream));
     MCK(cudaEventSynchronize(b));
-    if (m->tensor_path == 1) {
-        int st = 0;
-        MCK(cudaMemcpy(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost));
-        if (st) return mfail(m, st, "swgpu_mlp_predict: tensor-core wait timed out");
-    }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    if ((rc = read_status(m, "swgpu_mlp_predict"))) return rc;
     if (elapsed_ms) *elapsed_ms = ms;
     return SWGPU_OK;
 }
 
 int swgpu_mlp_gradients(void *handle, const int64_t *rows, int64_t nrows, float w_depth,
-                        float w_arrival, float *outputs, float *grad, float *loss) {
+                        float w_arrival, float w_error, float *outputs, float *grad,
+                        float *loss) {
     Mlp *m = static_cast<Mlp *>(handle);
     if (!m || !rows || nrows <= 0 || !m->targets)
         return mfail(m, SWGPU_EINVAL, "swgpu_mlp_gradients: bad argument or no targets");
+    if (int rc = usable(m, "swgpu_mlp_gradients")) return rc;
+    for (int64_t i = 0; i < nrows; i++)
+        if (rows[i] < 0 || rows[i] >= m->S * m->N)
+            return mfail(m, SWGPU_EINVAL, "swgpu_mlp_gradients: row %lld out of range",
+                         (long long)rows[i]);
     int rc;
     if (nrows > m->rows_cap) {
         if ((rc = malloc_dev(m, &m->rows, (size_t)nrows))) return rc;
@@ -1004,9 +1011,9 @@ int swgpu_mlp_gradients(void *handle, const int64_t *rows, int64_t nrows, float 
     }
     MCK(cudaMemcpyAsync(m->rows, rows, sizeof(long long) * nrows, cudaMemcpyHostToDevice,
                         m->stream));
-    if ((rc = batch_gradients(m, m->rows, 0, nrows, m->S * m->N, w_depth, w_arrival))) return rc;
+    if ((rc = batch_gradients(m, m->rows, 0, nrows, w_depth, w_arrival, w_error))) return rc;
     if (outputs)
-        MCK(cudaMemcpyAsync(outputs, m->scratch.y, sizeof(float) * kOut * nrows,
+        MCK(cudaMemcpyAsync(outputs, m->buf.y, sizeof(float) * kOut * nrows,
                             cudaMemcpyDeviceToHost, m->stream));
     if (grad)
         MCK(cudaMemcpyAsync(grad, m->grad, sizeof(float) * kNumParams, cudaMemcpyDeviceToHost,
@@ -1014,14 +1021,16 @@ int swgpu_mlp_gradients(void *handle, const int64_t *rows, int64_t nrows, float 
     if (loss)
         MCK(cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->stream));
     MCK(cudaStreamSynchronize(m->stream));
-    return SWGPU_OK;
+    return read_status(m, "swgpu_mlp_gradients");
 }
 
 int swgpu_mlp_train(void *handle, int steps, int64_t batch, uint64_t seed, float lr,
-                    float w_depth, float w_arrival, float *last_loss, float *elapsed_ms) {
+                    float w_depth, float w_arrival, float w_error, float *last_loss,
+                    float *elapsed_ms) {
     Mlp *m = static_cast<Mlp *>(handle);
     if (!m || steps <= 0 || batch <= 0 || !m->targets)
         return mfail(m, SWGPU_EINVAL, "swgpu_mlp_train: bad argument or no targets");
+    if (int rc = usable(m, "swgpu_mlp_train")) return rc;
     cudaEvent_t a, b;
     MCK(cudaEventCreate(&a));
     MCK(cudaEventCreate(&b));
@@ -1029,14 +1038,14 @@ int swgpu_mlp_train(void *handle, int steps, int64_t batch, uint64_t seed, float
     const float b1 = 0.9f, b2 = 0.999f;
     for (int s = 0; s < steps; s++) {
         const unsigned long long step_seed = seed * 0x9E3779B97F4A7C15ull + (unsigned)s;
-        int rc = batch_gradients(m, nullptr, step_seed, batch, m->S * m->N, w_depth, w_arrival);
+        int rc = batch_gradients(m, nullptr, step_seed, batch, w_depth, w_arrival, w_error);
         if (rc) return rc;
         m->adam_t++;
         const float c1 = 1.f / (1.f - powf(b1, (float)m->adam_t));
         const float c2 = 1.f / (1.f - powf(b2, (float)m->adam_t));
-        mlp_adam<<<(kNumParams + 255) / 256, 256, 0, m->stream>>>(
+        mlp_adam<<<(unsigned)((kNumParams + 255) / 256), 256, 0, m->stream>>>(
             m->params, m->grad, m->adam_m, m->adam_v, kNumParams, lr, b1, b2, 1e-8f, c1, c2);
-        mlp_pack_weights<<<(kH * kS2 + 255) / 256, 256, 0, m->stream>>>(m->params, m->w);
+        mlp_pack_weights<<<(kH * kH + 255) / 256, 256, 0, m->stream>>>(m->params, m->w);
     }
     MCK(cudaGetLastError());
     MCK(cudaEventRecord(b, m->stream));
@@ -1045,6 +1054,7 @@ int swgpu_mlp_train(void *handle, int steps, int64_t batch, uint64_t seed, float
     cudaEventElapsedTime(&ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    if (int rc = read_status(m, "swgpu_mlp_train")) return rc;
     if (elapsed_ms) *elapsed_ms = ms;
     if (last_loss) MCK(cudaMemcpy(last_loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost));
     return SWGPU_OK;
@@ -1058,14 +1068,6 @@ int swgpu_mlp_get_params(void *handle, float *params) {
     return SWGPU_OK;
 }
 
-int swgpu_mlp_num_params(void) { return kNumParams; }
-
-int swgpu_mlp_set_tensor_path(void *handle, int path) {
-    Mlp *m = static_cast<Mlp *>(handle);
-    if (!m || (path != 0 && path != 1))
-        return mfail(m, SWGPU_EINVAL, "swgpu_mlp_set_tensor_path: 0 (mma.sync) or 1 (tcgen05)");
-    m->tensor_path = path;
-    return SWGPU_OK;
-}
+int swgpu_mlp_num_params(void) { return (int)kNumParams; }
 
 }  // extern "C"

@@ -248,42 +248,47 @@ int swgpu_set_tracking(void *handle, int on, double threshold);
 int swgpu_get_tracking(void *handle, float *max_depth, float *arrival_time);
 
 /* ---- BF16 MLP surrogate (swgpu_mlp_*) ---------------------------------
- * A 16 -> 128 -> 128 -> 2 ReLU network predicting per (scenario, triangle)
- * row the normalised maximum depth and arrival time from 9 scenario
- * parameters and the triangle's bed, centroid and distance to the source;
- * BF16 weights and activations on mma.sync tensor cores with FP32
- * accumulation, FP32 master weights trained by Adam.  params is the flat
- * FP32 vector W1 [16][128], b1 [128], W2 [128][128], b2 [128], W3 [128][2],
- * b3 [2] (swgpu_mlp_num_params() floats, in-major weights); the feature
- * map is (raw - mean) * inv_std over 16 features (the last 3 are zero).
- * Handles use the current device and their own stream.  No counterpart in
- * the reference. */
+ * A 16 -> 256 -> 256 -> 256 -> 3 ReLU network predicting per (scenario,
+ * triangle) row the normalised maximum depth, the normalised arrival time
+ * and an estimate of the first output's absolute error, from 9 scenario
+ * parameters and the triangle's centroid, bed and distance to the inflow.
+ * BF16 weights and activations, FP32 accumulation; every layer of width
+ * 256 runs as tcgen05.mma tiles (128 rows x 256 units) accumulating in
+ * tensor memory, in the forward and the backward pass; FP32 master weights
+ * trained by Adam.  params is the flat FP32 vector W1 [16][256], b1 [256],
+ * W2 [256][256], b2, W3 [256][256], b3, W4 [256][3], b4 [3]
+ * (swgpu_mlp_num_params() floats, in-major weights); the feature map is
+ * (raw - mean) * inv_std over 16 features (the last 3 are zero).  Handles
+ * use the current device and their own stream; a handle whose kernel
+ * reports SWGPU_ETIMEOUT is unusable (every later call fails).  No
+ * counterpart in the reference. */
 int swgpu_mlp_num_params(void);
 int swgpu_mlp_create(const float *params, const float *feature_mean,
                      const float *feature_inv_std, void **mlp_out);
 int swgpu_mlp_destroy(void *mlp);
 const char *swgpu_mlp_last_error(void *mlp);
-/* tri_xyz [ntri][3]: centroid x, y and bed; scen [nscen][9]; targets
- * [nscen][ntri][2] (may be NULL for prediction only). */
-int swgpu_mlp_set_data(void *mlp, const float *tri_xyz, int64_t ntri, const float *scen,
+/* tri [ntri][4]: centroid x, y, bed and distance to the inflow; scen
+ * [nscen][9]; targets [nscen][ntri][2] (normalised depth and arrival; may
+ * be NULL for prediction only). */
+int swgpu_mlp_set_data(void *mlp, const float *tri, int64_t ntri, const float *scen,
                        int64_t nscen, const float *targets);
 /* rows row0 .. row0+nrows-1 (row = scenario * ntri + triangle) into a
- * DEVICE buffer out [nrows][2]; *elapsed_ms (may be NULL) = kernel time. */
+ * DEVICE buffer out [nrows][3]; *elapsed_ms (may be NULL) = device time. */
 int swgpu_mlp_predict(void *mlp, int64_t row0, int64_t nrows, float *out_device,
                       float *elapsed_ms);
-/* Outputs [nrows][2], gradient of the loss (flat like params) and loss of
+/* Outputs [nrows][3], gradient of the loss (flat like params) and loss of
  * the given rows, without updating: mean over rows of
- * w_depth (y0 - t0)^2 + w_arrival (y1 - t1)^2. */
+ * w_depth (y0 - t0)^2 + w_arrival (y1 - t1)^2 + w_error (y2 - |y0 - t0|)^2,
+ * with |y0 - t0| held constant in the last term (the error estimate learns
+ * the depth output's error without changing it). */
 int swgpu_mlp_gradients(void *mlp, const int64_t *rows, int64_t nrows, float w_depth,
-                        float w_arrival, float *outputs, float *grad, float *loss);
+                        float w_arrival, float w_error, float *outputs, float *grad,
+                        float *loss);
 /* steps Adam steps on random batches of batch rows (seeded). */
 int swgpu_mlp_train(void *mlp, int steps, int64_t batch, uint64_t seed, float lr,
-                    float w_depth, float w_arrival, float *last_loss, float *elapsed_ms);
+                    float w_depth, float w_arrival, float w_error, float *last_loss,
+                    float *elapsed_ms);
 int swgpu_mlp_get_params(void *mlp, float *params);
-/* Inference kernel of swgpu_mlp_predict: 0 = mma.sync (default), 1 =
- * tcgen05 (both hidden layers as 128 x 128 tcgen05.mma chains from shared
- * memory into tensor memory). */
-int swgpu_mlp_set_tensor_path(void *mlp, int path);
 
 /* Frees everything the handle owns.  No counterpart in the reference (its
  * PyCUDA allocations are released by the garbage collector). */

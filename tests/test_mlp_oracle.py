@@ -17,13 +17,12 @@ from oracle import mlp_oracle as MO
 def _problem(seed, nscen=3, ntri=7, nrows=11):
     rng = np.random.default_rng(seed)
     scen = rng.uniform(-1.0, 1.0, (nscen, MO.NP)).astype(np.float32)
-    tri = rng.uniform(-2.0, 2.0, (ntri, 3)).astype(np.float32)
+    tri = rng.uniform(-2.0, 2.0, (ntri, 4)).astype(np.float32)
     rows = rng.choice(nscen * ntri, nrows, replace=False)
-    targets = rng.normal(size=(nscen * ntri, MO.OUT))
+    targets = rng.normal(size=(nscen * ntri, MO.NT))
     mu = rng.normal(size=MO.F).astype(np.float32) * 0.1
     isd = rng.uniform(0.5, 2.0, MO.F).astype(np.float32)
-    sizes = MO.F * MO.H + MO.H + MO.H * MO.H + MO.H + MO.H * MO.OUT + MO.OUT
-    params = rng.normal(size=sizes) * 0.2
+    params = rng.normal(size=MO.NUM_PARAMS) * 0.1
     return params, scen, tri, rows, targets, mu, isd
 
 
@@ -49,14 +48,18 @@ def test_backward_matches_finite_differences(monkeypatch):
     params, scen, tri, rows, targets, mu, isd = _problem(7)
     # the biases are read as float32: keep them exactly representable
     P = MO.unflatten(params)
-    for b in ("b1", "b2", "b3"):
+    for b in ("b1", "b2", "b3", "b4"):
         P[b][...] = P[b].astype(np.float32)
     params = MO.flatten(P)
-    _, loss, grad = MO.forward_backward(params, scen, tri, rows, targets, mu, isd, 1.0, 0.5)
+    y0, loss, grad = MO.forward_backward(params, scen, tri, rows, targets, mu, isd, 1.0, 0.5,
+                                         0.7)
+    # the error term's target |y0 - t0| is a constant of the gradient: hold it
+    t0 = np.asarray(targets).reshape(-1, MO.NT)[rows, 0]
+    frozen = np.abs(y0[:, 0] - t0)
     rng = np.random.default_rng(3)
     # every block of the flat vector: weights and biases of each layer
     o, picks = 0, []
-    for shape in ((MO.F, MO.H), (MO.H,), (MO.H, MO.H), (MO.H,), (MO.H, MO.OUT), (MO.OUT,)):
+    for _, shape in MO.SHAPES:
         n = int(np.prod(shape))
         picks += list(o + rng.choice(n, min(n, 6), replace=False))
         o += n
@@ -68,16 +71,18 @@ def test_backward_matches_finite_differences(monkeypatch):
         up, dn = params.copy(), params.copy()
         up[j] += h
         dn[j] -= h
-        lu = MO.forward_backward(up, scen, tri, rows, targets, mu, isd, 1.0, 0.5)[1]
-        ld = MO.forward_backward(dn, scen, tri, rows, targets, mu, isd, 1.0, 0.5)[1]
+        lu = MO.forward_backward(up, scen, tri, rows, targets, mu, isd, 1.0, 0.5, 0.7,
+                                 frozen_error=frozen)[1]
+        ld = MO.forward_backward(dn, scen, tri, rows, targets, mu, isd, 1.0, 0.5, 0.7,
+                                 frozen_error=frozen)[1]
         fd = (lu - ld) / (2.0 * h)
         assert fd == pytest.approx(grad[j], rel=1e-5, abs=1e-9 * max(1.0, loss)), j
 
 
 def test_features_hand_computed_row():
     scen = np.zeros((2, MO.NP), np.float32)
-    scen[1] = [0.5, 3.0, 4.0, 1.0, 2.0, 0.03, 0.1, 0.2, 0.3]   # centre (3, 4)
-    tri = np.array([[0.0, 0.0, -1.0], [6.0, 8.0, 2.5]], np.float32)
+    scen[1] = [300.0, 900.0, 2000.0, 0.03, 0.1, 0.2, -0.3, 0.05, 0.0]
+    tri = np.array([[0.0, 0.0, -1.0, 10.0], [6.0, 8.0, 2.5, 5.0]], np.float32)
     mu = np.zeros(MO.F, np.float32)
     isd = np.ones(MO.F, np.float32)
     mu[12], isd[12] = 1.0, 0.5
@@ -85,5 +90,5 @@ def test_features_hand_computed_row():
     assert f.dtype == np.float32 and f.shape == (1, MO.F)
     assert np.array_equal(f[0, :MO.NP], scen[1])
     assert (f[0, 9], f[0, 10], f[0, 11]) == (2.5, 6.0, 8.0)
-    assert f[0, 12] == np.float32((5.0 - 1.0) * 0.5)          # distance to the centre is 5
+    assert f[0, 12] == np.float32((5.0 - 1.0) * 0.5)          # distance to the inflow is 5
     assert np.all(f[0, 13:] == 0.0)

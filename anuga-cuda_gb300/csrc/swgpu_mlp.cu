@@ -8,7 +8,7 @@
 //   16 -> 256 -> 256 -> 256 -> 3  (ReLU after each hidden layer)
 // with weights and activations in BF16 and every product accumulated in
 // FP32; its outputs are the normalised maximum depth, the normalised
-// arrival time and an estimate of the first output's absolute error.
+// arrival time and the 90% quantile of the first output's absolute error.
 //
 // Every GEMM of the forward and backward passes is the one kernel
 // tc_gemm: a CTA of 4 warps computes a 128 x N tile (N = 256 or 16) of
@@ -50,6 +50,7 @@ constexpr int kOut = 3;      // outputs: depth, arrival time, depth-error estima
 constexpr int kTargets = 2;  // targets per row: depth, arrival time
 constexpr int kParams = 9;   // scenario parameters
 constexpr int kTri = 4;      // per-triangle table: x, y, z, distance to the inflow
+constexpr float kQuantile = 0.9f;  // quantile of the depth error the third output learns
 
 // flat FP32 parameter vector, weights in-major ([in][out]):
 // W1 [16][256], b1, W2 [256][256], b2, W3 [256][256], b3, W4 [256][3], b4
@@ -496,8 +497,9 @@ __global__ void __launch_bounds__(256) mlp_head_predict(const __nv_bfloat16 *__r
 // Training head: outputs, loss, dL/dy and the gradient into layer 3,
 // dz3 = (dy W4^T) * relu'(h3), stored row-major and feature-major; the
 // output layer's own gradients (W4, b4) are summed per block.  loss =
-// mean over rows of w_d (y0 - t0)^2 + w_a (y1 - t1)^2 + w_e (y2 - |y0 - t0|)^2,
-// the error estimate's target |y0 - t0| taken as a constant.
+// mean over rows of w_d (y0 - t0)^2 + w_a (y1 - t1)^2 + w_e rho(|y0 - t0| - y2),
+// rho the pinball loss of the kQuantile quantile, so that y2 learns that
+// quantile of the depth output's absolute error (taken as a constant).
 __global__ void __launch_bounds__(256) mlp_head_train(
     const __nv_bfloat16 *__restrict__ h3, const BfWeights *W, const float *params,
     const float *__restrict__ targets, const long long *__restrict__ row_of, long long nrows,
@@ -524,14 +526,15 @@ __global__ void __launch_bounds__(256) mlp_head_train(
             head_forward(h3 + r * kH, W, params + kOffB4, hv, y);
             const float *t = targets + row_of[r] * kTargets;
             const float e0 = y[0] - t[0], e1 = y[1] - t[1];
-            const float e2 = y[2] - fabsf(e0);
+            const float u = fabsf(e0) - y[2];
+            const float pin = u >= 0.f ? kQuantile * u : (kQuantile - 1.f) * u;
             const float d0 = 2.f * w_d * e0 * inv_b, d1 = 2.f * w_a * e1 * inv_b,
-                        d2 = 2.f * w_e * e2 * inv_b;
+                        d2 = w_e * (u < 0.f ? 1.f - kQuantile : -kQuantile) * inv_b;
             if (lane == 0) {
                 y_out[r * kOut] = y[0];
                 y_out[r * kOut + 1] = y[1];
                 y_out[r * kOut + 2] = y[2];
-                atomicAdd(&lsum, (w_d * e0 * e0 + w_a * e1 * e1 + w_e * e2 * e2) * inv_b);
+                atomicAdd(&lsum, (w_d * e0 * e0 + w_a * e1 * e1 + w_e * pin) * inv_b);
                 atomicAdd(&gb4[0], d0);
                 atomicAdd(&gb4[1], d1);
                 atomicAdd(&gb4[2], d2);

@@ -100,6 +100,8 @@ def parse():
     ap.add_argument("--surrogate-test", type=int, default=512)
     ap.add_argument("--surrogate-cal", type=int, default=256)
     ap.add_argument("--surrogate-steps", type=int, default=20000)
+    ap.add_argument("--surrogate-only", action="store_true",
+                    help="measure only the surrogate workflow (one JSON line of its own)")
     return ap.parse_args()
 
 
@@ -628,6 +630,11 @@ def main():
         line = run_reference(args, rank, world)
         if line is not None:
             print(json.dumps(line))
+        return
+    if args.surrogate_only:
+        if rank == 0:
+            print(json.dumps({"metric": "surrogate time to answer within 5 cm vs solver alone",
+                              "surrogate": run_surrogate(args)}))
         return
     sc = build_workload(args.cells)
     out = run_ours(args, rank, world, local, sc)

@@ -250,7 +250,7 @@ int swgpu_get_tracking(void *handle, float *max_depth, float *arrival_time);
 /* ---- BF16 MLP surrogate (swgpu_mlp_*) ---------------------------------
  * A 16 -> 256 -> 256 -> 256 -> 3 ReLU network predicting per (scenario,
  * triangle) row the normalised maximum depth, the normalised arrival time
- * and an estimate of the first output's absolute error, from 9 scenario
+ * and the 90% quantile of the first output's absolute error, from 9 scenario
  * parameters and the triangle's centroid, bed and distance to the inflow.
  * BF16 weights and activations, FP32 accumulation; every layer of width
  * 256 runs as tcgen05.mma tiles (128 rows x 256 units) accumulating in
@@ -278,9 +278,10 @@ int swgpu_mlp_predict(void *mlp, int64_t row0, int64_t nrows, float *out_device,
                       float *elapsed_ms);
 /* Outputs [nrows][3], gradient of the loss (flat like params) and loss of
  * the given rows, without updating: mean over rows of
- * w_depth (y0 - t0)^2 + w_arrival (y1 - t1)^2 + w_error (y2 - |y0 - t0|)^2,
- * with |y0 - t0| held constant in the last term (the error estimate learns
- * the depth output's error without changing it). */
+ * w_depth (y0 - t0)^2 + w_arrival (y1 - t1)^2 + w_error rho(|y0 - t0| - y2),
+ * rho(u) = u (0.9 - [u < 0]) the pinball loss of the 90% quantile, with
+ * |y0 - t0| held constant (the error estimate learns that quantile of the
+ * depth output's error without changing it). */
 int swgpu_mlp_gradients(void *mlp, const int64_t *rows, int64_t nrows, float w_depth,
                         float w_arrival, float w_error, float *outputs, float *grad,
                         float *loss);

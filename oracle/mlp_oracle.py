@@ -12,15 +12,17 @@ BF16; the gradient of each hidden layer's pre-activation is rounded to BF16
 bias gradients are sums of those rounded values.
 
 Loss (mean over the rows): w_d (y0 - t0)^2 + w_a (y1 - t1)^2 +
-w_e (y2 - |y0 - t0|)^2, where the third output learns the first one's
-absolute error: |y0 - t0| is held constant in its term (no gradient flows
-through it into y0).
+w_e rho(|y0 - t0| - y2), rho(u) = u (q - [u < 0]) the pinball loss of the
+quantile q = 0.9, so that the third output learns that quantile of the first
+one's absolute error: |y0 - t0| is held constant in its term (no gradient
+flows through it into y0).
 """
 from __future__ import annotations
 
 import numpy as np
 
 F, H, OUT, NT, NP = 16, 256, 3, 2, 9
+QUANTILE = 0.9
 SHAPES = (("W1", (F, H)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)),
           ("b3", (H,)), ("W4", (H, OUT)), ("b4", (OUT,)))
 NUM_PARAMS = sum(int(np.prod(s)) for _, s in SHAPES)
@@ -87,9 +89,11 @@ def forward_backward(params, scen, tri, rows, targets, mu, isd, w_depth=1.0, w_a
     e0 = y[:, 0] - t[:, 0]
     e1 = y[:, 1] - t[:, 1]
     err = np.abs(e0) if frozen_error is None else np.asarray(frozen_error, np.float64)
-    e2 = y[:, 2] - err
-    loss = float(np.sum(w_depth * e0 * e0 + w_arrival * e1 * e1 + w_error * e2 * e2) / n)
-    dy = np.stack([2.0 * w_depth * e0, 2.0 * w_arrival * e1, 2.0 * w_error * e2], axis=1) / n
+    u = err - y[:, 2]
+    pin = np.where(u >= 0, QUANTILE * u, (QUANTILE - 1.0) * u)
+    loss = float(np.sum(w_depth * e0 * e0 + w_arrival * e1 * e1 + w_error * pin) / n)
+    d2 = w_error * np.where(u < 0, 1.0 - QUANTILE, -QUANTILE)
+    dy = np.stack([2.0 * w_depth * e0, 2.0 * w_arrival * e1, d2], axis=1) / n
     dz3 = bf16((dy @ W[3].T) * (h3 > 0))
     dz2 = bf16((dz3 @ W[2].T) * (h2 > 0))
     dz1 = bf16((dz2 @ W[1].T) * (h1 > 0))

@@ -32,7 +32,7 @@ on a window of the mesh: east of the westmost flagged block and, in y, the
 span of the flagged blocks and the inflow segment, each with a margin.  The
 window's west cut carries the tide delayed by the long-wave travel time to
 it (the sea's still level there, the tide being slow), its north and south
-cuts are walls.  Leaving out the deep sea, which sets the solver's CFL
+cuts are transmissive.  Leaving out the deep sea, which sets the solver's CFL
 step, the window needs several times fewer steps as well as fewer
 triangles.  The window's values replace the predictions in the flagged
 blocks.  ``evaluate`` reports the
@@ -48,7 +48,7 @@ import numpy as np
 from . import _lib
 from ._lib import lib
 from .boundaries import (Inflow_hydrograph_boundary, Reflective_boundary,
-                         Time_stage_fourier_boundary)
+                         Time_stage_fourier_boundary, Transmissive_boundary)
 from .config import DEFAULT
 from .ensemble import ALIGN, Ensemble
 from .mesh import Mesh, rectangular_cross
@@ -131,7 +131,7 @@ def _boundaries(theta):
                                                 period=TIDE_PERIOD),
             "inflow": Inflow_hydrograph_boundary(peak=peak, rise=rise, fall=dur - rise),
             "right": Reflective_boundary(), "top": Reflective_boundary(),
-            "bottom": Reflective_boundary(), "exterior": Reflective_boundary()}
+            "bottom": Reflective_boundary(), "exterior": Transmissive_boundary()}
 
 
 def family_scenario(fm: FamilyMesh, theta, finaltime=FINALTIME, mesh=None, zv=None):
@@ -400,8 +400,8 @@ def window_mesh(fm: FamilyMesh, xlo, ylo, yhi):
     """The sub-mesh of triangles with centroid x >= xlo and y in [ylo, yhi]:
     (mesh, vertex bed, family index of each sub-mesh triangle).  Boundary
     edges keep their family tags; cut edges facing west (toward the sea) are
-    tagged "cut_west", the other cut edges are reflective walls
-    ("exterior")."""
+    tagged "cut_west", the other cut edges "exterior" (transmissive: the
+    flood passes out of the window instead of reflecting back in)."""
     sel = (fm.xy[:, 0] >= xlo) & (fm.xy[:, 1] >= ylo) & (fm.xy[:, 1] <= yhi)
     idx = np.nonzero(sel)[0]
     local = -np.ones(fm.N, np.int64)
@@ -426,7 +426,7 @@ def window_scenario(fm: FamilyMesh, theta, xlo, ylo, yhi, cache=None):
     xlo (the whole width when xlo is 0) and within [ylo, yhi], with the sea
     at rest at the boundary's initial stage.  Its west cut carries the
     boundary's stage delayed by the long-wave travel time to xlo (wave_lag),
-    the sea's still level there; the north and south cuts are walls."""
+    the sea's still level there; the north and south cuts are transmissive."""
     cache = {} if cache is None else cache
     key = (xlo, ylo, yhi)
     if key not in cache:
@@ -443,7 +443,7 @@ def window_scenario(fm: FamilyMesh, theta, xlo, ylo, yhi, cache=None):
     return sc, fam_idx
 
 
-def window_scenarios(fm: FamilyMesh, thetas, flagged, margin=1000.0, quantum=500.0,
+def window_scenarios(fm: FamilyMesh, thetas, flagged, margin=1500.0, quantum=500.0,
                      block=ALIGN, cache=None):
     """For each scenario with flagged blocks ([S][nblocks] bool): its window
     (east of the westmost flagged block, and in y the span of the flagged
@@ -468,7 +468,7 @@ def window_scenarios(fm: FamilyMesh, thetas, flagged, margin=1000.0, quantum=500
     return out
 
 
-def fallback(fm: FamilyMesh, thetas, depth, err_est, k, tol=0.05, margin=1000.0, batch=32,
+def fallback(fm: FamilyMesh, thetas, depth, err_est, k, tol=0.05, margin=1500.0, batch=32,
              block=ALIGN, precision="mixed"):
     """The answer within ``tol``: predictions where the calibrated error
     estimate allows, window re-solves elsewhere.  Returns (depth [S][N],
@@ -491,7 +491,7 @@ def fallback(fm: FamilyMesh, thetas, depth, err_est, k, tol=0.05, margin=1000.0,
 
 
 def evaluate(fm: FamilyMesh, thetas, true_depth, solver_ms, pred_depth, err_est, infer_ms, k,
-             tol=0.05, margin=1000.0, block=ALIGN):
+             tol=0.05, margin=1500.0, block=ALIGN):
     """Time to an answer within ``tol`` (inference + window re-solves, device
     time) against the solver alone on the same scenarios, and the answer's
     error against the full solve."""

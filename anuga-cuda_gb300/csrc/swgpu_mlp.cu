@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256) mlp_features(FeatureTables F, const long 
 
 constexpr int kTileM = 128;  // rows per CTA (TMEM lanes)
 constexpr int kChunkK = 64;  // K per stage
-constexpr int kGemmThreads = 128;
+constexpr int kGemmThreads = 256;  // 8 warps: the epilogue splits the columns in two
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -277,11 +277,11 @@ __device__ __forceinline__ void cp_async_wait() {
 __device__ __forceinline__ void stage_operand(unsigned dst, const __nv_bfloat16 *src, long ld,
                                               long long r0, long long nvalid, int R, long k0,
                                               int kc) {
-    const int kvn = kc >> 3;       // 16-byte vectors per row in the chunk
-    const int nvec = R * kvn;
+    const int lg = kc == kChunkK ? 3 : 1;  // log2 of the 16-byte vectors per row (kc 64 or 16)
+    const int nvec = R << lg;
     for (int v = threadIdx.x; v < nvec; v += kGemmThreads) {
-        const int r = (v & 7) + 8 * (v / (8 * kvn));
-        const int kv = (v >> 3) % kvn;
+        const int r = (v & 7) + ((v >> (3 + lg)) << 3);
+        const int kv = (v >> 3) & ((1 << lg) - 1);
         const long long row = r0 + r;
         const bool in = row < nvalid;
         const __nv_bfloat16 *p = in ? src + row * ld + k0 + 8 * kv : src;
@@ -305,7 +305,8 @@ struct GemmArgs {
     __nv_bfloat16 *out_row;          // hidden/dgrad: [M][N]
     __nv_bfloat16 *out_col;          // hidden/dgrad: [N][ldc] (may be null)
     long ldc;
-    float *grad;                     // wgrad: [M][N] (or [N][M] transposed)
+    float *grad;                     // wgrad: partials [splits][M][N] (or [splits][N][M]
+                                     // transposed), one slice per blockIdx.y
     int *status;
 };
 
@@ -329,19 +330,30 @@ __device__ __forceinline__ void gemm_epilogue(const GemmArgs &g, long long row, 
                                               const float (&v)[W]) {
     if (row >= g.M) return;
     if (EPI == kEpiWgrad) {
+        float4 *dst = reinterpret_cast<float4 *>(g.grad + (long long)blockIdx.y * g.M * N +
+                                                 row * N + c0);
 #pragma unroll
-        for (int j = 0; j < W; j++) atomicAdd(&g.grad[row * N + c0 + j], v[j]);
+        for (int q = 0; q < W / 4; q++)
+            dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
         return;
     }
     if (EPI == kEpiWgradT) {
+        float *dst = g.grad + (long long)blockIdx.y * g.M * N;
 #pragma unroll
-        for (int j = 0; j < W; j++) atomicAdd(&g.grad[(long long)(c0 + j) * g.M + row], v[j]);
+        for (int j = 0; j < W; j++) dst[(long long)(c0 + j) * g.M + row] = v[j];
         return;
     }
     __align__(16) __nv_bfloat16 o[W];
     if (EPI == kEpiHidden) {
+        const float4 *bp = reinterpret_cast<const float4 *>(g.bias + c0);
 #pragma unroll
-        for (int j = 0; j < W; j++) o[j] = __float2bfloat16(fmaxf(v[j] + g.bias[c0 + j], 0.0f));
+        for (int q = 0; q < W / 4; q++) {
+            const float4 b = __ldg(bp + q);
+            o[4 * q] = __float2bfloat16(fmaxf(v[4 * q] + b.x, 0.0f));
+            o[4 * q + 1] = __float2bfloat16(fmaxf(v[4 * q + 1] + b.y, 0.0f));
+            o[4 * q + 2] = __float2bfloat16(fmaxf(v[4 * q + 2] + b.z, 0.0f));
+            o[4 * q + 3] = __float2bfloat16(fmaxf(v[4 * q + 3] + b.w, 0.0f));
+        }
     } else {  // dgrad: the ReLU mask of the activations this layer read
         __align__(16) __nv_bfloat16 pm[W];
         const int4 *src = reinterpret_cast<const int4 *>(g.mask + row * N + c0);
@@ -363,7 +375,7 @@ __device__ __forceinline__ void gemm_epilogue(const GemmArgs &g, long long row, 
 // C (128 x N tile) = A (tile rows) x B^T over this CTA's K range, then the
 // epilogue.  blockIdx.x: row tile; blockIdx.y: K split (weight gradients).
 template <int N, int EPI>
-__global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm(GemmArgs g) {
+__global__ void __launch_bounds__(kGemmThreads, 2) tc_gemm(GemmArgs g) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     GemmSmem<N> &S = *reinterpret_cast<GemmSmem<N> *>(
         smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u));
@@ -387,6 +399,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm(GemmArgs g) {
     tc_fence_after();
     const unsigned tmem = S.tmem_base;
     const int kc = g.K < kChunkK ? (int)g.K : kChunkK;  // 64, or 16 for K = 16
+    // every K range is non-empty: the host launches ceil(K / k_per_split)
+    // splits
     const int nk = (int)((ke - kb + kc - 1) / kc);
     constexpr unsigned idesc = tc_idesc(N);
     auto issue = [&](int c) {
@@ -431,19 +445,20 @@ __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm(GemmArgs g) {
         cp_async_wait<0>();
         if (nk > 0) cta_wait(&S.bar[(nk - 1) & 1], ((nk - 1) >> 1) & 1);
     } else {
+        // warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows; a warp may only
+        // reach its own quarter of the lanes) and half w / 4 of the columns
         tc_fence_after();
-        const long long row = m0 + 32 * warp + lane;
-        const unsigned lane_addr = tmem + ((unsigned)(32 * warp) << 16);
-        if (nk == 0) {
-            // an empty K range (a split past the end): nothing to add
-        } else if (N >= 32) {
+        const int quarter = warp & 3, half = warp >> 2;
+        const long long row = m0 + 32 * quarter + lane;
+        const unsigned lane_addr = tmem + ((unsigned)(32 * quarter) << 16);
+        if (N >= 64) {
 #pragma unroll 1
-            for (int c0 = 0; c0 < N; c0 += 32) {
+            for (int c0 = half * (N / 2); c0 < (half + 1) * (N / 2); c0 += 32) {
                 float v[32];
                 tc_ld32(lane_addr + c0, v);
                 gemm_epilogue<N, EPI, 32>(g, row, c0, v);
             }
-        } else {
+        } else if (half == 0) {
             float v[16];
             tc_ld16(lane_addr, v);
             gemm_epilogue<N, EPI, 16>(g, row, 0, v);
@@ -518,6 +533,12 @@ __global__ void __launch_bounds__(256) mlp_head_train(
     __syncthreads();
     const float inv_b = 1.0f / (float)nrows;
     const long long rb = (long long)blockIdx.x * kHeadRows;
+    // this lane's share of the output layer's gradients over the warp's rows
+    float gw[8][kOut], gb[kOut] = {0.f, 0.f, 0.f}, ls = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+#pragma unroll
+        for (int o = 0; o < kOut; o++) gw[j][o] = 0.f;
     for (int i = warp; i < kHeadRows; i += 8) {
         const long long r = rb + i;
         __align__(16) __nv_bfloat16 dz[8];
@@ -534,10 +555,10 @@ __global__ void __launch_bounds__(256) mlp_head_train(
                 y_out[r * kOut] = y[0];
                 y_out[r * kOut + 1] = y[1];
                 y_out[r * kOut + 2] = y[2];
-                atomicAdd(&lsum, (w_d * e0 * e0 + w_a * e1 * e1 + w_e * pin) * inv_b);
-                atomicAdd(&gb4[0], d0);
-                atomicAdd(&gb4[1], d1);
-                atomicAdd(&gb4[2], d2);
+                ls += (w_d * e0 * e0 + w_a * e1 * e1 + w_e * pin) * inv_b;
+                gb[0] += d0;
+                gb[1] += d1;
+                gb[2] += d2;
             }
 #pragma unroll
             for (int j = 0; j < 8; j++) {
@@ -547,15 +568,24 @@ __global__ void __launch_bounds__(256) mlp_head_train(
                 const float w2 = __bfloat162float(W->w4[c * kOut + 2]);
                 const float g = fmaf(d0, w0, fmaf(d1, w1, d2 * w2));
                 dz[j] = __float2bfloat16(hv[j] > 0.f ? g : 0.f);
-                atomicAdd(&gw4[c * kOut], hv[j] * d0);
-                atomicAdd(&gw4[c * kOut + 1], hv[j] * d1);
-                atomicAdd(&gw4[c * kOut + 2], hv[j] * d2);
+                gw[j][0] += hv[j] * d0;
+                gw[j][1] += hv[j] * d1;
+                gw[j][2] += hv[j] * d2;
             }
         } else {
 #pragma unroll
             for (int j = 0; j < 8; j++) dz[j] = __float2bfloat16(0.f);
         }
         *reinterpret_cast<int4 *>(&tile[i][8 * lane]) = *reinterpret_cast<const int4 *>(dz);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+#pragma unroll
+        for (int o = 0; o < kOut; o++) atomicAdd(&gw4[(8 * lane + j) * kOut + o], gw[j][o]);
+    if (lane == 0) {
+        atomicAdd(&lsum, ls);
+#pragma unroll
+        for (int o = 0; o < kOut; o++) atomicAdd(&gb4[o], gb[o]);
     }
     __syncthreads();
     // row-major rows of the block (rows up to Bp: the padding is zero)
@@ -578,15 +608,24 @@ __global__ void __launch_bounds__(256) mlp_head_train(
     if (threadIdx.x == 0) atomicAdd(loss, lsum);
 }
 
-// Bias gradients: sum over the batch of each feature-major gradient row.
+// Bias gradients: sum over the batch of each feature-major gradient row,
+// each row split over gridDim.y blocks (8 rows per thread and step, as one
+// 16-byte load).
 __global__ void __launch_bounds__(256) mlp_bias_grad(const __nv_bfloat16 *__restrict__ dz_col,
                                                      long long Bp, int nfeat,
                                                      float *__restrict__ gb) {
     const int f = blockIdx.x;
     if (f >= nfeat) return;
     float s = 0.f;
-    const __nv_bfloat16 *p = dz_col + (long long)f * Bp;
-    for (long long r = threadIdx.x; r < Bp; r += blockDim.x) s += __bfloat162float(p[r]);
+    const int4 *p = reinterpret_cast<const int4 *>(dz_col + (long long)f * Bp);
+    const long long nv = Bp / 8;  // Bp is a multiple of the 128-row tile
+    for (long long q = blockIdx.y * (long long)blockDim.x + threadIdx.x; q < nv;
+         q += (long long)gridDim.y * blockDim.x) {
+        const int4 u = p[q];
+        const __nv_bfloat16 *b = reinterpret_cast<const __nv_bfloat16 *>(&u);
+#pragma unroll
+        for (int j = 0; j < 8; j++) s += __bfloat162float(b[j]);
+    }
     __shared__ float sh[256];
     sh[threadIdx.x] = s;
     __syncthreads();
@@ -594,7 +633,19 @@ __global__ void __launch_bounds__(256) mlp_bias_grad(const __nv_bfloat16 *__rest
         if ((int)threadIdx.x < t) sh[threadIdx.x] += sh[threadIdx.x + t];
         __syncthreads();
     }
-    if (threadIdx.x == 0) gb[f] += sh[0];
+    if (threadIdx.x == 0) atomicAdd(&gb[f], sh[0]);
+}
+
+// Weight gradient from its per-split partials: out[i] += sum over s of
+// part[s][i] (the splits of the batch, in a fixed order).
+__global__ void __launch_bounds__(256) mlp_sum_partials(const float *__restrict__ part,
+                                                        int splits, long n,
+                                                        float *__restrict__ out) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int k = 0; k < splits; k++) s += part[(long)k * n + i];
+    out[i] += s;
 }
 
 // ---- weights ----------------------------------------------------------------
@@ -641,7 +692,11 @@ struct Buffers {  // one batch of rows (training) or one chunk (inference)
     __nv_bfloat16 *d3 = nullptr, *d2 = nullptr, *d3c = nullptr, *d2c = nullptr, *d1c = nullptr;
     long long *row_of = nullptr;
     float *y = nullptr;
+    float *part = nullptr;  // weight-gradient partials [splits][256 x 256]
 };
+
+// Batch rows per K split of the weight-gradient GEMMs.
+constexpr long kWgradRows = 512;
 
 struct Mlp {
     int device = 0;
@@ -721,7 +776,9 @@ int ensure_buffers(Mlp *m, long long rows, bool train, std::vector<void *> &owne
             (rc = malloc_dev(m, &B.d3, hr, &owned)) || (rc = malloc_dev(m, &B.d2, hr, &owned)) ||
             (rc = malloc_dev(m, &B.d3c, hr, &owned)) || (rc = malloc_dev(m, &B.d2c, hr, &owned)) ||
             (rc = malloc_dev(m, &B.d1c, hr, &owned)) ||
-            (rc = malloc_dev(m, &B.row_of, (size_t)cap, &owned)))
+            (rc = malloc_dev(m, &B.row_of, (size_t)cap, &owned)) ||
+            (rc = malloc_dev(m, &B.part, (size_t)((cap + kWgradRows - 1) / kWgradRows) * kH * kH,
+                             &owned)))
             return rc;
     }
     B.cap = cap;
@@ -787,9 +844,6 @@ int forward(Mlp *m, long long Bp, bool train) {
     return SWGPU_OK;
 }
 
-// Batch rows per K split of the weight-gradient GEMMs.
-constexpr long kWgradRows = 1024;
-
 // Forward, backward and the gradient vector of nrows rows (Bp padded).
 int batch_gradients(Mlp *m, const long long *d_rows, unsigned long long seed, long long nrows,
                     float w_d, float w_a, float w_e) {
@@ -807,13 +861,20 @@ int batch_gradients(Mlp *m, const long long *d_rows, unsigned long long seed, lo
         B.h3, W, m->params, m->targets, B.row_of, nrows, Bp, w_d, w_a, w_e, B.y, B.d3, B.d3c,
         m->grad, m->loss);
     MCK(cudaGetLastError());
+    // weight gradients: one partial per split of the batch, then their sum
     const int splits = (int)((Bp + kWgradRows - 1) / kWgradRows);
+    const dim3 bias_grid(kH, 16);
+    auto sum_parts = [&](long n, long off) {
+        mlp_sum_partials<<<(unsigned)((n + 255) / 256), 256, 0, m->stream>>>(B.part, splits, n,
+                                                                            m->grad + off);
+    };
     // layer 3: gW3 = H2^T dZ3 (in x out), gb3; dZ2 = (dZ3 W3^T) * relu'(H2)
     GemmArgs g = gemm_args(m, B.h2c, Bp, B.d3c, Bp, kH, Bp);
     g.k_per_split = kWgradRows;
-    g.grad = m->grad + kOffW3;
+    g.grad = B.part;
     if ((rc = launch_gemm<kH, kEpiWgrad>(m, g, splits))) return rc;
-    mlp_bias_grad<<<kH, 256, 0, m->stream>>>(B.d3c, Bp, kH, m->grad + kOffB3);
+    sum_parts((long)kH * kH, kOffW3);
+    mlp_bias_grad<<<bias_grid, 256, 0, m->stream>>>(B.d3c, Bp, kH, m->grad + kOffB3);
     g = gemm_args(m, B.d3, kH, W->w3, kH, Bp, kH);
     g.mask = B.h2;
     g.out_row = B.d2;
@@ -823,9 +884,10 @@ int batch_gradients(Mlp *m, const long long *d_rows, unsigned long long seed, lo
     // layer 2: gW2 = H1^T dZ2, gb2; dZ1 = (dZ2 W2^T) * relu'(H1)
     g = gemm_args(m, B.h1c, Bp, B.d2c, Bp, kH, Bp);
     g.k_per_split = kWgradRows;
-    g.grad = m->grad + kOffW2;
+    g.grad = B.part;
     if ((rc = launch_gemm<kH, kEpiWgrad>(m, g, splits))) return rc;
-    mlp_bias_grad<<<kH, 256, 0, m->stream>>>(B.d2c, Bp, kH, m->grad + kOffB2);
+    sum_parts((long)kH * kH, kOffW2);
+    mlp_bias_grad<<<bias_grid, 256, 0, m->stream>>>(B.d2c, Bp, kH, m->grad + kOffB2);
     g = gemm_args(m, B.d2, kH, W->w2, kH, Bp, kH);
     g.mask = B.h1;
     g.out_row = B.d3;  // dZ1 row-major is not needed again: B.d3 is free
@@ -835,9 +897,10 @@ int batch_gradients(Mlp *m, const long long *d_rows, unsigned long long seed, lo
     // layer 1: gW1^T = dZ1^T X (out x in), stored transposed into W1 [in][out]; gb1
     g = gemm_args(m, B.d1c, Bp, B.xc, Bp, kH, Bp);
     g.k_per_split = kWgradRows;
-    g.grad = m->grad + kOffW1;
+    g.grad = B.part;
     if ((rc = launch_gemm<kF, kEpiWgradT>(m, g, splits))) return rc;
-    mlp_bias_grad<<<kH, 256, 0, m->stream>>>(B.d1c, Bp, kH, m->grad + kOffB1);
+    sum_parts((long)kF * kH, kOffW1);
+    mlp_bias_grad<<<bias_grid, 256, 0, m->stream>>>(B.d1c, Bp, kH, m->grad + kOffB1);
     MCK(cudaGetLastError());
     return SWGPU_OK;
 }

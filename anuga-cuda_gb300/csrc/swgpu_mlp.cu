@@ -476,8 +476,9 @@ __global__ void __launch_bounds__(kGemmThreads, 2) tc_gemm(GemmArgs g) {
 
 constexpr int kHeadRows = 32;  // rows per block: one warp per row, 8 warps
 
-// y = H3 W4 + b4 for each row; the 8 columns of lane l are 8l .. 8l+7.
-__device__ __forceinline__ void head_forward(const __nv_bfloat16 *h, const BfWeights *W,
+// y = H3 W4 + b4 for each row; the 8 columns of lane l are 8l .. 8l+7;
+// w4 is the block's shared copy of W4 ([in][out], BF16).
+__device__ __forceinline__ void head_forward(const __nv_bfloat16 *h, const __nv_bfloat16 *w4,
                                              const float *b4, float (&hv)[8], float (&y)[kOut]) {
     const int lane = threadIdx.x & 31;
     __align__(16) __nv_bfloat16 hb[8];
@@ -488,7 +489,7 @@ __device__ __forceinline__ void head_forward(const __nv_bfloat16 *h, const BfWei
         hv[j] = __bfloat162float(hb[j]);
 #pragma unroll
         for (int o = 0; o < kOut; o++)
-            acc[o] = fmaf(hv[j], __bfloat162float(W->w4[(8 * lane + j) * kOut + o]), acc[o]);
+            acc[o] = fmaf(hv[j], __bfloat162float(w4[(8 * lane + j) * kOut + o]), acc[o]);
     }
 #pragma unroll
     for (int o = 0; o < kOut; o++) {
@@ -498,15 +499,22 @@ __device__ __forceinline__ void head_forward(const __nv_bfloat16 *h, const BfWei
     }
 }
 
+constexpr int kPredictRows = 64;  // rows per block of the inference head: 8 per warp
+
 __global__ void __launch_bounds__(256) mlp_head_predict(const __nv_bfloat16 *__restrict__ h3,
                                                         const BfWeights *W, const float *params,
                                                         long long nrows, float *__restrict__ out) {
+    __shared__ __nv_bfloat16 w4[kH * kOut];
+    for (int i = threadIdx.x; i < kH * kOut; i += blockDim.x) w4[i] = W->w4[i];
+    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long r = (long long)blockIdx.x * 8 + warp;
-    if (r >= nrows) return;
-    float hv[8], y[kOut];
-    head_forward(h3 + r * kH, W, params + kOffB4, hv, y);
-    if (lane < kOut) out[r * kOut + lane] = y[lane];
+    for (int i = warp; i < kPredictRows; i += 8) {
+        const long long r = (long long)blockIdx.x * kPredictRows + i;
+        if (r >= nrows) break;
+        float hv[8], y[kOut];
+        head_forward(h3 + r * kH, w4, params + kOffB4, hv, y);
+        if (lane < kOut) out[r * kOut + lane] = y[lane];
+    }
 }
 
 // Training head: outputs, loss, dL/dy and the gradient into layer 3,
@@ -524,10 +532,14 @@ __global__ void __launch_bounds__(256) mlp_head_train(
     // rows padded by 16 bytes: the feature-major pass reads down a column
     __shared__ __align__(16) __nv_bfloat16 tile[kHeadRows][kH + 8];
     __shared__ float gw4[kH * kOut];
+    __shared__ __nv_bfloat16 w4[kH * kOut];
     __shared__ float gb4[kOut];
     __shared__ float lsum;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < kH * kOut; i += blockDim.x) gw4[i] = 0.f;
+    for (int i = threadIdx.x; i < kH * kOut; i += blockDim.x) {
+        gw4[i] = 0.f;
+        w4[i] = W->w4[i];
+    }
     if (threadIdx.x < kOut) gb4[threadIdx.x] = 0.f;
     if (threadIdx.x == 0) lsum = 0.f;
     __syncthreads();
@@ -544,7 +556,7 @@ __global__ void __launch_bounds__(256) mlp_head_train(
         __align__(16) __nv_bfloat16 dz[8];
         if (r < nrows) {
             float hv[8], y[kOut];
-            head_forward(h3 + r * kH, W, params + kOffB4, hv, y);
+            head_forward(h3 + r * kH, w4, params + kOffB4, hv, y);
             const float *t = targets + row_of[r] * kTargets;
             const float e0 = y[0] - t[0], e1 = y[1] - t[1];
             const float u = fabsf(e0) - y[2];
@@ -563,9 +575,9 @@ __global__ void __launch_bounds__(256) mlp_head_train(
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int c = 8 * lane + j;
-                const float w0 = __bfloat162float(W->w4[c * kOut]);
-                const float w1 = __bfloat162float(W->w4[c * kOut + 1]);
-                const float w2 = __bfloat162float(W->w4[c * kOut + 2]);
+                const float w0 = __bfloat162float(w4[c * kOut]);
+                const float w1 = __bfloat162float(w4[c * kOut + 1]);
+                const float w2 = __bfloat162float(w4[c * kOut + 2]);
                 const float g = fmaf(d0, w0, fmaf(d1, w1, d2 * w2));
                 dz[j] = __float2bfloat16(hv[j] > 0.f ? g : 0.f);
                 gw[j][0] += hv[j] * d0;
@@ -643,9 +655,17 @@ __global__ void __launch_bounds__(256) mlp_sum_partials(const float *__restrict_
                                                         float *__restrict__ out) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float s = 0.f;
-    for (int k = 0; k < splits; k++) s += part[(long)k * n + i];
-    out[i] += s;
+    // four independent running sums (loads in flight together), fixed order
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int k = 0;
+    for (; k + 4 <= splits; k += 4) {
+        s0 += part[(long)k * n + i];
+        s1 += part[(long)(k + 1) * n + i];
+        s2 += part[(long)(k + 2) * n + i];
+        s3 += part[(long)(k + 3) * n + i];
+    }
+    for (; k < splits; k++) s0 += part[(long)k * n + i];
+    out[i] += (s0 + s1) + (s2 + s3);
 }
 
 // ---- weights ----------------------------------------------------------------
@@ -1044,7 +1064,7 @@ int swgpu_mlp_predict(void *handle, int64_t row0, int64_t nrows, float *out_devi
         mlp_features<<<(unsigned)((Bp + 255) / 256), 256, 0, m->stream>>>(
             tables(m), nullptr, 0, 0, row0 + r0, n, Bp, m->buf.xr, nullptr, nullptr);
         if ((rc = forward(m, Bp, false))) return rc;
-        mlp_head_predict<<<(unsigned)((n + 7) / 8), 256, 0, m->stream>>>(
+        mlp_head_predict<<<(unsigned)((n + kPredictRows - 1) / kPredictRows), 256, 0, m->stream>>>(
             m->buf.h3, m->w, m->params, n, out_device + r0 * kOut);
         MCK(cudaGetLastError());
     }

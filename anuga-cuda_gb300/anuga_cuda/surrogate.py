@@ -32,7 +32,7 @@ on a window of the mesh: east of the westmost flagged block and, in y, the
 span of the flagged blocks and the inflow segment, each with a margin.  The
 window's west cut carries the tide delayed by the long-wave travel time to
 it (the sea's still level there, the tide being slow), its north and south
-cuts are transmissive.  Leaving out the deep sea, which sets the solver's CFL
+cuts are walls.  Leaving out the deep sea, which sets the solver's CFL
 step, the window needs several times fewer steps as well as fewer
 triangles.  The window's values replace the predictions in the flagged
 blocks.  ``evaluate`` reports the
@@ -48,7 +48,7 @@ import numpy as np
 from . import _lib
 from ._lib import lib
 from .boundaries import (Inflow_hydrograph_boundary, Reflective_boundary,
-                         Time_stage_fourier_boundary, Transmissive_boundary)
+                         Time_stage_fourier_boundary)
 from .config import DEFAULT
 from .ensemble import ALIGN, Ensemble
 from .mesh import Mesh, rectangular_cross
@@ -131,7 +131,7 @@ def _boundaries(theta):
                                                 period=TIDE_PERIOD),
             "inflow": Inflow_hydrograph_boundary(peak=peak, rise=rise, fall=dur - rise),
             "right": Reflective_boundary(), "top": Reflective_boundary(),
-            "bottom": Reflective_boundary(), "exterior": Transmissive_boundary()}
+            "bottom": Reflective_boundary(), "exterior": Reflective_boundary()}
 
 
 def family_scenario(fm: FamilyMesh, theta, finaltime=FINALTIME, mesh=None, zv=None):
@@ -400,8 +400,7 @@ def window_mesh(fm: FamilyMesh, xlo, ylo, yhi):
     """The sub-mesh of triangles with centroid x >= xlo and y in [ylo, yhi]:
     (mesh, vertex bed, family index of each sub-mesh triangle).  Boundary
     edges keep their family tags; cut edges facing west (toward the sea) are
-    tagged "cut_west", the other cut edges "exterior" (transmissive: the
-    flood passes out of the window instead of reflecting back in)."""
+    tagged "cut_west", the other cut edges "exterior" (reflective walls)."""
     sel = (fm.xy[:, 0] >= xlo) & (fm.xy[:, 1] >= ylo) & (fm.xy[:, 1] <= yhi)
     idx = np.nonzero(sel)[0]
     local = -np.ones(fm.N, np.int64)
@@ -426,7 +425,9 @@ def window_scenario(fm: FamilyMesh, theta, xlo, ylo, yhi, cache=None):
     xlo (the whole width when xlo is 0) and within [ylo, yhi], with the sea
     at rest at the boundary's initial stage.  Its west cut carries the
     boundary's stage delayed by the long-wave travel time to xlo (wave_lag),
-    the sea's still level there; the north and south cuts are transmissive."""
+    the sea's still level there; the north and south cuts are walls, far
+    enough (the margin) from the flagged blocks that their reflections stay
+    small there."""
     cache = {} if cache is None else cache
     key = (xlo, ylo, yhi)
     if key not in cache:

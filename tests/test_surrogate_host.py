@@ -16,7 +16,10 @@ def fm():
 def test_family_mesh_tags_and_features(fm):
     m = fm.mesh
     assert set(m.tag_names) == {"bottom", "inflow", "left", "right", "top"}
-    assert m.tag_length("inflow") == pytest.approx(1000.0, rel=0.2)
+    # the east-edge cells whose edge midpoints fall in [4.5, 5.5] km (the
+    # hydrograph's discharge is spread over the tag's actual length)
+    cell = fm.length / 32
+    assert abs(m.tag_length("inflow") - 1000.0) <= cell
     assert fm.tri.shape == (fm.N, 4) and fm.tri.dtype == np.float32
     # the distance to the inflow segment is zero only on the east edge's segment
     east = fm.xy[:, 0] > fm.length - fm.length / 32
@@ -54,9 +57,9 @@ def test_static_depth_under_the_lagged_tide(fm):
     w0 = th[:, 4] + th[:, 6] + th[:, 8]
     wm = SG.max_tide(th)
     sea = fm.zc < -5.0
-    level = d[:, sea] + fm.zc[sea][None, :]
-    assert np.all(level >= w0[:, None] - 1e-6)
-    assert np.all(level <= wm[:, None] + 1e-6)
+    level = d[:, sea] + fm.zc[sea][None, :]     # d is float32: ~1e-5 m at 80 m depth
+    assert np.all(level >= w0[:, None] - 1e-4)
+    assert np.all(level <= wm[:, None] + 1e-4)
     # the lag grows toward the shore
     lag = SG.wave_lag(fm, 0.0)
     order = np.argsort(fm.xy[:, 0])

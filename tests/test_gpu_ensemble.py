@@ -64,3 +64,41 @@ def test_per_method_refused_on_ensemble(swgpu_built):
     assert lib().swgpu_compute_fluxes(ens._h, C.byref(ft)) != 0
     n = C.c_int()
     assert lib().swgpu_ensemble_size(ens._h, C.byref(n)) == 0 and n.value == 2
+
+
+def test_finished_scenario_costs_little_per_step(swgpu_built):
+    """A scenario that has reached its finaltime while another runs on: its
+    blocks read the halt flag and return without fetching their tiles.  Here
+    it comes first in the launch (the deeper water sorts it first), so every
+    launch still covers it; its cost per step, the ensemble's step minus the
+    running scenario's own step, stays a small fraction of a live step of the
+    same size (CUDA events around the graph launches)."""
+    import ctypes as C
+    from anuga_cuda import DEFAULT, _lib, scenarios
+    from anuga_cuda._lib import check, f64p, lib
+    from anuga_cuda.ensemble import Ensemble
+    a = scenarios.wet_dry(m=250, seed=3)
+    a.stage_centroid = a.stage_centroid + 1.0     # deeper: the smallest timestep, first
+    b = scenarios.wet_dry(m=250, seed=5)
+
+    def timed(ens, finals, warm, steps):
+        ft = ens._internal(np.asarray(finals, np.float64))
+        check(lib().swgpu_evolve_start(ens._h, 0.0, 1.0e6, 1.0e6), ens._h)
+        check(lib().swgpu_ensemble_set_finaltimes(ens._h, f64p(ft)), ens._h)
+        st, ms = _lib.State_t(), C.c_double()
+        check(lib().swgpu_evolve_run_timed(ens._h, warm, C.byref(st), C.byref(ms)), ens._h)
+        best = None
+        for _ in range(3):
+            check(lib().swgpu_evolve_run_timed(ens._h, steps, C.byref(st), C.byref(ms)), ens._h)
+            best = ms.value if best is None else min(best, ms.value)
+        return best / steps
+
+    both = Ensemble([a, b], DEFAULT, "mixed")
+    assert both.order == [0, 1]                  # the finishing scenario is first
+    t_both = timed(both, [1.0, 1.0e6], 48, 96)
+    assert both.states()[0].stop_reason == 2 and both.states()[1].stop_reason != 2
+    alone = Ensemble([b], DEFAULT, "mixed")
+    t_b = timed(alone, [1.0e6], 48, 96)
+    halted = t_both - t_b
+    print(f"running step {t_b * 1e3:.1f} us, with a finished scenario {t_both * 1e3:.1f} us")
+    assert halted <= 0.15 * t_b, (t_both, t_b)

@@ -1,6 +1,6 @@
 """The BF16 surrogate network on the tcgen05 tensor cores: forward outputs
-and loss gradients against the NumPy FP64 restatement (relative error
-within BF16 epsilon x sqrt(fan-in)), inference equal to the training
+and loss gradients against the NumPy FP64 restatement (outputs within one
+BF16 epsilon, gradients within a quarter of it), inference equal to the training
 forward bit for bit, training that lowers the loss, and the solver-trained
 surrogate with the solver as fallback on a small family mesh: its answer
 within the depth tolerance, sooner than the solver alone."""
@@ -9,7 +9,13 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = 2.0 ** -8 * np.sqrt(256)      # BF16 epsilon x sqrt(fan-in)
+# What the GPU and the FP64 oracle (same BF16 rounding points) are held to,
+# well inside BF16 epsilon x sqrt(fan-in) = 0.0625:
+# the outputs within one BF16 epsilon (an activation's rounding may flip),
+# the gradients within a quarter of it (measured: outputs 7e-4, gradients
+# 2e-6 .. 5e-5 relative to each block's largest entry).
+TOL_OUT = 2.0 ** -8
+TOL_GRAD = 2.0 ** -10
 
 
 @pytest.fixture(scope="module")
@@ -41,11 +47,14 @@ def test_gradients_match_oracle(small_family, swgpu_built):
     y, loss, g = sg.gradients(rows, 1.0, 0.5, 0.3)
     yo, losso, go = MO.forward_backward(sg.params(), th, fm.tri, rows, targets, sg.mu, sg.isd,
                                         1.0, 0.5, 0.3)
-    assert np.max(np.abs(y - yo)) <= TOL * np.max(np.abs(yo))
-    assert abs(loss - losso) <= TOL * losso
+    dev = {"outputs": np.max(np.abs(y - yo)) / np.max(np.abs(yo))}
     for name, o, n in _blocks():
         ref = go[o:o + n]
-        assert np.max(np.abs(g[o:o + n] - ref)) <= TOL * np.max(np.abs(ref)), name
+        dev[name] = np.max(np.abs(g[o:o + n] - ref)) / np.max(np.abs(ref))
+    print({k: f"{v:.2e}" for k, v in dev.items()})
+    assert abs(loss - losso) <= TOL_OUT * losso
+    assert dev.pop("outputs") <= TOL_OUT
+    assert all(v <= TOL_GRAD for v in dev.values()), dev
 
 
 def test_predict_equals_training_forward(small_family, swgpu_built):

@@ -2,8 +2,9 @@
 and loss gradients against the NumPy FP64 restatement (outputs within one
 BF16 epsilon, gradients within a quarter of it), inference equal to the training
 forward bit for bit, training that lowers the loss, and the solver-trained
-surrogate with the solver as fallback on a small family mesh: its answer
-within the depth tolerance, sooner than the solver alone."""
+surrogate with the solver as fallback on the family mesh: its answer within
+the depth tolerance in more blocks than the predictions alone, sooner than
+the solver alone."""
 import numpy as np
 import pytest
 

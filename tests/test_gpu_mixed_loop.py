@@ -29,7 +29,7 @@ def test_mixed_yields_and_steps_match_fp64(method, swgpu_built):
     # the step counts agree to the one step per yield interval that an FP32
     # CFL bound can shift at a yield clamp
     assert abs(nmx - n64) <= 5, (nmx, n64)
-    assert np.max(np.abs(wmx - w64)) <= 1e-4 * np.max(np.abs(w64))
+    assert np.max(np.abs(wmx - w64)) <= 1e-6 * np.max(np.abs(w64))   # measured 2e-8 .. 5e-8
 
 
 @pytest.mark.parametrize("method", ["euler", "rk2", "rk3"])

@@ -91,7 +91,7 @@ def test_mixed_close_to_fp64_on_harbour(swgpu_built):
     sb = b.evolve_steps(300)
     assert abs(sa.time - sb.time) <= 1e-5 * sa.time
     err = max_rel(b.quantities["stage"].centroid_values, a.quantities["stage"].centroid_values)
-    assert err < 1e-4, err
+    assert err < 1e-6, err   # measured 1.8e-7
 
 
 def test_nan_input_reports_status(swgpu_built):
@@ -143,7 +143,7 @@ def test_inflow_hydrograph_volume(precision, swgpu_built):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_transmissive_outflow_and_mixed_close(precision, swgpu_built):
     """The channel with all its open boundaries: runs clean in both
-    precisions, and the mixed precision stays within 1e-4 of FP64."""
+    precisions, and the mixed precision stays within 1e-6 of FP64."""
     from anuga_cuda import DEFAULT, scenarios
     sc = scenarios.channel_inflow(40, 12, seed=4, peak=1.0, rise=2.0)
     runs = {}
@@ -152,7 +152,7 @@ def test_transmissive_outflow_and_mixed_close(precision, swgpu_built):
         st = d.evolve_steps(400)
         assert st.status == 0
         runs[prec] = d.quantities["stage"].centroid_values
-    assert max_rel(runs[precision], runs["fp64"]) < 1e-4
+    assert max_rel(runs[precision], runs["fp64"]) < 1e-6   # measured 9e-8
 
 
 def test_limiter_variants_need_fp64(swgpu_built):

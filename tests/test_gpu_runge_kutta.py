@@ -112,7 +112,8 @@ def test_rk_mixed_close_to_fp64(method, swgpu_built):
         assert st.status == 0
         runs[prec] = d.quantities["stage"].centroid_values
     w64 = runs["fp64"]
-    assert np.max(np.abs(runs["mixed"] - w64)) / np.max(np.abs(w64)) < 1e-4
+    # measured 1.5e-7 (rk2), 1.1e-7 (rk3)
+    assert np.max(np.abs(runs["mixed"] - w64)) / np.max(np.abs(w64)) < 1e-6
 
 
 def test_method_switch_and_bad_method(swgpu_built):

@@ -325,9 +325,20 @@ __host__ __device__ constexpr int tmem_cols() {
 
 // The epilogue of one 32-column slice c0 .. c0+31 (or 16 for N = 16) of
 // this thread's row.
+// Row stride (elements) of the BF16 output tile staged in shared memory:
+// 129 words, so that a warp writing one row per lane, or reading 32
+// consecutive words of one row, touches 32 different banks.
+template <int N>
+constexpr int kStageStride = N + 2;
+
+// The epilogue of one 32-column slice c0 .. c0+31 (or 16 for N = 16) of
+// this thread's row (trow within the tile).  Weight gradients go straight to
+// their partial; activations and gradients of activations are written as
+// BF16 pairs into the shared-memory tile, stored to global memory by
+// gemm_store_tile.
 template <int N, int EPI, int W>
-__device__ __forceinline__ void gemm_epilogue(const GemmArgs &g, long long row, int c0,
-                                              const float (&v)[W]) {
+__device__ __forceinline__ void gemm_epilogue(const GemmArgs &g, long long row, int trow, int c0,
+                                              const float (&v)[W], __nv_bfloat16 *stile) {
     if (row >= g.M) return;
     if (EPI == kEpiWgrad) {
         float4 *dst = reinterpret_cast<float4 *>(g.grad + (long long)blockIdx.y * g.M * N +
@@ -363,12 +374,46 @@ __device__ __forceinline__ void gemm_epilogue(const GemmArgs &g, long long row, 
         for (int j = 0; j < W; j++)
             o[j] = __float2bfloat16(__bfloat162float(pm[j]) > 0.0f ? v[j] : 0.0f);
     }
-    int4 *dst = reinterpret_cast<int4 *>(g.out_row + row * N + c0);
+    unsigned *t32 = reinterpret_cast<unsigned *>(stile + trow * kStageStride<N> + c0);
 #pragma unroll
-    for (int q = 0; q < W / 8; q++) dst[q] = reinterpret_cast<const int4 *>(o)[q];
-    if (g.out_col) {
+    for (int j = 0; j < W / 2; j++) t32[j] = reinterpret_cast<const unsigned *>(o)[j];
+}
+
+// Stores the staged 128 x N BF16 tile: row-major (each warp writes whole
+// rows, 32 consecutive words per instruction) and, when asked,
+// feature-major (each warp writes one feature's 128 rows as 4-byte pairs,
+// 128 bytes per instruction).
+template <int N>
+__device__ __forceinline__ void gemm_store_tile(const GemmArgs &g, long long m0,
+                                                const __nv_bfloat16 *stile) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int TW = kStageStride<N> / 2;  // words per staged row
+    const unsigned *t32 = reinterpret_cast<const unsigned *>(stile);
+    for (int r = warp; r < kTileM; r += kGemmThreads / 32) {
+        const long long grow = m0 + r;
+        if (grow >= g.M) break;
+        unsigned *dst = reinterpret_cast<unsigned *>(g.out_row + grow * N);
 #pragma unroll
-        for (int j = 0; j < W; j++) g.out_col[(long long)(c0 + j) * g.ldc + row] = o[j];
+        for (int j = lane; j < N / 2; j += 32) dst[j] = t32[r * TW + j];
+    }
+    if (!g.out_col) return;
+    for (int c = warp; c < N; c += kGemmThreads / 32) {
+#pragma unroll
+        for (int p = 0; p < kTileM / 64; p++) {
+            const int r = 64 * p + 2 * lane;
+            const long long grow = m0 + r;
+            __nv_bfloat16 *dst = g.out_col + (long long)c * g.ldc + grow;
+            const __nv_bfloat16 a = stile[r * kStageStride<N> + c];
+            const __nv_bfloat16 b = stile[(r + 1) * kStageStride<N> + c];
+            if (grow + 1 < g.M) {
+                __nv_bfloat162 pair;
+                pair.x = a;
+                pair.y = b;
+                *reinterpret_cast<__nv_bfloat162 *>(dst) = pair;
+            } else if (grow < g.M) {
+                *dst = a;
+            }
+        }
     }
 }
 
@@ -449,19 +494,30 @@ __global__ void __launch_bounds__(kGemmThreads, 2) tc_gemm(GemmArgs g) {
         // reach its own quarter of the lanes) and half w / 4 of the columns
         tc_fence_after();
         const int quarter = warp & 3, half = warp >> 2;
-        const long long row = m0 + 32 * quarter + lane;
+        const int trow = 32 * quarter + lane;
+        const long long row = m0 + trow;
         const unsigned lane_addr = tmem + ((unsigned)(32 * quarter) << 16);
+        // the operand stages are free (every MMA has completed): the output
+        // tile is staged there
+        __nv_bfloat16 *stile = &S.a[0][0];
+        static_assert(EPI == kEpiWgrad || EPI == kEpiWgradT ||
+                          kTileM * kStageStride<N> * 2 <= sizeof(S.a) + sizeof(S.b),
+                      "staged tile fits in the operand stages");
         if (N >= 64) {
 #pragma unroll 1
             for (int c0 = half * (N / 2); c0 < (half + 1) * (N / 2); c0 += 32) {
                 float v[32];
                 tc_ld32(lane_addr + c0, v);
-                gemm_epilogue<N, EPI, 32>(g, row, c0, v);
+                gemm_epilogue<N, EPI, 32>(g, row, trow, c0, v, stile);
             }
         } else if (half == 0) {
             float v[16];
             tc_ld16(lane_addr, v);
-            gemm_epilogue<N, EPI, 16>(g, row, 0, v);
+            gemm_epilogue<N, EPI, 16>(g, row, trow, 0, v, stile);
+        }
+        if constexpr (EPI == kEpiHidden || EPI == kEpiDgrad) {
+            __syncthreads();
+            gemm_store_tile<N>(g, m0, stile);
         }
     }
     tc_fence_before();

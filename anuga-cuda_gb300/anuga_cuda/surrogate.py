@@ -1,5 +1,5 @@
 """BF16 surrogate of the solver's maximum depth and arrival time, with the
-solver as its fallback and judge.
+solver as its fallback and its check.
 
 The scenario family shares one mesh and bed: the wet/dry beach with bumps
 (a 1:100 beach rising to the east, the shoreline at x = 8 km, 40 seeded

@@ -456,6 +456,7 @@ __global__ void __launch_bounds__(kGemmThreads, 2) tc_gemm(GemmArgs g) {
         cp_async_commit();
     };
     bool ok = true;
+    int last = -1;  // the last chunk whose MMAs were committed
     if (nk > 0) issue(0);
     for (int c = 0; c < nk && ok; c++) {
         if (c + 1 < nk) {
@@ -480,15 +481,16 @@ __global__ void __launch_bounds__(kGemmThreads, 2) tc_gemm(GemmArgs g) {
                        smem_desc(b0 + 256u * kk, 128, sbo), idesc, c > 0 || kk > 0);
             tc_commit(&S.bar[s]);
         }
+        last = c;
     }
-    if (ok && nk > 0) ok = cta_wait(&S.bar[(nk - 1) & 1], ((nk - 1) >> 1) & 1);
+    if (ok && last >= 0) ok = cta_wait(&S.bar[last & 1], (last >> 1) & 1);
     if (!ok) {
         // status first; then let copies land (cp.async completes on its own)
-        // and give the MMAs in flight one more bounded wait before the
-        // columns are freed
+        // and give the MMAs in flight (up to the last committed chunk's) one
+        // more bounded wait before the columns are freed
         if (tid == 0) atomicExch(g.status, SWGPU_ETIMEOUT);
         cp_async_wait<0>();
-        if (nk > 0) cta_wait(&S.bar[(nk - 1) & 1], ((nk - 1) >> 1) & 1);
+        if (last >= 0) cta_wait(&S.bar[last & 1], (last >> 1) & 1);
     } else {
         // warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows; a warp may only
         // reach its own quarter of the lanes) and half w / 4 of the columns

@@ -686,3 +686,48 @@ class ReferenceKernels:
         for q in ["stage", "xmom", "ymom"]:
             self.q._interpolate_from_vertices_to_edges(
                 od.N, self._ptr(A[q + "_vertex_values"]), self._ptr(A[q + "_edge_values"]))
+
+
+# ------------------------------------------------- degenerate-timestep guard
+
+def degenerate_timestep_protection(max_speed, xmom, ymom, nbins=10):
+    """The reference's `apply_protection_against_isolated_degenerate_timesteps`
+    (src/anuga_cuda/gpu_domain_advanced.py:914-951) restated with plain loops:
+    when the fastest triangle exceeds 10 m/s and the histogram of max_speed
+    over 10 bins has an occupied last bin and empty bins 4 to 8, the momenta
+    of the triangles faster than the last bin's lower edge are zeroed (and
+    their max_speed).  The bins and counts are those of ANUGA's
+    ``numerical_tools.create_bins`` / ``histogram`` (ANUGA is a dependency
+    the reference does not vendor, version unpinned; restated from its
+    published definition): lower edges mn, mn + w, ... below mx, w = (mx -
+    mn) / nbins (the single edge mn when all speeds are equal); bin i counts
+    the speeds in [edge i, edge i+1), the last bin every speed from its edge
+    up.  Works on copies; returns (xmom, ymom, max_speed, zeroed indices)."""
+    ms = [float(v) for v in max_speed]
+    xm = [float(v) for v in xmom]
+    ym = [float(v) for v in ymom]
+    if not ms or max(ms) < 10.0:
+        return np.array(xm), np.array(ym), np.array(ms), []
+    mx, mn = max(ms), min(ms)
+    if mx == mn:
+        edges = [mn]
+    else:
+        w = (mx - mn) / nbins
+        # numpy.arange(mn, mx, w): ceil((mx - mn) / w) edges mn + i w
+        edges = [mn + i * w for i in range(int(np.ceil((mx - mn) / w)))]
+    hist = [0] * len(edges)
+    for v in ms:
+        b = -1
+        for j, e in enumerate(edges):
+            if v >= e:
+                b = j
+        if b >= 0:
+            hist[b] += 1
+    zeroed = []
+    if len(hist) > 1 and hist[-1] > 0 and all(hist[k] == 0 for k in range(4, 9)):
+        for k, v in enumerate(ms):
+            if v > edges[-1]:
+                xm[k] = ym[k] = 0.0
+                ms[k] = 0.0
+                zeroed.append(k)
+    return np.array(xm), np.array(ym), np.array(ms), zeroed

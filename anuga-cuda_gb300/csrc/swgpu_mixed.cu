@@ -369,7 +369,7 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
         const float n1 = nr.x, n2 = nr.y, L = __int_as_float(lq.x);
         const float4 el = T.es[i][tid];
         const float hl = el.x, dwl = el.y, uhl = el.z, vhl = el.w;
-        float hr, uhr, vhr, jump, rn = 3.0e38f;
+        float hr, uhr, vhr, jump;
         const int pki = lq.y;
         if (pki >= 0) {
             // the neighbour's stored edge state: the very numbers it uses
@@ -382,11 +382,9 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
             if ((unsigned)ln < (unsigned)cnt) {
                 en = T.es[m][ln];
                 wsn = T.ws[ln];
-                rn = T.rad[ln].x;
             } else {
                 en = ro(X.es + m * SP + n);
                 wsn = ro(X.ws + n);
-                rn = ro(reinterpret_cast<const float *>(X.rad + n));  // the radius only
             }
             wn = wsn.x;
             lnn = wsn.y;
@@ -410,8 +408,13 @@ __device__ __forceinline__ float flux_tile_triangle(const DevMixed &X, const Dev
         a0 -= f0 * L;
         a1 -= f1 * L;
         a2 -= f2 * L;
-        // min(rk/ms, rn/ms) = min(rk, rn)/ms: one division per edge
-        if (ms > eps) t = ominf(t, __fdividef(fminf(rk, rn), ms));
+        // ANUGA lowers the timestep by radii[k]/ms and radii[n]/ms at each
+        // edge (shallow_water_ext.c:4653-4664).  The neighbour n evaluates
+        // the same edge with the same two states and gets the same ms (the
+        // flux is exactly antisymmetric), so it contributes radii[n]/ms
+        // itself: over the mesh, each triangle's own radius gives the same
+        // minimum without the neighbour's radius being read.
+        if (ms > eps) t = ominf(t, __fdividef(rk, ms));
     }
     const float ghc = P.f_g * T.hf[tid];
     const float inv_area = T.rad[tid].y;
@@ -869,9 +872,10 @@ __global__ void __launch_bounds__(BS, 2048 / BS) distribute_mixed(DevMesh M, Dev
     int order;
     if (fused) {
         order = (int)ctrl->clk_order;
-        const bool first = blockIdx.x == 0 ||
-                           (M.blk_scen && M.blk_scen[(kb - 1) >> 8] != M.blk_scen[kb >> 8]);
-        if (first && tid == 0 && !halted) {
+        // the first block of each scenario (thread 0 alone reads the map)
+        if (tid == 0 && !halted &&
+            (blockIdx.x == 0 ||
+             (M.blk_scen && M.blk_scen[(kb - 1) >> 8] != M.blk_scen[kb >> 8]))) {
             commit_stage(ctrl, published_step_clock(ctrl), P, stg);
             announce_halt(ctrl);
         }

@@ -210,26 +210,32 @@ __device__ __forceinline__ void block_min_timestep(double t, Ctrl *ctrl) {
 }
 
 // FP32 variant for the mixed flux: the reduction stays in FP32 and only the
-// block's minimum is widened for the atomic.
+// block's minimum is widened for the atomic.  Non-negative floats (+inf
+// included) order as their bit patterns read as integers, so each warp takes
+// the minimum with one integer warp reduction; a NaN or negative timestep
+// maps to -1, which wins the minimum and raises the status.
 // ftmin_seen: the running minimum as read earlier by the block (default:
 // read it here, after the reduction).
+__device__ __forceinline__ int timestep_key(float t) {
+    return t >= 0.0f ? (__float_as_int(t) & 0x7fffffff) : -1;
+}
 template <int BLOCK = kBlock>
 __device__ __forceinline__ void block_min_timestep_f(float t, Ctrl *ctrl,
                                                      const unsigned long long *ftmin_seen =
                                                          nullptr) {
-    __shared__ float wminf[BLOCK / 32];
-    for (int o = 16; o > 0; o >>= 1) t = ominf(t, __shfl_xor_sync(0xffffffffu, t, o));
+    __shared__ int wmin[BLOCK / 32];
+    int key = __reduce_min_sync(0xffffffffu, timestep_key(t));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) wminf[warp] = t;
+    if (lane == 0) wmin[warp] = key;
     __syncthreads();
     if (warp == 0) {
-        t = lane < (int)(blockDim.x >> 5) ? wminf[lane] : 3.0e38f;
-        for (int o = 16; o > 0; o >>= 1) t = ominf(t, __shfl_xor_sync(0xffffffffu, t, o));
+        key = lane < (int)(blockDim.x >> 5) ? wmin[lane] : __float_as_int(3.0e38f);
+        key = __reduce_min_sync(0xffffffffu, key);
         if (lane == 0) {
-            if (!(t >= 0.0f)) {
+            if (key < 0) {
                 set_status(ctrl, SWGPU_ENONFINITE);
             } else {
-                const double td = (double)t;
+                const double td = (double)__int_as_float(key);
                 const unsigned long long bits = (unsigned long long)__double_as_longlong(td);
                 const unsigned long long seen =
                     ftmin_seen ? *ftmin_seen : *(volatile unsigned long long *)&ctrl->ftmin_bits;

@@ -137,6 +137,8 @@ def swcpu():
             getattr(L, name).restype = None
         L.swcpu_compute_fluxes.argtypes = [P]
         L.swcpu_compute_fluxes.restype = C.c_double
+        L.swcpu_edge_speeds.argtypes = [P, _d]
+        L.swcpu_edge_speeds.restype = C.c_int
         L.swcpu_update_conserved_quantities.argtypes = [P, C.c_double]
         L.swcpu_update_conserved_quantities.restype = C.c_int
         L.swcpu_update_timestep.argtypes = [P, C.c_double]
@@ -286,6 +288,14 @@ class OracleDomain:
 
     def compute_fluxes(self):
         return self.L.swcpu_compute_fluxes(self._ref())
+
+    def edge_speeds(self):
+        """Maximum wave speed of each (triangle, edge) from the triangle's own
+        side, [N, 3]; -1 where the dry-cell optimisation skips the edge."""
+        out = np.empty(3 * self.N)
+        if self.L.swcpu_edge_speeds(self._ref(), out.ctypes.data_as(_d)):
+            raise RuntimeError("discontinuous bed")
+        return out.reshape(-1, 3)
 
     def gravity_wb(self):
         self.L.swcpu_gravity_wb(self._ref())

@@ -238,6 +238,57 @@ double swcpu_compute_fluxes(swcpu_domain *D)
     return timestep;
 }
 
+/* The maximum wave speed of every edge evaluated from its own triangle's
+ * side, triangle-centric (each interior edge twice, once from each of its
+ * triangles), with the operations of swcpu_compute_fluxes: ms_out[3k + i],
+ * or -1 where the dry-cell optimisation skips the edge.  Test support for
+ * the timestep rule that lowers the timestep by each triangle's own radius
+ * only.  Returns nonzero on a discontinuous bed. */
+int swcpu_edge_speeds(const swcpu_domain *D, double *ms_out)
+{
+    const swcpu_params *P = D->params;
+    const long N = D->number_of_elements;
+    const double h0 = P->H0 * P->H0;
+    const double lim = 10 * P->H0;
+    double ql[3], qr[3], flux[3], zl, zr, ms;
+    long k, n, m, ki, nm;
+    int i;
+
+    for (k = 0; k < N; k++) {
+        for (i = 0; i < 3; i++) {
+            ki = 3 * k + i;
+            ql[0] = D->stage_edge_values[ki];
+            ql[1] = D->xmom_edge_values[ki];
+            ql[2] = D->ymom_edge_values[ki];
+            zl = D->bed_edge_values[ki];
+            n = D->neighbours[ki];
+            if (n < 0) {
+                m = -n - 1;
+                qr[0] = D->stage_boundary_values[m];
+                qr[1] = D->xmom_boundary_values[m];
+                qr[2] = D->ymom_boundary_values[m];
+                zr = zl;
+            } else {
+                nm = 3 * n + D->neighbour_edges[ki];
+                qr[0] = D->stage_edge_values[nm];
+                qr[1] = D->xmom_edge_values[nm];
+                qr[2] = D->ymom_edge_values[nm];
+                zr = D->bed_edge_values[nm];
+            }
+            if (P->optimise_dry_cells && fabs(ql[0] - zl) < P->epsilon &&
+                fabs(qr[0] - zr) < P->epsilon) {
+                ms_out[ki] = -1.0;
+                continue;
+            }
+            if (central_flux(ql, qr, zl, zr, D->normals[2 * ki], D->normals[2 * ki + 1], P,
+                             h0, lim, flux, &ms))
+                return 1;
+            ms_out[ki] = ms;
+        }
+    }
+    return 0;
+}
+
 /* src/anuga_HMPP/util_ext.h:66-108 (_gradient). */
 static void plane_gradient(double x0, double y0, double x1, double y1,
                            double x2, double y2, double q0, double q1,

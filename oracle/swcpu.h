@@ -112,6 +112,7 @@ typedef struct {
 } swcpu_domain;
 
 double swcpu_compute_fluxes(swcpu_domain *D);
+int swcpu_edge_speeds(const swcpu_domain *D, double *ms_out);
 void swcpu_gravity_wb(swcpu_domain *D);
 void swcpu_manning_friction(swcpu_domain *D);
 int swcpu_update_conserved_quantities(swcpu_domain *D, double dt);

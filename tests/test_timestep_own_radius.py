@@ -8,7 +8,9 @@ the timestep by its own triangle's radius only.  That gives the same number
 because the two evaluations of an edge see the same two states with the
 normal negated, so they produce bit-identical maximum speeds.  This test
 checks that symmetry edge by edge, and the resulting equality of the two
-minima, on the golden cases: at their initial state and after Euler steps."""
+minima, on the golden cases: at their initial state and after Euler steps.
+The kernel's block minimum is an integer warp reduction over the timesteps'
+bit patterns; the last test checks that key's order on the host."""
 import numpy as np
 import pytest
 
@@ -54,3 +56,30 @@ def test_own_radius_minimum_equals_anuga_rule(case, oracle_mod):
         od.update_boundary()
         wet_edges += _check_state(od)
     assert wet_edges > 0
+
+
+def _timestep_key(t):
+    """The mixed flux's integer key of an FP32 timestep: the bit pattern as a
+    signed integer for t >= 0 (sign bit cleared), -1 for NaN or t < 0."""
+    t = np.asarray(t, np.float32)
+    bits = t.view(np.int32) & np.int32(0x7FFFFFFF)
+    return np.where(t >= 0, bits, np.int32(-1)).astype(np.int32)
+
+
+def test_timestep_key_orders_as_the_floats():
+    rng = np.random.default_rng(5)
+    special = np.array([0.0, -0.0, np.inf, 3.0e38, np.finfo(np.float32).max,
+                        np.finfo(np.float32).tiny, 1e-45, 1.0, 0.5], np.float32)
+    for _ in range(200):
+        t = np.concatenate([rng.choice(special, 8),
+                            (10.0 ** rng.uniform(-40, 38, 56)).astype(np.float32)])
+        rng.shuffle(t)
+        k = _timestep_key(t)
+        # the minimum key is the key of the minimum timestep, and maps back to it
+        assert k.min() == _timestep_key(t.min())
+        assert np.array_equal(np.array([k.min()], np.int32).view(np.float32), [t.min()])
+        # a NaN or a negative timestep anywhere wins the minimum as -1
+        for bad in (np.nan, -1.0e-3, -np.inf):
+            u = t.copy()
+            u[rng.integers(len(u))] = bad
+            assert _timestep_key(u).min() == -1
